@@ -1,0 +1,199 @@
+"""GbaContext: the Python face of libgbattract's C ABI.
+
+A context owns device copies of proteins, grids and parameter tables (what
+the reference's DataManager + DeviceDataConfigurator hold per device,
+src/server/DataManager.cpp:23-101, src/server/DeviceDataConfigurator.tpp:28-362)
+and evaluates poses through the fused kernels.  Pose arrays may be numpy
+arrays (host) or torch tensors (host or CUDA); results come back in the same
+kind of array.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from .model import (DOF_MODES_WIDTH, DOF_WIDTH, RESULT_MODES_WIDTH, RESULT_WIDTH, GridOptions,
+                    GridSet, IntrplDesc, NLDesc, ParamTable, Protein)
+
+
+def _intrpl_c(d: IntrplDesc) -> _lib.IntrplDescC:
+    c = _lib.IntrplDescC()
+    c.numGrids = d.numGrids
+    for a in range(3):
+        c.dimN[a] = int(d.dimN[a])
+        c.posMin[a] = float(d.posMin[a])
+    c.gridSpacing = float(d.gridSpacing)
+    return c
+
+
+def _nl_c(d: NLDesc) -> _lib.NLDescC:
+    c = _lib.NLDescC()
+    for a in range(3):
+        c.dimN[a] = int(d.dimN[a])
+        c.posMin[a] = float(d.posMin[a])
+    c.gridSpacing = float(d.gridSpacing)
+    c.dPlateau = float(d.dPlateau)
+    c.numEl = int(d.numEl)
+    return c
+
+
+def grid_opts_c(opt: GridOptions) -> _lib.GridBuildOptsC:
+    c = _lib.GridBuildOptsC()
+    c.spacing = opt.spacing
+    c.plateau = opt.plateau
+    c.nl_cutoff = opt.nl_cutoff
+    c.margin = opt.margin
+    c.outer_ext = opt.outer_ext
+    c.n_alphabet = len(opt.alphabet)
+    for i, t in enumerate(opt.alphabet):
+        c.alphabet[i] = int(t)
+    return c
+
+
+def _is_torch(a) -> bool:
+    return hasattr(a, "data_ptr") and hasattr(a, "is_cuda")
+
+
+def _alloc_like(a, shape):
+    if _is_torch(a):
+        import torch
+        return torch.empty(shape, dtype=torch.float32, device=a.device)
+    return np.empty(shape, dtype=np.float32)
+
+
+def _check_poses(a, width: int, what: str):
+    if _is_torch(a):
+        import torch
+        if a.dtype != torch.float32 or a.dim() != 2 or a.shape[1] != width or not a.is_contiguous():
+            raise ValueError(f"{what}: expected a contiguous float32 (n, {width}) tensor")
+        return a
+    a = np.ascontiguousarray(a, dtype=np.float32)
+    if a.ndim != 2 or a.shape[1] != width:
+        raise ValueError(f"{what}: expected (n, {width}) poses")
+    return a
+
+
+class GbaContext:
+    """Device context; see include/gbattract.h for the semantics of each call."""
+
+    def __init__(self, device: int = 0):
+        self.lib = _lib.load()
+        h = C.c_void_p()
+        rc = self.lib.gba_create(device, C.byref(h))
+        if rc != _lib.GBA_OK:
+            raise _lib.GbaError(rc, self.lib.gba_last_error(None).decode())
+        self.h = h
+        self.device = device
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.gba_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _check(self, rc):
+        _lib.check(self.h, rc)
+
+    # ---- uploads -------------------------------------------------------------
+    def upload_protein(self, p: Protein) -> int:
+        out = C.c_uint32()
+        modes = p.modes if p.modes is not None else None
+        self._check(self.lib.gba_upload_protein(
+            self.h, p.n, _lib.ptr(p.xyz), _lib.ptr(p.type), _lib.ptr(p.mapped), _lib.ptr(p.charge),
+            p.n_modes, _lib.ptr(modes), _lib.ptr(p.mode_force), C.byref(out)))
+        return out.value
+
+    def upload_grid(self, g: GridSet) -> int:
+        out = C.c_uint32()
+        inner, outer, nl = _intrpl_c(g.inner), _intrpl_c(g.outer), _nl_c(g.nl)
+        nl.numEl = int(g.nl_list.shape[0])
+        self._check(self.lib.gba_upload_grid(
+            self.h, C.byref(inner), _lib.ptr(np.ascontiguousarray(g.inner_data)), C.byref(outer),
+            _lib.ptr(np.ascontiguousarray(g.outer_data)), C.byref(nl),
+            _lib.ptr(np.ascontiguousarray(g.nl_grid)),
+            _lib.ptr(np.ascontiguousarray(g.nl_list)) if g.nl_list.size else None, C.byref(out)))
+        return out.value
+
+    def upload_params(self, t: ParamTable) -> int:
+        out = C.c_uint32()
+        tab = np.ascontiguousarray(t.table)
+        self._check(self.lib.gba_upload_params(self.h, t.num_types, _lib.ptr(tab), t.potshape,
+                                               t.dielec, float(t.ffelec), C.byref(out)))
+        return out.value
+
+    def release(self, item: int):
+        self._check(self.lib.gba_release(self.h, item))
+
+    # ---- grid builder --------------------------------------------------------
+    def build_grid(self, rec: int, params: int, opt: GridOptions | None = None) -> int:
+        """Builds inner/outer/NL grids of receptor `rec` on the device."""
+        opt = opt or GridOptions()
+        o = grid_opts_c(opt)
+        out = C.c_uint32()
+        self._check(self.lib.gba_build_grid(self.h, rec, params, C.byref(o), C.byref(out)))
+        return out.value
+
+    def download_grid(self, grid: int) -> GridSet:
+        """Copies a device grid back into a host GridSet."""
+        i, o, n = _lib.IntrplDescC(), _lib.IntrplDescC(), _lib.NLDescC()
+        self._check(self.lib.gba_grid_info(self.h, grid, C.byref(i), C.byref(o), C.byref(n)))
+        inner = IntrplDesc(i.numGrids, tuple(i.dimN), i.gridSpacing, tuple(i.posMin))
+        outer = IntrplDesc(o.numGrids, tuple(o.dimN), o.gridSpacing, tuple(o.posMin))
+        nld = NLDesc(tuple(n.dimN), n.gridSpacing, n.dPlateau, tuple(n.posMin), n.numEl)
+        di = np.empty((inner.numGrids, inner.dimN[2], inner.dimN[1], inner.dimN[0], 4), np.float32)
+        do = np.empty((outer.numGrids, outer.dimN[2], outer.dimN[1], outer.dimN[0], 4), np.float32)
+        ng = np.empty((nld.dimN[2], nld.dimN[1], nld.dimN[0], 2), np.uint32)
+        nlst = np.empty(max(1, n.numEl), np.uint32)
+        self._check(self.lib.gba_download_grid(self.h, grid, _lib.ptr(di), _lib.ptr(do),
+                                               _lib.ptr(ng), _lib.ptr(nlst)))
+        return GridSet(inner, di, outer, do, nld, ng, nlst[:n.numEl])
+
+    # ---- evaluation ----------------------------------------------------------
+    def energy_6d(self, rec: int, lig: int, grid: int, params: int, dofs, out=None,
+                  stream=None):
+        """One energy+gradient evaluation per pose; returns (n, 7) results."""
+        dofs = _check_poses(dofs, DOF_WIDTH, "energy_6d")
+        n = dofs.shape[0]
+        if out is None:
+            out = _alloc_like(dofs, (n, RESULT_WIDTH))
+        self._check(self.lib.gba_energy_6d(self.h, rec, lig, grid, params, _lib.ptr(dofs), n,
+                                           _lib.ptr(out), stream))
+        return out
+
+    def energy_6d_modes(self, rec: int, lig: int, grid_rec: int, grid_lig: int, params: int,
+                        dofs, out=None, stream=None):
+        """Normal-mode variant; dofs (n, 26) -> results (n, 27)."""
+        dofs = _check_poses(dofs, DOF_MODES_WIDTH, "energy_6d_modes")
+        n = dofs.shape[0]
+        if out is None:
+            out = _alloc_like(dofs, (n, RESULT_MODES_WIDTH))
+        self._check(self.lib.gba_energy_6d_modes(self.h, rec, lig, grid_rec, grid_lig, params,
+                                                 _lib.ptr(dofs), n, _lib.ptr(out), stream))
+        return out
+
+    def census_6d(self, rec: int, lig: int, grid: int, params: int, dofs):
+        """Per-pose counts {n_grid, n_grid_charged, n_nl, n_nl_entries} (n, 4) uint32."""
+        dofs = _check_poses(dofs, DOF_WIDTH, "census_6d")
+        n = dofs.shape[0]
+        res = _alloc_like(dofs, (n, RESULT_WIDTH))
+        if _is_torch(dofs):
+            import torch
+            cen = torch.empty((n, 4), dtype=torch.int32, device=dofs.device)
+        else:
+            cen = np.empty((n, 4), dtype=np.uint32)
+        self._check(self.lib.gba_census_6d(self.h, rec, lig, grid, params, _lib.ptr(dofs), n,
+                                           _lib.ptr(res), _lib.ptr(cen)))
+        return cen, res

@@ -1,0 +1,453 @@
+/*
+ * gba_api.cu -- the C ABI of libgbattract (declared in include/gbattract.h).
+ *
+ * Owns the device copies of proteins, grids and parameter tables (the role of
+ * the reference's DataManager/DeviceManager, src/server/DataManager.cpp:23-101,
+ * src/server/DeviceManager.cpp:29-59) and dispatches the fused kernels.  No
+ * entry point throws or exits: failures come back as a status code with the
+ * message in gba_last_error().
+ */
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <mutex>
+#include <new>
+#include <stdexcept>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "gba_context.h"
+
+using namespace gba;
+
+namespace {
+thread_local std::string t_create_error;
+}
+
+/* ------------------------------------------------------------------------ */
+/* context helpers                                                          */
+/* ------------------------------------------------------------------------ */
+
+namespace gba {
+
+void DevBuffer::alloc(size_t b) {
+	release();
+	if (b == 0) return;
+	cudaError_t e = cudaMalloc(&ptr, b);
+	if (e != cudaSuccess) {
+		ptr = nullptr;
+		throw ApiError(e == cudaErrorMemoryAllocation ? GBA_ERR_OUT_OF_MEMORY : GBA_ERR_CUDA,
+				std::string("cudaMalloc(") + std::to_string(b) + "): " + cudaGetErrorString(e));
+	}
+	bytes = b;
+}
+
+void DevBuffer::release() {
+	if (ptr) cudaFree(ptr);
+	ptr = nullptr;
+	bytes = 0;
+}
+
+void DevBuffer::upload(const void* src, size_t b) {
+	alloc(b);
+	if (b) check_cuda(cudaMemcpy(ptr, src, b, cudaMemcpyHostToDevice), "upload");
+}
+
+void check_cuda(cudaError_t e, const char* what) {
+	if (e != cudaSuccess)
+		throw ApiError(e == cudaErrorMemoryAllocation ? GBA_ERR_OUT_OF_MEMORY : GBA_ERR_CUDA,
+				std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+bool is_device_pointer(const void* p) {
+	cudaPointerAttributes a;
+	cudaError_t e = cudaPointerGetAttributes(&a, p);
+	if (e != cudaSuccess) {
+		cudaGetLastError();
+		return false;
+	}
+	return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+Item* Context::find(gba_id id, ItemKind kind) {
+	auto it = items.find(id);
+	if (it == items.end() || it->second->kind != kind)
+		throw ApiError(GBA_ERR_UNKNOWN_ID, "unknown " + std::string(kind_name(kind)) + " id " +
+				std::to_string(id));
+	return it->second.get();
+}
+
+gba_id Context::add(std::unique_ptr<Item> item) {
+	std::lock_guard<std::mutex> g(mu);
+	gba_id id = next_id++;
+	items.emplace(id, std::move(item));
+	return id;
+}
+
+void* Context::staging(int slot, size_t bytes) {
+	DevBuffer& b = stage[slot];
+	if (b.bytes < bytes) b.alloc(bytes + bytes / 4);
+	return b.ptr;
+}
+
+const char* kind_name(ItemKind k) {
+	switch (k) {
+	case ItemKind::Protein: return "protein";
+	case ItemKind::Grid: return "grid";
+	case ItemKind::Params: return "parameter table";
+	}
+	return "item";
+}
+
+/* Derived members exactly as IntrplGrid's constructor
+ * (src/model/IntrplGrid.tpp:29-41); host code is built unfused. */
+DevIntrpl intrpl_from_desc(const gba_intrpl_desc& d) {
+	DevIntrpl g{};
+	for (int a = 0; a < 3; ++a) { g.dimN[a] = d.dimN[a]; g.pos[a] = d.posMin[a]; }
+	g.numGrids = d.numGrids;
+	g.dVox = d.gridSpacing;
+	const float vol = g.dVox * g.dVox * g.dVox;
+	g.voxelVol_inv = 1.f / vol;
+	g.dVox_inv = 1.f / g.dVox;
+	for (int a = 0; a < 3; ++a) g.maxDim[a] = g.pos[a] + (float)(g.dimN[a] - 1) * g.dVox;
+	return g;
+}
+
+/* NLGrid's constructor, src/model/NLGrid.tpp:29-41 */
+DevNL nl_from_desc(const gba_nl_desc& d) {
+	DevNL g{};
+	for (int a = 0; a < 3; ++a) { g.dimN[a] = d.dimN[a]; g.pos[a] = d.posMin[a]; }
+	const float dVox = d.gridSpacing;
+	g.dPlateau2 = d.dPlateau * d.dPlateau;
+	g.dPlateau2_inv = 1 / g.dPlateau2;
+	g.dVox_inv = 1 / dVox;
+	for (int a = 0; a < 3; ++a) g.maxDim[a] = g.pos[a] + (float)(g.dimN[a] - 1) * dVox;
+	g.ratio_size = (uint32_t)int(10000 * g.dPlateau2) + 1;
+	return g;
+}
+
+/* The sqrt-ratio table of src/model/NLGrid.tpp:45-50, bit-identical. */
+std::vector<float> nl_ratio_table(float dPlateau2) {
+	const int size = int(10000 * dPlateau2);
+	std::vector<float> r(size + 1);
+	for (int n = 0; n <= size; n++) {
+		double d2 = ((n + 0.5) / 10000);
+		r[n] = (float)std::sqrt(d2 / (double)dPlateau2);
+	}
+	return r;
+}
+
+}  // namespace gba
+
+#define GBA_API_BEGIN try {
+#define GBA_API_END(ctx)                                                   \
+	}                                                                      \
+	catch (const ApiError& e) {                                            \
+		(ctx)->set_error(e.what());                                        \
+		return e.code;                                                     \
+	}                                                                      \
+	catch (const std::bad_alloc&) {                                        \
+		(ctx)->set_error("host allocation failed");                        \
+		return GBA_ERR_OUT_OF_MEMORY;                                      \
+	}                                                                      \
+	catch (const std::exception& e) {                                      \
+		(ctx)->set_error(e.what());                                        \
+		return GBA_ERR_INVALID_ARGUMENT;                                   \
+	}                                                                      \
+	return GBA_OK;
+
+extern "C" {
+
+const char* gba_version(void) { return "gbattract 0.1 (sm_103a)"; }
+
+int gba_create(int device, gba_ctx** out) {
+	if (!out) {
+		t_create_error = "gba_create: out is NULL";
+		return GBA_ERR_INVALID_ARGUMENT;
+	}
+	*out = nullptr;
+	int n = 0;
+	cudaError_t e = cudaGetDeviceCount(&n);
+	if (e != cudaSuccess || n == 0) {
+		cudaGetLastError();
+		t_create_error = std::string("gba_create: no CUDA device (") + cudaGetErrorString(e) + ")";
+		return GBA_ERR_NO_DEVICE;
+	}
+	if (device < 0 || device >= n) {
+		t_create_error = "gba_create: device " + std::to_string(device) + " out of range [0," +
+				std::to_string(n) + ")";
+		return GBA_ERR_INVALID_ARGUMENT;
+	}
+	e = cudaSetDevice(device);
+	if (e == cudaSuccess) e = cudaFree(nullptr);
+	if (e != cudaSuccess) {
+		t_create_error = std::string("gba_create: ") + cudaGetErrorString(e);
+		return GBA_ERR_CUDA;
+	}
+	auto* c = new (std::nothrow) gba_ctx();
+	if (!c) {
+		t_create_error = "gba_create: host allocation failed";
+		return GBA_ERR_OUT_OF_MEMORY;
+	}
+	c->device = device;
+	cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device);
+	*out = c;
+	return GBA_OK;
+}
+
+int gba_destroy(gba_ctx* ctx) {
+	if (!ctx) return GBA_ERR_INVALID_ARGUMENT;
+	cudaSetDevice(ctx->device);
+	delete ctx;
+	return GBA_OK;
+}
+
+const char* gba_last_error(const gba_ctx* ctx) {
+	if (!ctx) return t_create_error.c_str();
+	return ctx->last_error();
+}
+
+int gba_upload_protein(gba_ctx* ctx, uint32_t n, const float* xyz, const uint32_t* type,
+		const uint32_t* mapped, const float* charge, uint32_t n_modes, const float* modes,
+		const float* mode_force, gba_id* out) {
+	if (!ctx) return GBA_ERR_INVALID_ARGUMENT;
+	GBA_API_BEGIN
+	if (!out || n == 0 || !xyz || !type || !mapped || !charge)
+		throw ApiError(GBA_ERR_INVALID_ARGUMENT, "gba_upload_protein: null pointer or n == 0");
+	if (n_modes > GBA_MODES_MAX)
+		throw ApiError(GBA_ERR_INVALID_ARGUMENT, "gba_upload_protein: n_modes > GBA_MODES_MAX");
+	if (n_modes > 0 && (!modes || !mode_force))
+		throw ApiError(GBA_ERR_INVALID_ARGUMENT, "gba_upload_protein: modes/mode_force NULL");
+	ctx->bind();
+	auto item = std::make_unique<ProteinItem>();
+	std::vector<float4> xq(n);
+	std::vector<uint32_t> tm(n);
+	uint32_t max_type = 0, max_mapped = 0;
+	for (uint32_t i = 0; i < n; ++i) {
+		xq[i] = make_float4(xyz[i], xyz[n + i], xyz[2 * (size_t)n + i], charge[i]);
+		if (type[i] > 0xffffu || mapped[i] > 0xffffu)
+			throw ApiError(GBA_ERR_INVALID_ARGUMENT, "gba_upload_protein: type/mapped type > 65535");
+		tm[i] = type[i] | (mapped[i] << 16);
+		max_type = std::max(max_type, type[i]);
+		max_mapped = std::max(max_mapped, mapped[i]);
+	}
+	item->xyzq.upload(xq.data(), xq.size() * sizeof(float4));
+	item->tm.upload(tm.data(), tm.size() * sizeof(uint32_t));
+	item->max_type = max_type;
+	item->max_mapped = max_mapped;
+	item->host_xyz.assign(xyz, xyz + 3 * (size_t)n);
+	item->dev.n = n;
+	item->dev.n_modes = n_modes;
+	item->dev.xyzq = (const float4*)item->xyzq.ptr;
+	item->dev.tm = (const uint32_t*)item->tm.ptr;
+	if (n_modes > 0) {
+		/* reference layout x[i*M+m] | y | z  ->  device [m][axis][i] */
+		std::vector<float> md((size_t)n_modes * 3 * n);
+		for (uint32_t a = 0; a < 3; ++a)
+			for (uint32_t i = 0; i < n; ++i)
+				for (uint32_t m = 0; m < n_modes; ++m)
+					md[((size_t)m * 3 + a) * n + i] = modes[(size_t)a * n * n_modes + (size_t)i * n_modes + m];
+		item->modes.upload(md.data(), md.size() * sizeof(float));
+		item->dev.modes = (const float*)item->modes.ptr;
+		for (uint32_t m = 0; m < n_modes; ++m) item->dev.mode_force[m] = mode_force[m];
+	}
+	*out = ctx->add(std::move(item));
+	GBA_API_END(ctx)
+}
+
+int gba_upload_grid(gba_ctx* ctx, const gba_intrpl_desc* inner, const float* inner_data,
+		const gba_intrpl_desc* outer, const float* outer_data, const gba_nl_desc* nl,
+		const gba_neighbour_desc* nl_grid, const uint32_t* nl_list, gba_id* out) {
+	if (!ctx) return GBA_ERR_INVALID_ARGUMENT;
+	GBA_API_BEGIN
+	if (!out || !inner || !inner_data || !outer || !outer_data || !nl || !nl_grid ||
+			(nl->numEl > 0 && !nl_list))
+		throw ApiError(GBA_ERR_INVALID_ARGUMENT, "gba_upload_grid: null pointer");
+	for (const gba_intrpl_desc* d : {inner, outer}) {
+		if (d->numGrids < 1 || d->dimN[0] < 2 || d->dimN[1] < 2 || d->dimN[2] < 2 ||
+				!(d->gridSpacing > 0))
+			throw ApiError(GBA_ERR_INVALID_ARGUMENT, "gba_upload_grid: bad interpolation grid descriptor");
+		if ((double)d->numGrids * d->dimN[0] * d->dimN[1] * d->dimN[2] > 4.0e9)
+			throw ApiError(GBA_ERR_INVALID_ARGUMENT, "gba_upload_grid: grid exceeds 2^32 float4");
+	}
+	if (nl->dimN[0] < 1 || nl->dimN[1] < 1 || nl->dimN[2] < 1 || !(nl->gridSpacing > 0) ||
+			!(nl->dPlateau > 0))
+		throw ApiError(GBA_ERR_INVALID_ARGUMENT, "gba_upload_grid: bad neighbour grid descriptor");
+	ctx->bind();
+	auto item = std::make_unique<GridItem>();
+	item->inner_desc = *inner;
+	item->outer_desc = *outer;
+	item->nl_desc = *nl;
+	const size_t ni = (size_t)inner->numGrids * inner->dimN[0] * inner->dimN[1] * inner->dimN[2];
+	const size_t no = (size_t)outer->numGrids * outer->dimN[0] * outer->dimN[1] * outer->dimN[2];
+	const size_t nv = (size_t)nl->dimN[0] * nl->dimN[1] * nl->dimN[2];
+	for (size_t v = 0; v < nv; ++v)
+		if ((uint64_t)nl_grid[v].idx + nl_grid[v].numEl > nl->numEl && nl_grid[v].numEl > 0)
+			throw ApiError(GBA_ERR_INVALID_ARGUMENT, "gba_upload_grid: neighbour descriptor past the list end");
+	item->inner.upload(inner_data, ni * sizeof(float4));
+	item->outer.upload(outer_data, no * sizeof(float4));
+	item->nlgrid.upload(nl_grid, nv * sizeof(uint2));
+	item->nllist.upload(nl_list, (size_t)nl->numEl * sizeof(uint32_t));
+	item->dev.inner = intrpl_from_desc(*inner);
+	item->dev.inner.data = (const float4*)item->inner.ptr;
+	item->dev.outer = intrpl_from_desc(*outer);
+	item->dev.outer.data = (const float4*)item->outer.ptr;
+	item->dev.nl = nl_from_desc(*nl);
+	std::vector<float> ratio = nl_ratio_table(item->dev.nl.dPlateau2);
+	item->ratio.upload(ratio.data(), ratio.size() * sizeof(float));
+	item->dev.nl.grid = (const uint2*)item->nlgrid.ptr;
+	item->dev.nl.list = (const uint32_t*)item->nllist.ptr;
+	item->dev.nl.ratio = (const float*)item->ratio.ptr;
+	/* every receptor index in the list is checked against the receptor at call time */
+	uint32_t max_idx = 0;
+	for (uint32_t k = 0; k < nl->numEl; ++k) max_idx = std::max(max_idx, nl_list[k]);
+	item->nl_max_index = nl->numEl ? max_idx : 0;
+	item->nl_has_entries = nl->numEl > 0;
+	*out = ctx->add(std::move(item));
+	GBA_API_END(ctx)
+}
+
+int gba_upload_params(gba_ctx* ctx, uint32_t num_types, const gba_ffparam* table, int potshape,
+		int dielec, float ffelec, gba_id* out) {
+	if (!ctx) return GBA_ERR_INVALID_ARGUMENT;
+	GBA_API_BEGIN
+	if (!out || !table || num_types == 0)
+		throw ApiError(GBA_ERR_INVALID_ARGUMENT, "gba_upload_params: null table or num_types == 0");
+	if (potshape != GBA_POTSHAPE_8_6 && potshape != GBA_POTSHAPE_12_6)
+		throw ApiError(GBA_ERR_INVALID_ARGUMENT, "gba_upload_params: unknown potential shape");
+	if (dielec != GBA_DIELEC_CONSTANT && dielec != GBA_DIELEC_VARIABLE)
+		throw ApiError(GBA_ERR_INVALID_ARGUMENT, "gba_upload_params: unknown dielectric");
+	ctx->bind();
+	auto item = std::make_unique<ParamsItem>();
+	const size_t T2 = (size_t)num_types * num_types;
+	std::vector<float4> lj(T2);
+	std::vector<float> iv(T2);
+	for (size_t k = 0; k < T2; ++k) {
+		lj[k] = make_float4(table[k].rc, table[k].ac, table[k].rmin2, table[k].emin);
+		iv[k] = (float)table[k].ipon;
+	}
+	item->lj.upload(lj.data(), T2 * sizeof(float4));
+	item->ivor.upload(iv.data(), T2 * sizeof(float));
+	item->host_table.assign(table, table + T2);
+	item->dev.num_types = num_types;
+	item->dev.potshape = potshape;
+	item->dev.dielec = dielec;
+	item->dev.ffelec = ffelec;
+	item->dev.lj = (const float4*)item->lj.ptr;
+	item->dev.ivor = (const float*)item->ivor.ptr;
+	*out = ctx->add(std::move(item));
+	GBA_API_END(ctx)
+}
+
+int gba_release(gba_ctx* ctx, gba_id id) {
+	if (!ctx) return GBA_ERR_INVALID_ARGUMENT;
+	GBA_API_BEGIN
+	ctx->bind();
+	std::lock_guard<std::mutex> g(ctx->mu);
+	auto it = ctx->items.find(id);
+	if (it == ctx->items.end())
+		throw ApiError(GBA_ERR_UNKNOWN_ID, "gba_release: unknown id " + std::to_string(id));
+	ctx->items.erase(it);
+	GBA_API_END(ctx)
+}
+
+int gba_energy_6d(gba_ctx* ctx, gba_id rec, gba_id lig, gba_id grid, gba_id params,
+		const gba_dof6d* dofs, size_t n, gba_result6d* out, void* stream) {
+	if (!ctx) return GBA_ERR_INVALID_ARGUMENT;
+	GBA_API_BEGIN
+	if (n == 0) return GBA_OK;
+	if (!dofs || !out) throw ApiError(GBA_ERR_INVALID_ARGUMENT, "gba_energy_6d: null dofs/out");
+	ctx->bind();
+	RigidLaunch L = ctx->rigid_launch(rec, lig, grid, params);
+	cudaStream_t s = (cudaStream_t)stream;
+	const bool din = is_device_pointer(dofs), dout = is_device_pointer(out);
+	std::unique_lock<std::mutex> stage_lock(ctx->stage_mu, std::defer_lock);
+	if (!din || !dout) stage_lock.lock();
+	L.n = n;
+	L.dofs = din ? dofs : (const gba_dof6d*)ctx->staging(0, n * sizeof(gba_dof6d));
+	L.out = dout ? out : (gba_result6d*)ctx->staging(1, n * sizeof(gba_result6d));
+	L.census = nullptr;
+	if (!din)
+		check_cuda(cudaMemcpyAsync((void*)L.dofs, dofs, n * sizeof(gba_dof6d), cudaMemcpyHostToDevice, s),
+				"gba_energy_6d: H2D");
+	ctx->run_rigid(L, s);
+	if (!dout)
+		check_cuda(cudaMemcpyAsync(out, L.out, n * sizeof(gba_result6d), cudaMemcpyDeviceToHost, s),
+				"gba_energy_6d: D2H");
+	if (!din || !dout) check_cuda(cudaStreamSynchronize(s), "gba_energy_6d: sync");
+	GBA_API_END(ctx)
+}
+
+int gba_census_6d(gba_ctx* ctx, gba_id rec, gba_id lig, gba_id grid, gba_id params,
+		const gba_dof6d* dofs, size_t n, gba_result6d* out, uint32_t* census) {
+	if (!ctx) return GBA_ERR_INVALID_ARGUMENT;
+	GBA_API_BEGIN
+	if (n == 0) return GBA_OK;
+	if (!dofs || !out || !census) throw ApiError(GBA_ERR_INVALID_ARGUMENT, "gba_census_6d: null pointer");
+	ctx->bind();
+	RigidLaunch L = ctx->rigid_launch(rec, lig, grid, params);
+	std::lock_guard<std::mutex> stage_lock(ctx->stage_mu);
+	const bool din = is_device_pointer(dofs), dout = is_device_pointer(out), dc = is_device_pointer(census);
+	L.n = n;
+	L.dofs = din ? dofs : (const gba_dof6d*)ctx->staging(0, n * sizeof(gba_dof6d));
+	L.out = dout ? out : (gba_result6d*)ctx->staging(1, n * sizeof(gba_result6d));
+	L.census = dc ? (PoseCensus*)census : (PoseCensus*)ctx->staging(2, n * sizeof(PoseCensus));
+	if (!din)
+		check_cuda(cudaMemcpy((void*)L.dofs, dofs, n * sizeof(gba_dof6d), cudaMemcpyHostToDevice), "H2D");
+	ctx->run_rigid(L, 0);
+	if (!dout) check_cuda(cudaMemcpy(out, L.out, n * sizeof(gba_result6d), cudaMemcpyDeviceToHost), "D2H");
+	if (!dc) check_cuda(cudaMemcpy(census, L.census, n * sizeof(PoseCensus), cudaMemcpyDeviceToHost), "D2H");
+	check_cuda(cudaDeviceSynchronize(), "gba_census_6d");
+	GBA_API_END(ctx)
+}
+
+}  // extern "C"
+
+/* ------------------------------------------------------------------------ */
+/* launch assembly                                                          */
+/* ------------------------------------------------------------------------ */
+
+namespace gba {
+
+RigidLaunch Context::rigid_launch(gba_id rec, gba_id lig, gba_id grid, gba_id params) {
+	std::lock_guard<std::mutex> g(mu);
+	auto* R = static_cast<ProteinItem*>(find(rec, ItemKind::Protein));
+	auto* Lg = static_cast<ProteinItem*>(find(lig, ItemKind::Protein));
+	auto* G = static_cast<GridItem*>(find(grid, ItemKind::Grid));
+	auto* P = static_cast<ParamsItem*>(find(params, ItemKind::Params));
+	validate_pair(*R, *Lg, *G, *P);
+	RigidLaunch L{};
+	L.rec = R->dev;
+	L.lig = Lg->dev;
+	L.grid = G->dev;
+	L.par = P->dev;
+	return L;
+}
+
+/* The index checks that keep every device access in bounds (the reference
+ * asserts them in debug builds only: src/model/neighborlist.h:94-97,
+ * src/model/IntrplGrid.h:132-146). */
+void Context::validate_pair(const ProteinItem& rec, const ProteinItem& lig, const GridItem& g,
+		const ParamsItem& p) {
+	if (lig.max_type > p.dev.num_types || rec.max_type > p.dev.num_types)
+		throw ApiError(GBA_ERR_INVALID_ARGUMENT, "bead type exceeds the parameter table (" +
+				std::to_string(std::max(lig.max_type, rec.max_type)) + " > " +
+				std::to_string(p.dev.num_types) + ")");
+	if (lig.max_mapped >= g.inner_desc.numGrids || lig.max_mapped >= g.outer_desc.numGrids)
+		throw ApiError(GBA_ERR_INVALID_ARGUMENT, "ligand mapped type exceeds the grid's channels");
+	if (g.nl_has_entries && g.nl_max_index >= rec.dev.n)
+		throw ApiError(GBA_ERR_INVALID_ARGUMENT, "neighbour list indexes beyond the receptor");
+}
+
+void Context::run_rigid(RigidLaunch& L, cudaStream_t s) {
+	const int threads = 256;
+	const int warps_per_block = threads / 32;
+	int bps = rigid_blocks_per_sm(threads, L.census != nullptr);
+	size_t want = (L.n + warps_per_block - 1) / warps_per_block;
+	size_t blocks = std::min<size_t>(want, (size_t)num_sms * bps);
+	if (blocks == 0) blocks = 1;
+	check_cuda(launch_rigid_energy(L, (int)blocks, threads, s), "rigid energy launch");
+}
+
+}  // namespace gba

@@ -1,0 +1,108 @@
+/*
+ * gba_context.h -- host-side state behind a gba_ctx handle.
+ */
+#ifndef GBA_CONTEXT_H_
+#define GBA_CONTEXT_H_
+
+#include <memory>
+#include <mutex>
+#include <stdexcept>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "gba_internal.h"
+
+namespace gba {
+
+/* Carries a GBA_ERR_* code through the C++ implementation to the C ABI. */
+struct ApiError : std::runtime_error {
+	int code;
+	ApiError(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+void check_cuda(cudaError_t e, const char* what);
+bool is_device_pointer(const void* p);
+
+/* One cudaMalloc'd buffer, freed on destruction. */
+struct DevBuffer {
+	void* ptr = nullptr;
+	size_t bytes = 0;
+	DevBuffer() = default;
+	DevBuffer(const DevBuffer&) = delete;
+	DevBuffer& operator=(const DevBuffer&) = delete;
+	~DevBuffer() { release(); }
+	void alloc(size_t b);
+	void release();
+	void upload(const void* src, size_t b);
+};
+
+enum class ItemKind { Protein, Grid, Params };
+const char* kind_name(ItemKind k);
+
+struct Item {
+	ItemKind kind;
+	explicit Item(ItemKind k) : kind(k) {}
+	virtual ~Item() {}
+};
+
+struct ProteinItem : Item {
+	ProteinItem() : Item(ItemKind::Protein) {}
+	DevBuffer xyzq, tm, modes;
+	DevProtein dev{};
+	uint32_t max_type = 0, max_mapped = 0;
+	std::vector<float> host_xyz;   /* SoA copy for host-side layout work */
+};
+
+struct GridItem : Item {
+	GridItem() : Item(ItemKind::Grid) {}
+	DevBuffer inner, outer, nlgrid, nllist, ratio;
+	DevGrid dev{};
+	gba_intrpl_desc inner_desc{}, outer_desc{};
+	gba_nl_desc nl_desc{};
+	uint32_t nl_max_index = 0;
+	bool nl_has_entries = false;
+};
+
+struct ParamsItem : Item {
+	ParamsItem() : Item(ItemKind::Params) {}
+	DevBuffer lj, ivor;
+	DevParams dev{};
+	std::vector<gba_ffparam> host_table;
+};
+
+DevIntrpl intrpl_from_desc(const gba_intrpl_desc& d);
+DevNL nl_from_desc(const gba_nl_desc& d);
+std::vector<float> nl_ratio_table(float dPlateau2);
+
+struct Context {
+	int device = 0;
+	int num_sms = 0;
+	std::mutex mu;                 /* items map */
+	std::mutex stage_mu;           /* host-pointer staging buffers */
+	std::unordered_map<gba_id, std::unique_ptr<Item>> items;
+	gba_id next_id = 1;
+	DevBuffer stage[4];
+
+	mutable std::mutex err_mu;
+	std::string err;
+
+	void bind() { check_cuda(cudaSetDevice(device), "cudaSetDevice"); }
+	void set_error(const std::string& m) { std::lock_guard<std::mutex> g(err_mu); err = m; }
+	const char* last_error() const { std::lock_guard<std::mutex> g(err_mu); return err.c_str(); }
+
+	Item* find(gba_id id, ItemKind kind);
+	gba_id add(std::unique_ptr<Item> item);
+	void* staging(int slot, size_t bytes);
+
+	RigidLaunch rigid_launch(gba_id rec, gba_id lig, gba_id grid, gba_id params);
+	void validate_pair(const ProteinItem& rec, const ProteinItem& lig, const GridItem& g,
+			const ParamsItem& p);
+	void run_rigid(RigidLaunch& L, cudaStream_t s);
+};
+
+}  // namespace gba
+
+struct gba_ctx : gba::Context {};
+
+#endif

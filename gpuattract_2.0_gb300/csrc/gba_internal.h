@@ -1,0 +1,94 @@
+/*
+ * gba_internal.h -- device-side data layout of libgbattract.
+ *
+ * Everything the fused kernels read lives in plain device buffers laid out for
+ * one-instruction loads:
+ *   protein  : float4 {x, y, z, q} per bead + uint32 {type | mapped << 16}
+ *              + modes as (M, 3, n) floats so lane-per-bead reads coalesce
+ *   grids    : the reference's channel-major float4 layout (channel 0 =
+ *              charge), one buffer per inner/outer grid; derived constants
+ *              (maxDim, 1/dVox, 1/voxelVol) precomputed on the host exactly as
+ *              IntrplGrid's constructor does (src/model/IntrplGrid.tpp:29-41)
+ *   NL grid  : uint2 {numEl, idx} per voxel + uint32 list + the sqrt-ratio
+ *              table of src/model/NLGrid.tpp:45-50 (bit-identical)
+ *   params   : float4 {rc, ac, rmin2, emin} + float ipon per type pair
+ */
+#ifndef GBA_INTERNAL_H_
+#define GBA_INTERNAL_H_
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include "../../include/gbattract.h"
+
+namespace gba {
+
+struct DevProtein {
+	uint32_t n;
+	uint32_t n_modes;
+	const float4* xyzq;       /* n */
+	const uint32_t* tm;       /* n: type | mapped << 16 */
+	const float* modes;       /* n_modes * 3 * n, [m][axis][i] */
+	float mode_force[GBA_MODES_MAX];
+};
+
+struct DevIntrpl {
+	uint32_t dimN[3];
+	uint32_t numGrids;
+	float pos[3];
+	float maxDim[3];
+	float dVox, dVox_inv, voxelVol_inv;
+	const float4* data;       /* numGrids * Nx*Ny*Nz */
+};
+
+struct DevNL {
+	uint32_t dimN[3];
+	uint32_t ratio_size;      /* entries in ratio[] */
+	float pos[3];
+	float maxDim[3];
+	float dVox_inv;
+	float dPlateau2, dPlateau2_inv;
+	const uint2* grid;        /* Nx*Ny*Nz {numEl, idx} */
+	const uint32_t* list;
+	const float* ratio;
+};
+
+struct DevGrid {
+	DevIntrpl inner, outer;
+	DevNL nl;
+};
+
+struct DevParams {
+	uint32_t num_types;
+	int potshape;             /* GBA_POTSHAPE_* */
+	int dielec;               /* GBA_DIELEC_* */
+	float ffelec;
+	const float4* lj;         /* T*T {rc, ac, rmin2, emin} */
+	const float* ivor;        /* T*T ipon as float */
+};
+
+/* Per-pose census used for the roofline byte count (same meaning as the
+ * oracle's orc_pose_stats counters). */
+struct PoseCensus {
+	uint32_t n_grid, n_grid_charged, n_nl, n_nl_entries;
+};
+
+/* ---- launch wrappers (energy_rigid.cu) ----------------------------------- */
+
+struct RigidLaunch {
+	DevProtein rec, lig;
+	DevGrid grid;
+	DevParams par;
+	const gba_dof6d* dofs;
+	gba_result6d* out;
+	PoseCensus* census;       /* nullptr: no census */
+	size_t n;
+};
+
+cudaError_t launch_rigid_energy(const RigidLaunch& L, int blocks, int threads, cudaStream_t s);
+
+/* Number of resident blocks per SM of the rigid kernel for `threads`. */
+int rigid_blocks_per_sm(int threads, bool census);
+
+}  // namespace gba
+
+#endif

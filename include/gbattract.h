@@ -1,0 +1,212 @@
+/*
+ * gbattract.h -- C ABI of the GB300 docking energy/gradient library (libgbattract).
+ *
+ * This library replaces the energy backend of gpuATTRACT 2.0 behind its
+ * Service/Server request interface.  Every entry point returns an int status
+ * (GBA_OK == 0) and never throws or exits; gba_last_error() gives the message.
+ * All structs below are plain FP32/uint32 PODs laid out bit-for-bit like the
+ * reference's own types, so a WorkItem's input/result slices pass through
+ * without conversion.
+ *
+ * Reference interfaces each declaration stands in for are cited as
+ * path:line inside the gpuATTRACT 2.0 source tree.
+ */
+#ifndef GBATTRACT_H_
+#define GBATTRACT_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* MODES_MAX_NUMBER, src/model/Types_6D_Config.h:11 */
+#define GBA_MODES_MAX 10
+
+/* ---- status codes ------------------------------------------------------- */
+#define GBA_OK                   0
+#define GBA_ERR_INVALID_ARGUMENT 1  /* std::invalid_argument in the reference */
+#define GBA_ERR_UNKNOWN_ID       2  /* DataManager::get on a missing id, src/server/DataManager.cpp:23-50 */
+#define GBA_ERR_CUDA             3  /* CUDA_CHECK -> std::runtime_error, src/commons/macros.h:62-72 */
+#define GBA_ERR_OUT_OF_MEMORY    4
+#define GBA_ERR_TIMEOUT          5  /* a device-side wait/iteration budget ran out */
+#define GBA_ERR_NO_DEVICE        6
+#define GBA_ERR_DEVICE_CHECK     7  /* a device-side bounds check recorded a bad index */
+
+typedef struct gba_ctx gba_ctx;
+typedef uint32_t gba_id;      /* id of a device-resident data item (protein, grid, table) */
+
+/* ---- pose / result records ---------------------------------------------- */
+
+/* as::DOF_6D<float>, src/model/Types_6D.h:32-37: translation, then ZYZ Euler angles */
+typedef struct { float pos[3]; float ang[3]; } gba_dof6d;
+
+/* as::Result_6D<float>, src/model/Types_6D.h:47-54: energy, force sum (= -dE/dpos),
+ * Euler-angle "torque" (= -dE/dang) */
+typedef struct { float E; float pos[3]; float ang[3]; } gba_result6d;
+
+/* as::DOF_6D_Modes<float>, src/model/Types_6D_Modes.h:33-41 */
+typedef struct {
+	gba_dof6d rigid;
+	float modesRec[GBA_MODES_MAX];
+	float modesLig[GBA_MODES_MAX];
+} gba_dof6d_modes;
+
+/* as::Result_6D_Modes<float>, src/model/Types_6D_Modes.h:54-60 */
+typedef struct {
+	gba_result6d rigid;
+	float modesRec[GBA_MODES_MAX];
+	float modesLig[GBA_MODES_MAX];
+} gba_result6d_modes;
+
+/* ---- model data descriptors --------------------------------------------- */
+
+/* ParamTable<float>::attractFFParams_t, src/model/ParamTable.h:24-30 (after the
+ * attract.par transform of src/fileIO/readFile.cpp:484-497) */
+typedef struct { float rc; float ac; int32_t ipon; float rmin2; float emin; } gba_ffparam;
+
+/* PotShape, src/model/ParamTable.h:12-16 (same enumerator order) */
+#define GBA_POTSHAPE_12_6 0
+#define GBA_POTSHAPE_8_6  1
+/* Dielec, src/model/SimParam.h:41-44 */
+#define GBA_DIELEC_CONSTANT 0
+#define GBA_DIELEC_VARIABLE 1
+
+/* IntrplGrid<float>::Desc, src/model/IntrplGrid.h:183-207 (typemask dropped,
+ * data passed separately).  Data layout: numGrids channels, channel 0 the
+ * charge grid, each channel z-major slices of x-fastest rows of float4
+ * (fx, fy, fz, E) -- exactly what readGridFromGridFile builds,
+ * src/fileIO/readFile.cpp:261-356. posMin is already translated by -pivot. */
+typedef struct {
+	uint32_t numGrids;
+	uint32_t dimN[3];
+	float gridSpacing;
+	float posMin[3];
+} gba_intrpl_desc;
+
+/* NLGrid<float>::Desc, src/model/NLGrid.h:151-165 */
+typedef struct {
+	uint32_t dimN[3];
+	float gridSpacing;
+	float dPlateau;
+	float posMin[3];
+	uint32_t numEl;        /* total entries of the concatenated neighbour list */
+} gba_nl_desc;
+
+/* NeighbourDesc, src/model/NLGrid.h:30-35 */
+typedef struct { uint32_t numEl; uint32_t idx; } gba_neighbour_desc;
+
+/* ---- context ------------------------------------------------------------ */
+
+/* Version string of the library. */
+const char* gba_version(void);
+
+/* Opens a context on CUDA device `device`.  Stands in for the per-device state
+ * the reference keeps in DeviceManager/DataManager (src/server/DeviceManager.cpp:29-59)
+ * plus the per-worker GPUEnergyService6D buffers (src/service/GPUEnergyService6D.tpp:100-160). */
+int gba_create(int device, gba_ctx** out);
+
+/* Frees every device copy owned by the context. */
+int gba_destroy(gba_ctx* ctx);
+
+/* Message of the last failed call on this context ("" if none).  With ctx ==
+ * NULL, the message of the last failed gba_create on this thread. */
+const char* gba_last_error(const gba_ctx* ctx);
+
+/* ---- uploads (synchronous; the library owns the device copies) ----------- */
+
+/* Protein, src/model/Protein.h:39-167 uploaded like DeviceDataConfigurator::attach
+ * (src/server/DeviceDataConfigurator.tpp:28-95).
+ *  xyz        3*n floats, SoA (x[0..n), y[0..n), z[0..n)), pivotized
+ *  type       n raw ATTRACT types after the default map (99 -> 0); 0 = dummy bead
+ *  mapped     n grid channels of the partner's grid (0 = no grid term)
+ *  charge     n charges
+ *  n_modes    0..GBA_MODES_MAX; modes = 3*n*n_modes floats in the reference's
+ *             layout x[i*n_modes+m], then y, then z (src/model/Protein.h:88-98);
+ *             mode_force = n_modes floats (may be NULL when n_modes == 0) */
+int gba_upload_protein(gba_ctx* ctx, uint32_t n, const float* xyz, const uint32_t* type,
+		const uint32_t* mapped, const float* charge, uint32_t n_modes,
+		const float* modes, const float* mode_force, gba_id* out);
+
+/* GridUnion (inner + outer IntrplGrid, NLGrid), src/model/GridUnion.h:20, uploaded
+ * like src/server/DeviceDataConfigurator.tpp:141-326 but as plain device buffers.
+ *  inner_data / outer_data: numGrids*dimN.x*dimN.y*dimN.z float4 (16 B each)
+ *  nl_grid: dimN.x*dimN.y*dimN.z descriptors; nl_list: nl->numEl receptor indices */
+int gba_upload_grid(gba_ctx* ctx,
+		const gba_intrpl_desc* inner, const float* inner_data,
+		const gba_intrpl_desc* outer, const float* outer_data,
+		const gba_nl_desc* nl, const gba_neighbour_desc* nl_grid, const uint32_t* nl_list,
+		gba_id* out);
+
+/* ParamTable<float> (src/model/ParamTable.h:18-101) + SimParam<float>
+ * (src/model/SimParam.h:39-55); table[numTypes*typeA + typeB] as getParams(). */
+int gba_upload_params(gba_ctx* ctx, uint32_t num_types, const gba_ffparam* table,
+		int potshape, int dielec, float ffelec, gba_id* out);
+
+/* Drops a data item (DataManager::remove). */
+int gba_release(gba_ctx* ctx, gba_id id);
+
+/* ---- evaluation ----------------------------------------------------------- */
+
+/* One energy+gradient evaluation per pose (rigid body), the work of one
+ * CPUEnergyService6D / GPUEnergyService6D item processor
+ * (src/service/CPUEnergyService6D.tpp:63-200, src/service/GPUEnergyService6D.tpp:470-510),
+ * fused into one kernel launch.  `dofs`/`out` may be device or host pointers.
+ * `stream` is a cudaStream_t (NULL = legacy default stream).  With two device
+ * pointers the call is asynchronous on `stream`; if either is a host pointer the
+ * copies run on `stream` and the call returns after the stream has drained. */
+int gba_energy_6d(gba_ctx* ctx, gba_id rec, gba_id lig, gba_id grid, gba_id params,
+		const gba_dof6d* dofs, size_t n, gba_result6d* out, void* stream);
+
+/* Normal-mode variant (CPUEnergyService6DModes, src/service/CPUEnergyService6DModes.tpp:76-336):
+ * the receptor is deformed and interpolated in the ligand grid `grid_lig`, the
+ * ligand deformed and interpolated in the receptor grid `grid_rec`, one NL pass
+ * on the receptor NL grid.  Pointer/stream semantics as gba_energy_6d. */
+int gba_energy_6d_modes(gba_ctx* ctx, gba_id rec, gba_id lig, gba_id grid_rec, gba_id grid_lig,
+		gba_id params, const gba_dof6d_modes* dofs, size_t n, gba_result6d_modes* out,
+		void* stream);
+
+/* ---- grid builder --------------------------------------------------------- */
+
+/* Options of the device grid builder (inner 0.9 A, outer 1.8 A, plateau 10 A,
+ * neighbour radius 10.8 A, outer extension 32 inner voxels). */
+typedef struct {
+	float spacing;          /* inner voxel size */
+	float plateau;          /* NL plateau distance */
+	float nl_cutoff;        /* neighbour-list radius around a voxel centre */
+	float margin;           /* inner box = receptor bounding box + margin */
+	uint32_t outer_ext;     /* outer extension, in inner voxels per side */
+	uint32_t n_alphabet;    /* ligand types that get a channel (<= 98) */
+	uint32_t alphabet[99];  /* raw ligand type served by channel c+1 */
+} gba_grid_build_opts;
+
+/* Builds the inner, outer and neighbour-list grids of receptor `rec` on the
+ * device, in the layout of readGridFromGridFile (src/fileIO/readFile.cpp:261-422)
+ * -- the step the reference delegates to ATTRACT's grid program
+ * (attract::Grid::calculate_std, declared at src/fileIO/grid_orig.h:143). */
+int gba_build_grid(gba_ctx* ctx, gba_id rec, gba_id params, const gba_grid_build_opts* opt,
+		gba_id* out);
+
+/* Descriptors of a device grid (sizes for gba_download_grid). */
+int gba_grid_info(gba_ctx* ctx, gba_id grid, gba_intrpl_desc* inner, gba_intrpl_desc* outer,
+		gba_nl_desc* nl);
+
+/* Copies a device grid to host buffers sized from gba_grid_info (any may be NULL). */
+int gba_download_grid(gba_ctx* ctx, gba_id grid, float* inner, float* outer,
+		gba_neighbour_desc* nl_grid, uint32_t* nl_list);
+
+/* ---- instrumentation ---------------------------------------------------------- */
+
+/* gba_energy_6d plus, per pose, 4 counters {beads interpolated, of which
+ * charged, beads with an NL lookup, sum of their voxels' numEl}: the inputs of
+ * the roofline byte count.  No reference counterpart (measurement only).
+ * Synchronous; pointers may be host or device. */
+int gba_census_6d(gba_ctx* ctx, gba_id rec, gba_id lig, gba_id grid, gba_id params,
+		const gba_dof6d* dofs, size_t n, gba_result6d* out, uint32_t* census);
+
+#ifdef __cplusplus
+}  /* extern "C" */
+#endif
+
+#endif /* GBATTRACT_H_ */

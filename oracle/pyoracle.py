@@ -1,0 +1,345 @@
+"""ctypes binding of the CPU oracle (oracle/_build/liboracle.so) and of the
+reference's own CPU path (oracle/_ref/libattract_ref.so, present only where
+the reference tree was available at build time).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and the
+CPU-baseline leg of bench.py, never by the product package.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import sys
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+ROOT = HERE.parent
+ORACLE_LIB = HERE / "_build" / "liboracle.so"
+REF_LIB = HERE / "_ref" / "libattract_ref.so"
+
+
+def _pkg():
+    if str(ROOT) not in sys.path:
+        sys.path.insert(0, str(ROOT))
+    import __graft_entry__
+    return __graft_entry__.load_package()
+
+
+class IntrplDescC(C.Structure):
+    _fields_ = [("numGrids", C.c_uint32), ("dimN", C.c_uint32 * 3),
+                ("gridSpacing", C.c_float), ("posMin", C.c_float * 3)]
+
+
+class NLDescC(C.Structure):
+    _fields_ = [("dimN", C.c_uint32 * 3), ("gridSpacing", C.c_float), ("dPlateau", C.c_float),
+                ("posMin", C.c_float * 3), ("numEl", C.c_uint32)]
+
+
+class OrcProtein(C.Structure):
+    _fields_ = [("n", C.c_uint32), ("xyz", C.c_void_p), ("type", C.c_void_p),
+                ("mapped", C.c_void_p), ("charge", C.c_void_p), ("n_modes", C.c_uint32),
+                ("modes", C.c_void_p), ("mode_force", C.c_void_p)]
+
+
+class OrcGrid(C.Structure):
+    _fields_ = [("inner", IntrplDescC), ("inner_data", C.c_void_p),
+                ("outer", IntrplDescC), ("outer_data", C.c_void_p),
+                ("nl", NLDescC), ("nl_grid", C.c_void_p), ("nl_list", C.c_void_p)]
+
+
+class OrcParams(C.Structure):
+    _fields_ = [("num_types", C.c_uint32), ("table", C.c_void_p), ("potshape", C.c_int),
+                ("dielec", C.c_int), ("ffelec", C.c_float)]
+
+
+class OrcGridOpts(C.Structure):
+    _fields_ = [("spacing", C.c_float), ("plateau", C.c_float), ("nl_cutoff", C.c_float),
+                ("margin", C.c_float), ("outer_ext", C.c_uint32), ("n_alphabet", C.c_uint32),
+                ("alphabet", C.c_uint32 * 99)]
+
+
+STATS_DTYPE = np.dtype([("n_grid", "<u4"), ("n_grid_charged", "<u4"), ("n_nl", "<u4"),
+                        ("n_nl_entries", "<u4"), ("n_pairs", "<u4"), ("pad", "<u4"),
+                        ("abs_E", "<f8"), ("abs_F", "<f8"), ("abs_T", "<f8")])
+
+_orc = None
+_ref = None
+
+
+def _p(a):
+    return None if a is None else C.c_void_p(a.ctypes.data)
+
+
+def lib():
+    global _orc
+    if _orc is None:
+        if not ORACLE_LIB.exists():
+            raise ImportError(f"oracle not built: {ORACLE_LIB} (make -C oracle)")
+        _orc = C.CDLL(str(ORACLE_LIB))
+        for f in ("orc_energy_6d", "orc_energy_6d_f64", "orc_energy_6d_modes", "orc_minimize_6d",
+                  "orc_minimize_6d_modes", "orc_grid_layout", "orc_grid_build",
+                  "orc_pairwise_energy_f64"):
+            getattr(_orc, f).restype = C.c_int
+    return _orc
+
+
+def ref_available() -> bool:
+    return REF_LIB.exists()
+
+
+def ref_lib():
+    global _ref
+    if _ref is None:
+        if not REF_LIB.exists():
+            raise ImportError(f"reference CPU path not built: {REF_LIB} (oracle/build_ref.sh)")
+        _ref = C.CDLL(str(REF_LIB))
+        _ref.ref_last_error.restype = C.c_char_p
+        for f in ("ref_energy_6d", "ref_energy_6d_modes", "ref_read_pdb", "ref_read_params"):
+            getattr(_ref, f).restype = C.c_int
+    return _ref
+
+
+class _Keep:
+    """Holds numpy arrays alive while their addresses sit in ctypes structs."""
+    def __init__(self):
+        self.arrs = []
+
+    def __call__(self, a, dtype=None):
+        if a is None:
+            return None
+        a = np.ascontiguousarray(a, dtype=dtype)
+        self.arrs.append(a)
+        return a.ctypes.data
+
+
+def protein_c(p, keep: _Keep) -> OrcProtein:
+    c = OrcProtein()
+    c.n = p.n
+    c.xyz = keep(p.xyz, np.float32)
+    c.type = keep(p.type, np.uint32)
+    c.mapped = keep(p.mapped, np.uint32)
+    c.charge = keep(p.charge, np.float32)
+    c.n_modes = p.n_modes
+    c.modes = keep(p.modes, np.float32) if p.n_modes else None
+    c.mode_force = keep(p.mode_force, np.float32) if p.n_modes else None
+    return c
+
+
+def _intrpl(d) -> IntrplDescC:
+    c = IntrplDescC()
+    c.numGrids = d.numGrids
+    for a in range(3):
+        c.dimN[a] = int(d.dimN[a])
+        c.posMin[a] = float(d.posMin[a])
+    c.gridSpacing = float(d.gridSpacing)
+    return c
+
+
+def grid_c(g, keep: _Keep) -> OrcGrid:
+    c = OrcGrid()
+    c.inner = _intrpl(g.inner)
+    c.outer = _intrpl(g.outer)
+    c.inner_data = keep(g.inner_data, np.float32)
+    c.outer_data = keep(g.outer_data, np.float32)
+    for a in range(3):
+        c.nl.dimN[a] = int(g.nl.dimN[a])
+        c.nl.posMin[a] = float(g.nl.posMin[a])
+    c.nl.gridSpacing = float(g.nl.gridSpacing)
+    c.nl.dPlateau = float(g.nl.dPlateau)
+    c.nl.numEl = int(g.nl_list.shape[0])
+    c.nl_grid = keep(g.nl_grid, np.uint32)
+    c.nl_list = keep(g.nl_list if g.nl_list.size else np.zeros(1, np.uint32), np.uint32)
+    return c
+
+
+def params_c(t, keep: _Keep) -> OrcParams:
+    c = OrcParams()
+    c.num_types = t.num_types
+    c.table = keep(t.table)
+    c.potshape = t.potshape
+    c.dielec = t.dielec
+    c.ffelec = float(t.ffelec)
+    return c
+
+
+def _check(rc, what):
+    if rc != 0:
+        raise RuntimeError(f"{what} failed with status {rc}")
+
+
+def energy_6d(rec, lig, grid, params, dofs, stats: bool = False, nthreads: int = 0):
+    """FP32 rigid energies (n, 7) [+ per-pose stats] from the restatement."""
+    k = _Keep()
+    dofs = np.ascontiguousarray(dofs, dtype=np.float32)
+    n = dofs.shape[0]
+    out = np.zeros((n, 7), dtype=np.float32)
+    st = np.zeros(n, dtype=STATS_DTYPE) if stats else None
+    R, L, G, P = protein_c(rec, k), protein_c(lig, k), grid_c(grid, k), params_c(params, k)
+    _check(lib().orc_energy_6d(C.byref(R), C.byref(L), C.byref(G), C.byref(P), _p(dofs),
+                               C.c_size_t(n), _p(out), _p(st), nthreads), "orc_energy_6d")
+    return (out, st) if stats else out
+
+
+def energy_6d_f64(rec, lig, grid, params, dofs, nthreads: int = 0):
+    k = _Keep()
+    dofs = np.ascontiguousarray(dofs, dtype=np.float32)
+    n = dofs.shape[0]
+    out = np.zeros((n, 7), dtype=np.float64)
+    R, L, G, P = protein_c(rec, k), protein_c(lig, k), grid_c(grid, k), params_c(params, k)
+    _check(lib().orc_energy_6d_f64(C.byref(R), C.byref(L), C.byref(G), C.byref(P), _p(dofs),
+                                   C.c_size_t(n), _p(out), nthreads), "orc_energy_6d_f64")
+    return out
+
+
+def energy_6d_modes(rec, lig, grid_rec, grid_lig, params, dofs, stats: bool = False,
+                    nthreads: int = 0):
+    k = _Keep()
+    dofs = np.ascontiguousarray(dofs, dtype=np.float32)
+    n = dofs.shape[0]
+    out = np.zeros((n, 27), dtype=np.float32)
+    st = np.zeros(n, dtype=STATS_DTYPE) if stats else None
+    R, L = protein_c(rec, k), protein_c(lig, k)
+    GR, GL, P = grid_c(grid_rec, k), grid_c(grid_lig, k), params_c(params, k)
+    _check(lib().orc_energy_6d_modes(C.byref(R), C.byref(L), C.byref(GR), C.byref(GL),
+                                     C.byref(P), _p(dofs), C.c_size_t(n), _p(out), _p(st),
+                                     nthreads), "orc_energy_6d_modes")
+    return (out, st) if stats else out
+
+
+def minimize_6d(rec, lig, grid, params, dofs, max_fun_eval: int, nthreads: int = 0):
+    """VA13 per pose: (last state (n,6), last result (n,7), evaluations (n,))."""
+    k = _Keep()
+    dofs = np.ascontiguousarray(dofs, dtype=np.float32)
+    n = dofs.shape[0]
+    st = np.zeros((n, 6), np.float32)
+    res = np.zeros((n, 7), np.float32)
+    nev = np.zeros(n, np.int32)
+    R, L, G, P = protein_c(rec, k), protein_c(lig, k), grid_c(grid, k), params_c(params, k)
+    _check(lib().orc_minimize_6d(C.byref(R), C.byref(L), C.byref(G), C.byref(P), _p(dofs),
+                                 C.c_size_t(n), max_fun_eval, _p(st), _p(res), _p(nev), nthreads),
+           "orc_minimize_6d")
+    return st, res, nev
+
+
+def minimize_6d_modes(rec, lig, grid_rec, grid_lig, params, dofs, max_fun_eval: int,
+                      nthreads: int = 0):
+    k = _Keep()
+    dofs = np.ascontiguousarray(dofs, dtype=np.float32)
+    n = dofs.shape[0]
+    st = np.zeros((n, 26), np.float32)
+    res = np.zeros((n, 27), np.float32)
+    nev = np.zeros(n, np.int32)
+    R, L = protein_c(rec, k), protein_c(lig, k)
+    GR, GL, P = grid_c(grid_rec, k), grid_c(grid_lig, k), params_c(params, k)
+    _check(lib().orc_minimize_6d_modes(C.byref(R), C.byref(L), C.byref(GR), C.byref(GL),
+                                       C.byref(P), _p(dofs), C.c_size_t(n), max_fun_eval,
+                                       _p(st), _p(res), _p(nev), nthreads), "orc_minimize_6d_modes")
+    return st, res, nev
+
+
+def grid_opts_c(opt) -> OrcGridOpts:
+    c = OrcGridOpts()
+    c.spacing, c.plateau, c.nl_cutoff, c.margin = opt.spacing, opt.plateau, opt.nl_cutoff, opt.margin
+    c.outer_ext = opt.outer_ext
+    c.n_alphabet = len(opt.alphabet)
+    for i, t in enumerate(opt.alphabet):
+        c.alphabet[i] = int(t)
+    return c
+
+
+def build_grid(rec, params, opt, nthreads: int = 0):
+    """CPU grid builder (FP64 accumulation) -> gbattract.GridSet."""
+    m = _pkg().model
+    k = _Keep()
+    R, P, O = protein_c(rec, k), params_c(params, k), grid_opts_c(opt)
+    inner, outer, nl = IntrplDescC(), IntrplDescC(), NLDescC()
+    _check(lib().orc_grid_layout(C.byref(R), C.byref(O), C.byref(inner), C.byref(outer),
+                                 C.byref(nl)), "orc_grid_layout")
+    di = np.zeros((inner.numGrids, inner.dimN[2], inner.dimN[1], inner.dimN[0], 4), np.float32)
+    do = np.zeros((outer.numGrids, outer.dimN[2], outer.dimN[1], outer.dimN[0], 4), np.float32)
+    ng = np.zeros((nl.dimN[2], nl.dimN[1], nl.dimN[0], 2), np.uint32)
+    cap = int(ng.shape[0] * ng.shape[1] * ng.shape[2]) * 16
+    while True:
+        lst = np.zeros(max(cap, 1), np.uint32)
+        rc = lib().orc_grid_build(C.byref(R), C.byref(P), C.byref(O), C.byref(inner), _p(di),
+                                  C.byref(outer), _p(do), C.byref(nl), _p(ng), _p(lst),
+                                  C.c_size_t(cap), nthreads)
+        if rc == 0:
+            break
+        if nl.numEl > cap:
+            cap = int(nl.numEl)
+            continue
+        _check(rc, "orc_grid_build")
+    to_i = lambda d: m.IntrplDesc(d.numGrids, tuple(d.dimN), d.gridSpacing, tuple(d.posMin))
+    nld = m.NLDesc(tuple(nl.dimN), nl.gridSpacing, nl.dPlateau, tuple(nl.posMin), nl.numEl)
+    return m.GridSet(to_i(inner), di, to_i(outer), do, nld, ng, lst[:nl.numEl].copy())
+
+
+def pairwise_energy_f64(rec, lig, q_rec, q_lig, r0, eps, dielec, ffelec, cutoff, dofs6):
+    k = _Keep()
+    R, L = protein_c(rec, k), protein_c(lig, k)
+    dofs6 = np.ascontiguousarray(dofs6, np.float64)
+    n = dofs6.shape[0]
+    out = np.zeros(n, np.float64)
+    T = r0.shape[0]
+    _check(lib().orc_pairwise_energy_f64(
+        C.byref(R), C.byref(L), k(q_rec, np.float64), k(q_lig, np.float64), T,
+        k(r0, np.float64), k(eps, np.float64), int(dielec), C.c_double(ffelec),
+        C.c_double(cutoff), _p(dofs6), C.c_size_t(n), _p(out)), "orc_pairwise_energy_f64")
+    return out
+
+
+# ---- the reference's own CPU path ------------------------------------------
+
+def ref_energy_6d(rec, lig, grid, params, dofs, nworkers: int = 2, item_size: int = 100):
+    k = _Keep()
+    dofs = np.ascontiguousarray(dofs, dtype=np.float32)
+    n = dofs.shape[0]
+    out = np.zeros((n, 7), dtype=np.float32)
+    R, L, G, P = protein_c(rec, k), protein_c(lig, k), grid_c(grid, k), params_c(params, k)
+    rc = ref_lib().ref_energy_6d(C.byref(R), C.byref(L), C.byref(G), C.byref(P), _p(dofs),
+                                 C.c_size_t(n), _p(out), nworkers, item_size)
+    if rc != 0:
+        raise RuntimeError(ref_lib().ref_last_error().decode())
+    return out
+
+
+def ref_energy_6d_modes(rec, lig, grid_rec, grid_lig, params, dofs, nworkers: int = 2,
+                        item_size: int = 100):
+    k = _Keep()
+    dofs = np.ascontiguousarray(dofs, dtype=np.float32)
+    n = dofs.shape[0]
+    out = np.zeros((n, 27), dtype=np.float32)
+    R, L = protein_c(rec, k), protein_c(lig, k)
+    GR, GL, P = grid_c(grid_rec, k), grid_c(grid_lig, k), params_c(params, k)
+    rc = ref_lib().ref_energy_6d_modes(C.byref(R), C.byref(L), C.byref(GR), C.byref(GL),
+                                       C.byref(P), _p(dofs), C.c_size_t(n), _p(out), nworkers,
+                                       item_size)
+    if rc != 0:
+        raise RuntimeError(ref_lib().ref_last_error().decode())
+    return out
+
+
+def ref_read_pdb(path: str, default_map: bool = True):
+    """(xyz (3,n), type, charge) through the reference's reduced-PDB reader."""
+    n = ref_lib().ref_read_pdb(str(path).encode(), int(default_map), None, None, None, 0)
+    if n < 0:
+        raise RuntimeError(ref_lib().ref_last_error().decode())
+    xyz = np.zeros((3, n), np.float32)
+    t = np.zeros(n, np.uint32)
+    q = np.zeros(n, np.float32)
+    ref_lib().ref_read_pdb(str(path).encode(), int(default_map), _p(xyz), _p(t), _p(q), n)
+    return xyz, t, q
+
+
+def ref_read_params(path: str):
+    """(table as FFPARAM records, potshape) through the reference's attract.par reader."""
+    ps = C.c_int()
+    T = ref_lib().ref_read_params(str(path).encode(), None, 0, C.byref(ps))
+    if T < 0:
+        raise RuntimeError(ref_lib().ref_last_error().decode())
+    m = _pkg().model
+    tab = np.zeros(T * T, m.FFPARAM_DTYPE)
+    ref_lib().ref_read_params(str(path).encode(), _p(tab), T, C.byref(ps))
+    return tab, ps.value

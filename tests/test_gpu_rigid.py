@@ -1,0 +1,135 @@
+"""Parity of the fused rigid kernel (through the C ABI) with the reference
+CPU path: golden fixtures of the reference's own outputs, the oracle on fresh
+seeded cases, bit-exact census counts, the host- and device-pointer paths and
+the error behaviour.
+
+Tolerance: per pose, |got - ref| / max(|ref|, 0.05 * S) <= 1e-4 for the energy
+and for the force and torque vectors (Euclidean norms), where S is the sum of
+absolute term magnitudes the oracle reports for that pose.  The floor bounds
+the FP32 summation error of heavily cancelling sums (~sqrt(n) * 6e-8 * S)."""
+import numpy as np
+import pytest
+
+from conftest import golden_inputs
+
+pytestmark = pytest.mark.gpu
+
+RTOL = 1e-4
+
+
+def pose_errors(got, ref, st):
+    got = got.astype(np.float64)
+    ref = ref.astype(np.float64)
+    eE = np.abs(got[:, 0] - ref[:, 0]) / np.maximum(np.abs(ref[:, 0]), 0.05 * st["abs_E"] + 1e-30)
+    eF = np.linalg.norm(got[:, 1:4] - ref[:, 1:4], axis=1) / np.maximum(
+        np.linalg.norm(ref[:, 1:4], axis=1), 0.05 * st["abs_F"] + 1e-30)
+    eT = np.linalg.norm(got[:, 4:7] - ref[:, 4:7], axis=1) / np.maximum(
+        np.linalg.norm(ref[:, 4:7], axis=1), 0.05 * st["abs_T"] + 1e-30)
+    return eE, eF, eT
+
+
+@pytest.fixture(scope="module")
+def ctx(pkg):
+    from gbattract.context import GbaContext
+    c = GbaContext(0)
+    yield c
+    c.close()
+
+
+def upload(ctx, rec, lig, grid, params):
+    return (ctx.upload_protein(rec), ctx.upload_protein(lig), ctx.upload_grid(grid),
+            ctx.upload_params(params))
+
+
+@pytest.mark.parametrize("name", ["rigid_synth", "rigid_const", "rigid_pdb"])
+def test_golden_reference_outputs(name, golden_cases, oracle, ctx):
+    d = golden_cases[name]
+    rec, lig, params, opts = golden_inputs(d)
+    grid = oracle.build_grid(rec, params, opts)
+    _, st = oracle.energy_6d(rec, lig, grid, params, d["dofs"], stats=True)
+    got = ctx.energy_6d(*upload(ctx, rec, lig, grid, params), d["dofs"])
+    for e in pose_errors(got, d["ref_out"], st):
+        assert float(e.max()) <= RTOL
+
+
+def test_fresh_case_vs_oracle_and_census(small_case, oracle, ctx):
+    wl, grid = small_case
+    ref, st = oracle.energy_6d(wl.rec, wl.lig, grid, wl.params, wl.dofs, stats=True)
+    ids = upload(ctx, wl.rec, wl.lig, grid, wl.params)
+    got = ctx.energy_6d(*ids, wl.dofs)
+    for e in pose_errors(got, ref, st):
+        assert float(e.max()) <= RTOL
+    cen, res2 = ctx.census_6d(*ids, wl.dofs)
+    # grid indices and neighbour walks are bit-exact: identical counts per pose
+    assert np.array_equal(cen[:, 0], st["n_grid"])
+    assert np.array_equal(cen[:, 1], st["n_grid_charged"])
+    assert np.array_equal(cen[:, 2], st["n_nl"])
+    assert np.array_equal(cen[:, 3], st["n_nl_entries"])
+    assert np.array_equal(res2, got)
+
+
+def test_device_and_host_pointers_agree(small_case, ctx):
+    import torch
+    wl, grid = small_case
+    ids = upload(ctx, wl.rec, wl.lig, grid, wl.params)
+    host = ctx.energy_6d(*ids, wl.dofs)
+    d = torch.from_numpy(wl.dofs).cuda()
+    dev = ctx.energy_6d(*ids, d)
+    torch.cuda.synchronize()
+    assert dev.is_cuda
+    assert np.array_equal(dev.cpu().numpy(), host)
+    pinned = torch.from_numpy(wl.dofs).pin_memory()
+    pin_out = ctx.energy_6d(*ids, pinned)
+    assert np.array_equal(pin_out.numpy(), host)
+
+
+def test_edge_sizes(small_case, oracle, ctx):
+    wl, grid = small_case
+    ids = upload(ctx, wl.rec, wl.lig, grid, wl.params)
+    empty = ctx.energy_6d(*ids, np.zeros((0, 6), np.float32))
+    assert empty.shape == (0, 7)
+    one = ctx.energy_6d(*ids, wl.dofs[:1])
+    ref = oracle.energy_6d(wl.rec, wl.lig, grid, wl.params, wl.dofs[:1])
+    assert np.allclose(one, ref, rtol=1e-4, atol=1e-3 * np.abs(ref).max())
+    # a pose far outside every grid interacts with nothing
+    far = np.array([[500.0, 0, 0, 0.3, 0.2, 0.1]], np.float32)
+    assert np.all(ctx.energy_6d(*ids, far) == 0.0)
+    # odd pose counts that do not fill a warp / block / wave
+    for n in (31, 33, 257):
+        dofs = np.repeat(wl.dofs, (n + len(wl.dofs) - 1) // len(wl.dofs), axis=0)[:n]
+        out = ctx.energy_6d(*ids, dofs)
+        assert np.array_equal(out[: len(wl.dofs)], ctx.energy_6d(*ids, dofs[: len(wl.dofs)]))
+
+
+def test_errors(small_case, pkg, ctx):
+    from gbattract import GbaError
+    wl, grid = small_case
+    rec, lig, g, p = upload(ctx, wl.rec, wl.lig, grid, wl.params)
+    with pytest.raises(GbaError) as e:
+        ctx.energy_6d(rec, lig, g, 9999, wl.dofs)
+    assert e.value.code == 2
+    with pytest.raises(GbaError) as e:
+        ctx.energy_6d(rec, lig, p, g, wl.dofs)      # kinds swapped
+    assert e.value.code == 2
+    bad = pkg.Protein(xyz=wl.lig.xyz, type=wl.lig.type + 40, mapped=wl.lig.mapped,
+                      charge=wl.lig.charge)
+    badid = ctx.upload_protein(bad)
+    with pytest.raises(GbaError) as e:
+        ctx.energy_6d(rec, badid, g, p, wl.dofs)
+    assert e.value.code == 1
+    ctx.release(badid)
+    with pytest.raises(GbaError):
+        ctx.release(badid)
+
+
+def test_fp64_error_statement(small_case, oracle, ctx):
+    """Error of the GPU FP32 result against the FP64 oracle, stated per pose."""
+    wl, grid = small_case
+    ids = upload(ctx, wl.rec, wl.lig, grid, wl.params)
+    got = ctx.energy_6d(*ids, wl.dofs)
+    _, st = oracle.energy_6d(wl.rec, wl.lig, grid, wl.params, wl.dofs, stats=True)
+    ref64 = oracle.energy_6d_f64(wl.rec, wl.lig, grid, wl.params, wl.dofs)
+    eE, eF, eT = pose_errors(got, ref64, st)
+    print(f"FP32 GPU vs FP64 oracle: E max {eE.max():.2e} median {np.median(eE):.2e}; "
+          f"F max {eF.max():.2e}; torque max {eT.max():.2e}")
+    assert float(eE.max()) < 1e-3

@@ -36,6 +36,13 @@ class GridBuildOptsC(C.Structure):
                 ("alphabet", C.c_uint32 * 99)]
 
 
+class PairJobC(C.Structure):
+    _fields_ = [("rec", C.c_uint32), ("lig", C.c_uint32), ("grid", C.c_uint32),
+                ("params", C.c_uint32), ("start", C.c_void_p), ("n", C.c_size_t),
+                ("out_state", C.c_void_p), ("out_result", C.c_void_p),
+                ("out_nevals", C.c_void_p), ("reserved", C.c_void_p)]
+
+
 class GbaError(RuntimeError):
     def __init__(self, code: int, msg: str):
         super().__init__(f"gbattract error {code} ({ERRORS.get(code, '?')}): {msg}")
@@ -73,6 +80,11 @@ def load() -> C.CDLL:
                            C.POINTER(NLDescC)], I),
         "gba_download_grid": ([P, U32, P, P, P, P], I),
         "gba_census_6d": ([P, U32, U32, U32, U32, P, SZ, P, P], I),
+        "gba_minimize_6d": ([P, U32, U32, U32, U32, P, SZ, I, P, P, P, P], I),
+        "gba_minimize_6d_plain": ([P, U32, U32, U32, U32, P, SZ, I, P, P, P, P], I),
+        "gba_batch_minimize_6d": ([P, C.POINTER(PairJobC), SZ, I, P], I),
+        "gba_batch_energy_6d": ([P, C.POINTER(PairJobC), SZ, P], I),
+        "gba_set_deadline": ([P, U32], I),
     }
     for name, (args, res) in {**sig, **optional}.items():
         try:

@@ -184,6 +184,68 @@ class GbaContext:
                                                  _lib.ptr(dofs), n, _lib.ptr(out), stream))
         return out
 
+    # ---- minimization ----------------------------------------------------------
+    def _min_outputs(self, dofs):
+        n = dofs.shape[0]
+        if _is_torch(dofs):
+            import torch
+            return (torch.empty((n, DOF_WIDTH), dtype=torch.float32, device=dofs.device),
+                    torch.empty((n, RESULT_WIDTH), dtype=torch.float32, device=dofs.device),
+                    torch.empty(n, dtype=torch.int32, device=dofs.device))
+        return (np.empty((n, DOF_WIDTH), np.float32), np.empty((n, RESULT_WIDTH), np.float32),
+                np.empty(n, np.int32))
+
+    def minimize_6d(self, rec: int, lig: int, grid: int, params: int, dofs, max_evals: int = 500,
+                    stream=None):
+        """Device-resident VA13 per pose: (last state (n,6), last result (n,7), evals (n,))."""
+        dofs = _check_poses(dofs, DOF_WIDTH, "minimize_6d")
+        st, res, nev = self._min_outputs(dofs)
+        self._check(self.lib.gba_minimize_6d(self.h, rec, lig, grid, params, _lib.ptr(dofs),
+                                             dofs.shape[0], int(max_evals), _lib.ptr(st),
+                                             _lib.ptr(res), _lib.ptr(nev), stream))
+        return st, res, nev
+
+    def minimize_6d_plain(self, rec: int, lig: int, grid: int, params: int, dofs,
+                          max_evals: int = 500, stream=None):
+        """Host VA13 + one energy launch per evaluation round (host arrays only)."""
+        dofs = np.ascontiguousarray(dofs, dtype=np.float32)
+        st, res, nev = self._min_outputs(dofs)
+        self._check(self.lib.gba_minimize_6d_plain(self.h, rec, lig, grid, params, _lib.ptr(dofs),
+                                                   dofs.shape[0], int(max_evals), _lib.ptr(st),
+                                                   _lib.ptr(res), _lib.ptr(nev), stream))
+        return st, res, nev
+
+    def _jobs(self, pairs, with_state: bool):
+        """pairs: list of (rec, lig, grid, params, dofs) -> (ctypes array, outputs)."""
+        jobs = (_lib.PairJobC * len(pairs))()
+        outs = []
+        for k, (rec, lig, grid, params, dofs) in enumerate(pairs):
+            dofs = _check_poses(dofs, DOF_WIDTH, "batch")
+            st, res, nev = self._min_outputs(dofs)
+            j = jobs[k]
+            j.rec, j.lig, j.grid, j.params = rec, lig, grid, params
+            j.start, j.n = _lib.ptr(dofs), dofs.shape[0]
+            j.out_state = _lib.ptr(st) if with_state else None
+            j.out_result = _lib.ptr(res)
+            j.out_nevals = _lib.ptr(nev) if with_state else None
+            outs.append((dofs, st, res, nev))
+        return jobs, outs
+
+    def batch_energy_6d(self, pairs, stream=None):
+        """One launch over the poses of many pairs; returns a list of (n_k, 7) results."""
+        jobs, outs = self._jobs(pairs, with_state=False)
+        self._check(self.lib.gba_batch_energy_6d(self.h, jobs, len(pairs), stream))
+        return [o[2] for o in outs]
+
+    def batch_minimize_6d(self, pairs, max_evals: int = 500, stream=None):
+        """One persistent launch minimizing the poses of many pairs; list of (state, result, evals)."""
+        jobs, outs = self._jobs(pairs, with_state=True)
+        self._check(self.lib.gba_batch_minimize_6d(self.h, jobs, len(pairs), int(max_evals), stream))
+        return [(o[1], o[2], o[3]) for o in outs]
+
+    def set_deadline(self, milliseconds: int):
+        self._check(self.lib.gba_set_deadline(self.h, int(milliseconds)))
+
     def census_6d(self, rec: int, lig: int, grid: int, params: int, dofs):
         """Per-pose counts {n_grid, n_grid_charged, n_nl, n_nl_entries} (n, 4) uint32."""
         dofs = _check_poses(dofs, DOF_WIDTH, "census_6d")

@@ -91,6 +91,30 @@ void* Context::staging(int slot, size_t bytes) {
 	return b.ptr;
 }
 
+void* Context::pinned(int slot, size_t bytes) {
+	if (pinned_bytes[slot] < bytes) {
+		if (pinned_buf[slot]) cudaFreeHost(pinned_buf[slot]);
+		pinned_buf[slot] = nullptr;
+		pinned_bytes[slot] = 0;
+		check_cuda(cudaMallocHost(&pinned_buf[slot], bytes + bytes / 4), "cudaMallocHost");
+		pinned_bytes[slot] = bytes + bytes / 4;
+	}
+	return pinned_buf[slot];
+}
+
+TuneParams Context::tuned(const std::string& kind, size_t) const {
+	auto it = tune.find(kind);
+	return it == tune.end() ? TuneParams{} : it->second;
+}
+
+Context::~Context() {
+	clear_graphs();
+	if (capture_stream) cudaStreamDestroy(capture_stream);
+	if (pinned_status) cudaFreeHost(pinned_status);
+	for (void* p : pinned_buf)
+		if (p) cudaFreeHost(p);
+}
+
 const char* kind_name(ItemKind k) {
 	switch (k) {
 	case ItemKind::Protein: return "protein";
@@ -242,12 +266,12 @@ int gba_upload_protein(gba_ctx* ctx, uint32_t n, const float* xyz, const uint32_
 	item->dev.xyzq = (const float4*)item->xyzq.ptr;
 	item->dev.tm = (const uint32_t*)item->tm.ptr;
 	if (n_modes > 0) {
-		/* reference layout x[i*M+m] | y | z  ->  device [m][axis][i] */
+		/* reference layout x[i*M+m] | y | z  ->  device [i][m][axis] */
 		std::vector<float> md((size_t)n_modes * 3 * n);
 		for (uint32_t a = 0; a < 3; ++a)
 			for (uint32_t i = 0; i < n; ++i)
 				for (uint32_t m = 0; m < n_modes; ++m)
-					md[((size_t)m * 3 + a) * n + i] = modes[(size_t)a * n * n_modes + (size_t)i * n_modes + m];
+					md[((size_t)i * n_modes + m) * 3 + a] = modes[(size_t)a * n * n_modes + (size_t)i * n_modes + m];
 		item->modes.upload(md.data(), md.size() * sizeof(float));
 		item->dev.modes = (const float*)item->modes.ptr;
 		for (uint32_t m = 0; m < n_modes; ++m) item->dev.mode_force[m] = mode_force[m];
@@ -304,6 +328,7 @@ int gba_upload_grid(gba_ctx* ctx, const gba_intrpl_desc* inner, const float* inn
 	for (uint32_t k = 0; k < nl->numEl; ++k) max_idx = std::max(max_idx, nl_list[k]);
 	item->nl_max_index = nl->numEl ? max_idx : 0;
 	item->nl_has_entries = nl->numEl > 0;
+	item->nl_list_radius = (double)nl->dPlateau + 0.5 * std::sqrt(3.0) * (double)nl->gridSpacing;
 	*out = ctx->add(std::move(item));
 	GBA_API_END(ctx)
 }
@@ -349,6 +374,8 @@ int gba_release(gba_ctx* ctx, gba_id id) {
 	if (it == ctx->items.end())
 		throw ApiError(GBA_ERR_UNKNOWN_ID, "gba_release: unknown id " + std::to_string(id));
 	ctx->items.erase(it);
+	ctx->model_cache.clear();
+	ctx->clear_graphs();
 	GBA_API_END(ctx)
 }
 
@@ -376,6 +403,33 @@ int gba_energy_6d(gba_ctx* ctx, gba_id rec, gba_id lig, gba_id grid, gba_id para
 		check_cuda(cudaMemcpyAsync(out, L.out, n * sizeof(gba_result6d), cudaMemcpyDeviceToHost, s),
 				"gba_energy_6d: D2H");
 	if (!din || !dout) check_cuda(cudaStreamSynchronize(s), "gba_energy_6d: sync");
+	GBA_API_END(ctx)
+}
+
+int gba_energy_6d_modes(gba_ctx* ctx, gba_id rec, gba_id lig, gba_id grid_rec, gba_id grid_lig,
+		gba_id params, const gba_dof6d_modes* dofs, size_t n, gba_result6d_modes* out,
+		void* stream) {
+	if (!ctx) return GBA_ERR_INVALID_ARGUMENT;
+	GBA_API_BEGIN
+	if (n == 0) return GBA_OK;
+	if (!dofs || !out) throw ApiError(GBA_ERR_INVALID_ARGUMENT, "gba_energy_6d_modes: null dofs/out");
+	ctx->bind();
+	ModesLaunch L = ctx->modes_launch(rec, lig, grid_rec, grid_lig, params);
+	cudaStream_t s = (cudaStream_t)stream;
+	const bool din = is_device_pointer(dofs), dout = is_device_pointer(out);
+	std::unique_lock<std::mutex> stage_lock(ctx->stage_mu, std::defer_lock);
+	if (!din || !dout) stage_lock.lock();
+	L.n = n;
+	L.dofs = din ? dofs : (const gba_dof6d_modes*)ctx->staging(0, n * sizeof(gba_dof6d_modes));
+	L.out = dout ? out : (gba_result6d_modes*)ctx->staging(1, n * sizeof(gba_result6d_modes));
+	if (!din)
+		check_cuda(cudaMemcpyAsync((void*)L.dofs, dofs, n * sizeof(gba_dof6d_modes),
+				cudaMemcpyHostToDevice, s), "gba_energy_6d_modes: H2D");
+	ctx->run_modes(L, s);
+	if (!dout)
+		check_cuda(cudaMemcpyAsync(out, L.out, n * sizeof(gba_result6d_modes), cudaMemcpyDeviceToHost, s),
+				"gba_energy_6d_modes: D2H");
+	if (!din || !dout) check_cuda(cudaStreamSynchronize(s), "gba_energy_6d_modes: sync");
 	GBA_API_END(ctx)
 }
 
@@ -418,10 +472,10 @@ RigidLaunch Context::rigid_launch(gba_id rec, gba_id lig, gba_id grid, gba_id pa
 	auto* P = static_cast<ParamsItem*>(find(params, ItemKind::Params));
 	validate_pair(*R, *Lg, *G, *P);
 	RigidLaunch L{};
-	L.rec = R->dev;
-	L.lig = Lg->dev;
-	L.grid = G->dev;
-	L.par = P->dev;
+	L.m.rec = R->dev;
+	L.m.lig = Lg->dev;
+	L.m.grid = G->dev;
+	L.m.par = P->dev;
 	return L;
 }
 
@@ -438,6 +492,39 @@ void Context::validate_pair(const ProteinItem& rec, const ProteinItem& lig, cons
 		throw ApiError(GBA_ERR_INVALID_ARGUMENT, "ligand mapped type exceeds the grid's channels");
 	if (g.nl_has_entries && g.nl_max_index >= rec.dev.n)
 		throw ApiError(GBA_ERR_INVALID_ARGUMENT, "neighbour list indexes beyond the receptor");
+}
+
+ModesLaunch Context::modes_launch(gba_id rec, gba_id lig, gba_id grid_rec, gba_id grid_lig,
+		gba_id params) {
+	std::lock_guard<std::mutex> g(mu);
+	auto* R = static_cast<ProteinItem*>(find(rec, ItemKind::Protein));
+	auto* Lg = static_cast<ProteinItem*>(find(lig, ItemKind::Protein));
+	auto* GR = static_cast<GridItem*>(find(grid_rec, ItemKind::Grid));
+	auto* GL = static_cast<GridItem*>(find(grid_lig, ItemKind::Grid));
+	auto* P = static_cast<ParamsItem*>(find(params, ItemKind::Params));
+	validate_pair(*R, *Lg, *GR, *P);
+	/* receptor beads are interpolated in the ligand grid */
+	if (R->max_mapped >= GL->inner_desc.numGrids || R->max_mapped >= GL->outer_desc.numGrids)
+		throw ApiError(GBA_ERR_INVALID_ARGUMENT, "receptor mapped type exceeds the ligand grid's channels");
+	ModesLaunch L{};
+	L.rec = R->dev;
+	L.lig = Lg->dev;
+	L.grid_rec = GR->dev;
+	L.grid_lig = GL->dev;
+	L.par = P->dev;
+	L.rec_modes = R->dev.modes;
+	L.rec_ms = 3 * R->dev.n_modes;
+	L.lig_modes = Lg->dev.modes;
+	L.lig_ms = 3 * Lg->dev.n_modes;
+	return L;
+}
+
+void Context::run_modes(ModesLaunch& L, cudaStream_t s) {
+	const int threads = 256;
+	int bps = modes_blocks_per_sm(threads);
+	size_t want = (L.n + threads / 32 - 1) / (threads / 32);
+	size_t blocks = std::max<size_t>(1, std::min<size_t>(want, (size_t)num_sms * bps));
+	check_cuda(launch_modes_energy(L, (int)blocks, threads, s), "modes energy launch");
 }
 
 void Context::run_rigid(RigidLaunch& L, cudaStream_t s) {

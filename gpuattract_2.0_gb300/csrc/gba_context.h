@@ -4,12 +4,14 @@
 #ifndef GBA_CONTEXT_H_
 #define GBA_CONTEXT_H_
 
+#include <map>
 #include <memory>
 #include <mutex>
 #include <stdexcept>
 #include <string>
 #include <unordered_map>
 #include <vector>
+#include <cstring>
 
 #include "gba_internal.h"
 
@@ -62,6 +64,10 @@ struct GridItem : Item {
 	gba_nl_desc nl_desc{};
 	uint32_t nl_max_index = 0;
 	bool nl_has_entries = false;
+	/* radius around a voxel centre that its list is known to cover: the
+	 * builder's nl_cutoff, or for uploaded grids the least radius the
+	 * reference's NL term relies on (plateau + half a voxel diagonal) */
+	double nl_list_radius = 0.0;
 };
 
 struct ParamsItem : Item {
@@ -75,7 +81,28 @@ DevIntrpl intrpl_from_desc(const gba_intrpl_desc& d);
 DevNL nl_from_desc(const gba_nl_desc& d);
 std::vector<float> nl_ratio_table(float dPlateau2);
 
+/* Launch shape chosen by the autotuner (or the defaults). */
+struct TuneParams {
+	int threads = 128;
+	int blocks_per_sm = 64;   /* capped by occupancy */
+	int chunk = 1;
+};
+
+/* Signature of a captured minimizer pipeline. */
+struct GraphKey {
+	int kind;
+	uintptr_t a, b, c, d, e, f;
+	size_t n;
+	int p0, p1, p2, p3;
+	unsigned long long deadline;
+	bool operator<(const GraphKey& o) const {
+		return std::memcmp(this, &o, sizeof(GraphKey)) < 0;
+	}
+};
+
 struct Context {
+	Context() = default;
+	~Context();
 	int device = 0;
 	int num_sms = 0;
 	std::mutex mu;                 /* items map */
@@ -94,11 +121,28 @@ struct Context {
 	Item* find(gba_id id, ItemKind kind);
 	gba_id add(std::unique_ptr<Item> item);
 	void* staging(int slot, size_t bytes);
+	void* pinned(int slot, size_t bytes);
+
+	/* minimizer / batch state */
+	std::map<std::vector<gba_id>, std::unique_ptr<DevBuffer>> model_cache;
+	DevBuffer pair_buf, aux;
+	int32_t* pinned_status = nullptr;
+	void* pinned_buf[2] = {nullptr, nullptr};
+	size_t pinned_bytes[2] = {0, 0};
+	std::map<GraphKey, cudaGraphExec_t> graphs;
+	cudaStream_t capture_stream = nullptr;
+	uint32_t deadline_ms = 0;
+	std::map<std::string, TuneParams> tune;
+	TuneParams tuned(const std::string& kind, size_t n) const;
+	void run_minimize(MinLaunch& L, cudaStream_t s, int32_t* status_out);
+	void clear_graphs();
 
 	RigidLaunch rigid_launch(gba_id rec, gba_id lig, gba_id grid, gba_id params);
 	void validate_pair(const ProteinItem& rec, const ProteinItem& lig, const GridItem& g,
 			const ParamsItem& p);
 	void run_rigid(RigidLaunch& L, cudaStream_t s);
+	ModesLaunch modes_launch(gba_id rec, gba_id lig, gba_id grid_rec, gba_id grid_lig, gba_id params);
+	void run_modes(ModesLaunch& L, cudaStream_t s);
 };
 
 }  // namespace gba

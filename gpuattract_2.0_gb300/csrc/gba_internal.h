@@ -4,7 +4,8 @@
  * Everything the fused kernels read lives in plain device buffers laid out for
  * one-instruction loads:
  *   protein  : float4 {x, y, z, q} per bead + uint32 {type | mapped << 16}
- *              + modes as (M, 3, n) floats so lane-per-bead reads coalesce
+ *              + modes per bead [i][m][axis] (3M contiguous floats), so a
+ *              neighbour gather reads one short contiguous record
  *   grids    : the reference's channel-major float4 layout (channel 0 =
  *              charge), one buffer per inner/outer grid; derived constants
  *              (maxDim, 1/dVox, 1/voxelVol) precomputed on the host exactly as
@@ -27,7 +28,7 @@ struct DevProtein {
 	uint32_t n_modes;
 	const float4* xyzq;       /* n */
 	const uint32_t* tm;       /* n: type | mapped << 16 */
-	const float* modes;       /* n_modes * 3 * n, [m][axis][i] */
+	const float* modes;       /* n * 3 * n_modes, [i][m][axis] */
 	float mode_force[GBA_MODES_MAX];
 };
 
@@ -74,10 +75,15 @@ struct PoseCensus {
 
 /* ---- launch wrappers (energy_rigid.cu) ----------------------------------- */
 
-struct RigidLaunch {
+/* Everything one rigid receptor-ligand pair's evaluation reads. */
+struct RigidModel {
 	DevProtein rec, lig;
 	DevGrid grid;
 	DevParams par;
+};
+
+struct RigidLaunch {
+	RigidModel m;
 	const gba_dof6d* dofs;
 	gba_result6d* out;
 	PoseCensus* census;       /* nullptr: no census */
@@ -85,6 +91,56 @@ struct RigidLaunch {
 };
 
 cudaError_t launch_rigid_energy(const RigidLaunch& L, int blocks, int threads, cudaStream_t s);
+
+/* ---- persistent minimizer (minimize.cu) ---------------------------------- */
+
+struct MinLaunch {
+	const RigidModel* models;       /* device array, one per pair */
+	const uint32_t* pair_of;        /* per pose pair index; nullptr = pair 0 */
+	const gba_dof6d* start;
+	gba_dof6d* out_state;           /* last evaluated DOF */
+	gba_result6d* out_result;       /* last evaluated Result */
+	int32_t* out_nevals;            /* energy evaluations (may be nullptr) */
+	size_t n;
+	int max_evals;
+	int chunk;                      /* poses claimed per queue grab */
+	unsigned long long* counter;    /* work-queue cursor, zeroed before launch */
+	int* status;                    /* GBA_OK or GBA_ERR_TIMEOUT */
+	unsigned long long budget_ns;   /* per-warp wall-time budget, 0 = none */
+};
+
+cudaError_t launch_minimize_rigid(const MinLaunch& L, int blocks, int threads, cudaStream_t s);
+int minimize_blocks_per_sm(int threads);
+
+/* multi-pair scoring: one launch over the poses of many pairs */
+struct BatchEnergyLaunch {
+	const RigidModel* models;
+	const uint32_t* pair_of;
+	const gba_dof6d* dofs;
+	gba_result6d* out;
+	size_t n;
+};
+
+cudaError_t launch_batch_energy(const BatchEnergyLaunch& L, int blocks, int threads, cudaStream_t s);
+
+/* ---- normal-mode variant (energy_modes.cu) ------------------------------- */
+
+struct ModesLaunch {
+	DevProtein rec, lig;
+	DevGrid grid_rec;         /* receptor grid: ligand beads + NL */
+	DevGrid grid_lig;         /* ligand grid: receptor beads */
+	DevParams par;
+	const float* rec_modes;   /* [i][m][axis] */
+	uint32_t rec_ms;          /* floats per receptor bead record (3*Mr) */
+	const float* lig_modes;
+	uint32_t lig_ms;
+	const gba_dof6d_modes* dofs;
+	gba_result6d_modes* out;
+	size_t n;
+};
+
+cudaError_t launch_modes_energy(const ModesLaunch& L, int blocks, int threads, cudaStream_t s);
+int modes_blocks_per_sm(int threads);
 
 /* Number of resident blocks per SM of the rigid kernel for `threads`. */
 int rigid_blocks_per_sm(int threads, bool census);

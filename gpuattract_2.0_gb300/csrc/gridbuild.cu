@@ -306,6 +306,7 @@ extern "C" int gba_build_grid(gba_ctx* ctx, gba_id rec, gba_id params,
 		item->dev.nl.ratio = (const float*)item->ratio.ptr;
 		item->nl_max_index = R->dev.n - 1;
 		item->nl_has_entries = total > 0;
+		item->nl_list_radius = opt->nl_cutoff;
 		check_cuda(cudaDeviceSynchronize(), "grid build");
 		*out = ctx->add(std::move(item));
 	} catch (const ApiError& e) {

@@ -1,0 +1,341 @@
+/*
+ * minimize_api.cu -- host side of minimization and multi-pair batches.
+ *
+ *   gba_minimize_6d        batched form: one persistent work-queue launch,
+ *                          VA13 on the device, the whole pipeline (cursor
+ *                          reset, copies, kernel) replayed as a cached CUDA graph
+ *   gba_minimize_6d_plain  the reference's execution model on the same GPU:
+ *                          VA13 per pose on the host, one energy launch plus
+ *                          host<->device copies per evaluation round
+ *                          (src/apps/em/RequestHandler.tpp:130-216)
+ *   gba_batch_*            many receptor-ligand pairs of uneven sizes in one launch
+ */
+#include <algorithm>
+#include <chrono>
+#include <cstring>
+#include <vector>
+
+#include "gba_context.h"
+#include "va13.cuh"
+
+namespace gba {
+
+namespace {
+
+/* device copies of RigidModel arrays, keyed by the id tuple list */
+const RigidModel* models_on_device(Context* ctx, const std::vector<RigidModel>& m,
+		const std::vector<gba_id>& key, cudaStream_t s) {
+	auto it = ctx->model_cache.find(key);
+	if (it == ctx->model_cache.end()) {
+		auto buf = std::make_unique<DevBuffer>();
+		buf->upload(m.data(), m.size() * sizeof(RigidModel));
+		it = ctx->model_cache.emplace(key, std::move(buf)).first;
+	}
+	(void)s;
+	return (const RigidModel*)it->second->ptr;
+}
+
+struct Placement {
+	bool device;
+	size_t off;       /* offset in the staging arrays when not device */
+};
+
+}  // namespace
+
+/* Runs the persistent minimizer over `total` poses whose inputs/outputs live
+ * in device memory; captured in a CUDA graph cached by launch signature. */
+void Context::run_minimize(MinLaunch& L, cudaStream_t s, int32_t* status_out) {
+	TuneParams tp = tuned("minimize", L.n);
+	const int threads = tp.threads;
+	const int bps = std::min(tp.blocks_per_sm, minimize_blocks_per_sm(threads));
+	const size_t warps = (size_t)num_sms * bps * (threads / 32);
+	size_t blocks = (size_t)num_sms * bps;
+	if (warps > L.n) blocks = std::max<size_t>(1, (L.n * 32 + threads - 1) / threads);
+	L.chunk = tp.chunk;
+	if (!aux.ptr) {
+		aux.alloc(64);
+		check_cuda(cudaMallocHost((void**)&pinned_status, sizeof(int32_t)), "cudaMallocHost");
+	}
+	L.counter = (unsigned long long*)aux.ptr;
+	L.status = (int*)((char*)aux.ptr + 8);
+
+	GraphKey key{};
+	key.kind = 1;
+	key.a = (uintptr_t)L.models;
+	key.b = (uintptr_t)L.pair_of;
+	key.c = (uintptr_t)L.start;
+	key.d = (uintptr_t)L.out_state;
+	key.e = (uintptr_t)L.out_result;
+	key.f = (uintptr_t)L.out_nevals;
+	key.n = L.n;
+	key.p0 = L.max_evals;
+	key.p1 = (int)blocks;
+	key.p2 = threads;
+	key.p3 = L.chunk;
+	key.deadline = L.budget_ns;
+	cudaGraphExec_t exec = nullptr;
+	auto it = graphs.find(key);
+	if (it != graphs.end()) {
+		exec = it->second;
+	} else {
+		if (!capture_stream)
+			check_cuda(cudaStreamCreateWithFlags(&capture_stream, cudaStreamNonBlocking), "stream");
+		check_cuda(cudaStreamBeginCapture(capture_stream, cudaStreamCaptureModeThreadLocal), "capture");
+		cudaMemsetAsync(aux.ptr, 0, 16, capture_stream);
+		cudaError_t le = launch_minimize_rigid(L, (int)blocks, threads, capture_stream);
+		cudaMemcpyAsync(pinned_status, L.status, sizeof(int32_t), cudaMemcpyDeviceToHost, capture_stream);
+		cudaGraph_t g = nullptr;
+		cudaError_t ce = cudaStreamEndCapture(capture_stream, &g);
+		check_cuda(le, "minimize launch (capture)");
+		check_cuda(ce, "end capture");
+		cudaError_t ie = cudaGraphInstantiate(&exec, g, 0);
+		cudaGraphDestroy(g);
+		check_cuda(ie, "graph instantiate");
+		if (graphs.size() > 64) clear_graphs();
+		graphs.emplace(key, exec);
+	}
+	check_cuda(cudaGraphLaunch(exec, s), "graph launch");
+	check_cuda(cudaStreamSynchronize(s), "minimize sync");
+	if (status_out) *status_out = *pinned_status;
+}
+
+void Context::clear_graphs() {
+	for (auto& kv : graphs) cudaGraphExecDestroy(kv.second);
+	graphs.clear();
+}
+
+}  // namespace gba
+
+using namespace gba;
+
+#define GBA_TRY try {
+#define GBA_CATCH(ctx)                                  \
+	}                                                   \
+	catch (const ApiError& e) {                         \
+		(ctx)->set_error(e.what());                     \
+		return e.code;                                  \
+	}                                                   \
+	catch (const std::exception& e) {                   \
+		(ctx)->set_error(e.what());                     \
+		return GBA_ERR_INVALID_ARGUMENT;                \
+	}                                                   \
+	return GBA_OK;
+
+namespace {
+
+/* Gathers the poses of all jobs into device arrays (staging slots 0..2),
+ * returning per-job placements. */
+struct Gathered {
+	std::vector<RigidModel> models;
+	std::vector<gba_id> key;
+	std::vector<uint32_t> pair_of;
+	std::vector<size_t> offset;
+	size_t total = 0;
+};
+
+Gathered gather_jobs(Context* ctx, const gba_pair_job* jobs, size_t njobs) {
+	Gathered G;
+	for (size_t j = 0; j < njobs; ++j) {
+		const gba_pair_job& jb = jobs[j];
+		RigidLaunch L = ctx->rigid_launch(jb.rec, jb.lig, jb.grid, jb.params);
+		G.models.push_back(L.m);
+		G.key.insert(G.key.end(), {jb.rec, jb.lig, jb.grid, jb.params});
+		G.offset.push_back(G.total);
+		G.total += jb.n;
+		if (jb.n && (!jb.start || !jb.out_result))
+			throw ApiError(GBA_ERR_INVALID_ARGUMENT, "batch: job " + std::to_string(j) + " has null pointers");
+	}
+	if (G.total > 0xffffffffull) throw ApiError(GBA_ERR_INVALID_ARGUMENT, "batch: more than 2^32 poses");
+	G.pair_of.resize(G.total);
+	for (size_t j = 0; j < njobs; ++j)
+		std::fill(G.pair_of.begin() + G.offset[j], G.pair_of.begin() + G.offset[j] + jobs[j].n, (uint32_t)j);
+	return G;
+}
+
+void copy_in(void* dst, const void* src, size_t bytes, cudaStream_t s) {
+	check_cuda(cudaMemcpyAsync(dst, src, bytes, is_device_pointer(src) ? cudaMemcpyDeviceToDevice
+			: cudaMemcpyHostToDevice, s), "batch: gather");
+}
+
+void copy_out(void* dst, const void* src, size_t bytes, cudaStream_t s) {
+	check_cuda(cudaMemcpyAsync(dst, src, bytes, is_device_pointer(dst) ? cudaMemcpyDeviceToDevice
+			: cudaMemcpyDeviceToHost, s), "batch: scatter");
+}
+
+}  // namespace
+
+extern "C" {
+
+int gba_minimize_6d(gba_ctx* ctx, gba_id rec, gba_id lig, gba_id grid, gba_id params,
+		const gba_dof6d* start, size_t n, int max_evals, gba_dof6d* out_state,
+		gba_result6d* out_result, int32_t* out_nevals, void* stream) {
+	if (!ctx) return GBA_ERR_INVALID_ARGUMENT;
+	gba_pair_job job{rec, lig, grid, params, start, n, out_state, out_result, out_nevals, nullptr};
+	return gba_batch_minimize_6d(ctx, &job, 1, max_evals, stream);
+}
+
+int gba_batch_minimize_6d(gba_ctx* ctx, const gba_pair_job* jobs, size_t njobs, int max_evals,
+		void* stream) {
+	if (!ctx) return GBA_ERR_INVALID_ARGUMENT;
+	GBA_TRY
+	if (njobs == 0) return GBA_OK;
+	if (!jobs) throw ApiError(GBA_ERR_INVALID_ARGUMENT, "gba_batch_minimize_6d: null jobs");
+	if (max_evals < 0) throw ApiError(GBA_ERR_INVALID_ARGUMENT, "max_evals < 0");
+	for (size_t j = 0; j < njobs; ++j)
+		if (jobs[j].n && !jobs[j].out_state)
+			throw ApiError(GBA_ERR_INVALID_ARGUMENT, "gba_batch_minimize_6d: null out_state");
+	ctx->bind();
+	cudaStream_t s = (cudaStream_t)stream;
+	std::lock_guard<std::mutex> lk(ctx->stage_mu);
+	Gathered G;
+	{
+		std::lock_guard<std::mutex> g(ctx->mu);
+		G = gather_jobs(ctx, jobs, njobs);
+	}
+	if (G.total == 0) return GBA_OK;
+	const size_t n = G.total;
+	const bool single_dev = njobs == 1 && is_device_pointer(jobs[0].start) &&
+			is_device_pointer(jobs[0].out_state) && is_device_pointer(jobs[0].out_result) &&
+			(!jobs[0].out_nevals || is_device_pointer(jobs[0].out_nevals));
+	MinLaunch L{};
+	L.n = n;
+	L.max_evals = max_evals;
+	L.models = models_on_device(ctx, G.models, G.key, s);
+	if (njobs > 1) {
+		ctx->pair_buf.upload(G.pair_of.data(), n * sizeof(uint32_t));
+		L.pair_of = (const uint32_t*)ctx->pair_buf.ptr;
+	}
+	L.budget_ns = (unsigned long long)ctx->deadline_ms * 1000000ull;
+	if (single_dev) {
+		L.start = jobs[0].start;
+		L.out_state = jobs[0].out_state;
+		L.out_result = jobs[0].out_result;
+		L.out_nevals = jobs[0].out_nevals;
+	} else {
+		L.start = (const gba_dof6d*)ctx->staging(0, n * sizeof(gba_dof6d));
+		L.out_state = (gba_dof6d*)ctx->staging(1, n * sizeof(gba_dof6d));
+		L.out_result = (gba_result6d*)ctx->staging(2, n * sizeof(gba_result6d));
+		L.out_nevals = (int32_t*)ctx->staging(3, n * sizeof(int32_t));
+		for (size_t j = 0; j < njobs; ++j)
+			if (jobs[j].n) copy_in((void*)(L.start + G.offset[j]), jobs[j].start, jobs[j].n * sizeof(gba_dof6d), s);
+	}
+	int32_t status = GBA_OK;
+	ctx->run_minimize(L, s, &status);
+	if (!single_dev) {
+		for (size_t j = 0; j < njobs; ++j) {
+			const size_t o = G.offset[j], m = jobs[j].n;
+			if (!m) continue;
+			copy_out(jobs[j].out_state, L.out_state + o, m * sizeof(gba_dof6d), s);
+			copy_out(jobs[j].out_result, L.out_result + o, m * sizeof(gba_result6d), s);
+			if (jobs[j].out_nevals) copy_out(jobs[j].out_nevals, L.out_nevals + o, m * sizeof(int32_t), s);
+		}
+		check_cuda(cudaStreamSynchronize(s), "batch minimize: scatter");
+	}
+	if (status == GBA_ERR_TIMEOUT)
+		throw ApiError(GBA_ERR_TIMEOUT, "minimization stopped: device wall-time budget exhausted");
+	GBA_CATCH(ctx)
+}
+
+int gba_batch_energy_6d(gba_ctx* ctx, const gba_pair_job* jobs, size_t njobs, void* stream) {
+	if (!ctx) return GBA_ERR_INVALID_ARGUMENT;
+	GBA_TRY
+	if (njobs == 0) return GBA_OK;
+	if (!jobs) throw ApiError(GBA_ERR_INVALID_ARGUMENT, "gba_batch_energy_6d: null jobs");
+	ctx->bind();
+	cudaStream_t s = (cudaStream_t)stream;
+	std::lock_guard<std::mutex> lk(ctx->stage_mu);
+	Gathered G;
+	{
+		std::lock_guard<std::mutex> g(ctx->mu);
+		G = gather_jobs(ctx, jobs, njobs);
+	}
+	if (G.total == 0) return GBA_OK;
+	const size_t n = G.total;
+	BatchEnergyLaunch L{};
+	L.n = n;
+	L.models = models_on_device(ctx, G.models, G.key, s);
+	ctx->pair_buf.upload(G.pair_of.data(), n * sizeof(uint32_t));
+	L.pair_of = (const uint32_t*)ctx->pair_buf.ptr;
+	L.dofs = (const gba_dof6d*)ctx->staging(0, n * sizeof(gba_dof6d));
+	L.out = (gba_result6d*)ctx->staging(2, n * sizeof(gba_result6d));
+	for (size_t j = 0; j < njobs; ++j)
+		if (jobs[j].n) copy_in((void*)(L.dofs + G.offset[j]), jobs[j].start, jobs[j].n * sizeof(gba_dof6d), s);
+	const int threads = 256;
+	size_t blocks = std::max<size_t>(1, std::min<size_t>((n + 7) / 8, (size_t)ctx->num_sms * 3));
+	check_cuda(launch_batch_energy(L, (int)blocks, threads, s), "batch energy launch");
+	for (size_t j = 0; j < njobs; ++j)
+		if (jobs[j].n) copy_out(jobs[j].out_result, L.out + G.offset[j], jobs[j].n * sizeof(gba_result6d), s);
+	check_cuda(cudaStreamSynchronize(s), "batch energy");
+	GBA_CATCH(ctx)
+}
+
+int gba_minimize_6d_plain(gba_ctx* ctx, gba_id rec, gba_id lig, gba_id grid, gba_id params,
+		const gba_dof6d* start, size_t n, int max_evals, gba_dof6d* out_state,
+		gba_result6d* out_result, int32_t* out_nevals, void* stream) {
+	if (!ctx) return GBA_ERR_INVALID_ARGUMENT;
+	GBA_TRY
+	if (n == 0) return GBA_OK;
+	if (!start || !out_state || !out_result)
+		throw ApiError(GBA_ERR_INVALID_ARGUMENT, "gba_minimize_6d_plain: null pointer");
+	if (is_device_pointer(start) || is_device_pointer(out_state) || is_device_pointer(out_result))
+		throw ApiError(GBA_ERR_INVALID_ARGUMENT, "gba_minimize_6d_plain: host pointers required");
+	ctx->bind();
+	cudaStream_t s = (cudaStream_t)stream;
+	RigidLaunch L = ctx->rigid_launch(rec, lig, grid, params);
+	std::lock_guard<std::mutex> lk(ctx->stage_mu);
+	/* pinned request/result buffers, like the server's HostPinnedAllocator
+	 * buffers (src/service/GPUEnergyService.tpp:22-23) */
+	gba_dof6d* hin = (gba_dof6d*)ctx->pinned(0, n * sizeof(gba_dof6d));
+	gba_result6d* hout = (gba_result6d*)ctx->pinned(1, n * sizeof(gba_result6d));
+	gba_dof6d* din = (gba_dof6d*)ctx->staging(0, n * sizeof(gba_dof6d));
+	gba_result6d* dout = (gba_result6d*)ctx->staging(1, n * sizeof(gba_result6d));
+	std::vector<VA13<6>> va(n);
+	std::vector<size_t> active(n), next;
+	std::vector<int32_t> nev(n, 0);
+	for (size_t p = 0; p < n; ++p) {
+		const double x0[6] = {start[p].ang[0], start[p].ang[1], start[p].ang[2], start[p].pos[0],
+				start[p].pos[1], start[p].pos[2]};
+		va[p].start(x0, 6, max_evals);
+		active[p] = p;
+	}
+	while (!active.empty()) {
+		const size_t na = active.size();
+		for (size_t k = 0; k < na; ++k) {
+			const double* pt = va[active[k]].point();
+			gba_dof6d& d = hin[k];
+			d.ang[0] = (float)pt[0]; d.ang[1] = (float)pt[1]; d.ang[2] = (float)pt[2];
+			d.pos[0] = (float)pt[3]; d.pos[1] = (float)pt[4]; d.pos[2] = (float)pt[5];
+		}
+		check_cuda(cudaMemcpyAsync(din, hin, na * sizeof(gba_dof6d), cudaMemcpyHostToDevice, s), "plain: H2D");
+		L.dofs = din;
+		L.out = dout;
+		L.n = na;
+		L.census = nullptr;
+		ctx->run_rigid(L, s);
+		check_cuda(cudaMemcpyAsync(hout, dout, na * sizeof(gba_result6d), cudaMemcpyDeviceToHost, s), "plain: D2H");
+		check_cuda(cudaStreamSynchronize(s), "plain: sync");
+		next.clear();
+		for (size_t k = 0; k < na; ++k) {
+			const size_t p = active[k];
+			const gba_result6d& r = hout[k];
+			out_state[p] = hin[k];
+			out_result[p] = r;
+			++nev[p];
+			const double g[6] = {-(double)r.ang[0], -(double)r.ang[1], -(double)r.ang[2],
+					-(double)r.pos[0], -(double)r.pos[1], -(double)r.pos[2]};
+			va[p].provide((double)r.E, g);
+			if (!va[p].done()) next.push_back(p);
+		}
+		active.swap(next);
+	}
+	if (out_nevals) std::memcpy(out_nevals, nev.data(), n * sizeof(int32_t));
+	GBA_CATCH(ctx)
+}
+
+int gba_set_deadline(gba_ctx* ctx, uint32_t milliseconds) {
+	if (!ctx) return GBA_ERR_INVALID_ARGUMENT;
+	ctx->deadline_ms = milliseconds;
+	return GBA_OK;
+}
+
+}  // extern "C"

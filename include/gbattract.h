@@ -167,6 +167,88 @@ int gba_energy_6d_modes(gba_ctx* ctx, gba_id rec, gba_id lig, gba_id grid_rec, g
 		gba_id params, const gba_dof6d_modes* dofs, size_t n, gba_result6d_modes* out,
 		void* stream);
 
+/* ---- minimization and multi-pair batches ----------------------------------- */
+
+/* One receptor-ligand pair's share of a batch.  For gba_batch_energy_6d,
+ * `start` holds the poses and only `out_result` is written. */
+typedef struct {
+	gba_id rec, lig, grid, params;
+	const gba_dof6d* start;      /* n poses (host or device) */
+	size_t n;
+	gba_dof6d* out_state;        /* last evaluated DOF per pose */
+	gba_result6d* out_result;    /* last evaluated Result per pose */
+	int32_t* out_nevals;         /* energy evaluations per pose (may be NULL) */
+	uint64_t* reserved;          /* must be NULL */
+} gba_pair_job;
+
+/* Minimizes every pose with the VA13 quasi-Newton method the reference runs
+ * through emATTRACT (src/apps/em/minfor.f:1-182, src/apps/em/mc11a.f:1-143,
+ * driven by RequestHandler::run, src/apps/em/RequestHandler.tpp:102-216),
+ * entirely on the device: one persistent work-queue launch, the minimizer
+ * state resident on the GPU, the pipeline replayed as a CUDA graph.
+ * Per pose it reports the last evaluated DOF and Result (what
+ * RequestHandler::getResultStates/getResultEnGrads return) and the number of
+ * energy evaluations; max_evals is maxFunEval (500 in the reference,
+ * src/apps/em/VA13Solver.h:66).  Synchronous. */
+int gba_minimize_6d(gba_ctx* ctx, gba_id rec, gba_id lig, gba_id grid, gba_id params,
+		const gba_dof6d* start, size_t n, int max_evals, gba_dof6d* out_state,
+		gba_result6d* out_result, int32_t* out_nevals, void* stream);
+
+/* The same minimization over the poses of many pairs of uneven sizes in one
+ * persistent launch (poses from every pair share one work queue). */
+int gba_batch_minimize_6d(gba_ctx* ctx, const gba_pair_job* jobs, size_t njobs, int max_evals,
+		void* stream);
+
+/* One energy+gradient evaluation for the poses of many pairs in one launch. */
+int gba_batch_energy_6d(gba_ctx* ctx, const gba_pair_job* jobs, size_t njobs, void* stream);
+
+/* The reference's execution model on the same GPU: VA13 per pose on the host
+ * and one fused energy launch (plus host<->device copies and a sync) per
+ * evaluation round, as RequestHandler + Server + GPU service do.  Host
+ * pointers only; results identical in meaning to gba_minimize_6d. */
+int gba_minimize_6d_plain(gba_ctx* ctx, gba_id rec, gba_id lig, gba_id grid, gba_id params,
+		const gba_dof6d* start, size_t n, int max_evals, gba_dof6d* out_state,
+		gba_result6d* out_result, int32_t* out_nevals, void* stream);
+
+/* Wall-time budget for device minimization (0 = none): warps stop claiming
+ * poses once it is spent and the call returns GBA_ERR_TIMEOUT; the
+ * counterpart of Server::setWaitTime (src/server/Server.h:71). */
+int gba_set_deadline(gba_ctx* ctx, uint32_t milliseconds);
+
+/* ---- pairwise (grid-free) path and its adjoint ------------------------------ */
+
+/* Free parameters of the pairwise path.  All arrays are DEVICE pointers.
+ * r0/eps/ipon: num_types^2 entries indexed [rec type - 1][lig type - 1]
+ * (ParamTable::getParams order, src/model/ParamTable.h:78-80), turned into
+ * rc = eps r0^8, ac = eps r0^6 as src/fileIO/readFile.cpp:484-497 does. */
+typedef struct {
+	uint32_t num_types;
+	const float* r0;
+	const float* eps;
+	const int32_t* ipon;
+	const float* q_lig;      /* per ligand bead */
+	const float* q_rec;      /* per receptor bead */
+	int potshape;            /* GBA_POTSHAPE_8_6 */
+	int dielec;
+	float ffelec;
+	float cutoff;            /* pair cutoff (<= what the grid's NL lists cover) */
+} gba_pairwise_params;
+
+/* Exact ATTRACT pair energy over all receptor-ligand pairs within `cutoff`
+ * (the NL pair terms of src/model/neighborlist.h:104-157 without the plateau
+ * subtraction, src/model/forcefield.h), candidates taken from `grid`'s
+ * neighbour lists.  No reference counterpart as an entry point: the reference
+ * has no differentiable scoring.  Device pointers; asynchronous on `stream`.
+ *  forward  (gE == NULL): E_out[n] = energy per pose
+ *  backward (gE != NULL): recomputes everything and writes g_dofs[n*6]
+ *           = gE * dE/dDOF in (pos, ang) order -- i.e. -gE * Result, the
+ *           convention of src/apps/em/meta.h:114-121 -- and ADDS gE-weighted
+ *           dE/dq_lig, dE/dq_rec, dE/dr0, dE/deps into the FP64 arrays. */
+int gba_pairwise_6d(gba_ctx* ctx, gba_id rec, gba_id lig, gba_id grid,
+		const gba_pairwise_params* pp, const gba_dof6d* dofs, size_t n, float* E_out,
+		const float* gE, float* g_dofs, double* g_qlig, double* g_qrec, double* g_r0,
+		double* g_eps, void* stream);
+
 /* ---- grid builder --------------------------------------------------------- */
 
 /* Options of the device grid builder (inner 0.9 A, outer 1.8 A, plateau 10 A,

@@ -1211,44 +1211,131 @@ int orc_grid_build(const orc_protein* rec, const orc_params* par, const orc_grid
 	return GBA_OK;
 }
 
+/* Pairwise path in FP64 (the reference for the adjoint checks).  Poses are
+ * DOF_6D records (pos xyz, ang xyz) in double.  A pair (i, j) counts when
+ * r_ij < cutoff at the pose itself, or -- with ref_dofs6 -- at the reference
+ * pose, so central differences see one smooth function.  LJ follows
+ * LJPotForce (src/model/forcefield.h:30-83) with the ipon/rmin2/emin branch,
+ * Coulomb follows ChargePotForce (:87-146) without the |q q| switch.
+ * out_E[n]; out_grad[n*6] (may be NULL) = dE/dDOF from the analytic forces and
+ * the TorqueMat reduction of src/model/reduction.h:81-103. */
 int orc_pairwise_energy_f64(const orc_protein* rec, const orc_protein* lig,
 		const double* q_rec, const double* q_lig, uint32_t T,
-		const double* r0, const double* eps, int dielec, double ffelec, double cutoff,
-		const double* dofs6, size_t n, double* out_E) {
-	if (!rec || !lig || !q_rec || !q_lig || !r0 || !eps || (n && (!dofs6 || !out_E)))
+		const double* r0, const double* eps, const int32_t* ipon, int dielec, double ffelec,
+		double cutoff, const double* dofs6, const double* ref_dofs6, size_t n, double* out_E,
+		double* out_grad) {
+	if (!rec || !lig || !q_rec || !q_lig || !r0 || !eps || !ipon || (n && (!dofs6 || !out_E)))
 		return GBA_ERR_INVALID_ARGUMENT;
 	const float* RX = rec->xyz; const float* RY = RX + rec->n; const float* RZ = RY + rec->n;
 	const float* LX = lig->xyz; const float* LY = LX + lig->n; const float* LZ = LY + lig->n;
 	const double cut2 = cutoff * cutoff;
 	for (size_t p = 0; p < n; ++p) {
 		const double* s = dofs6 + 6 * p;
-		double m[9];
-		euler2rotmat<double>(s[0], s[1], s[2], m);
-		double E = 0;
+		const double* sr = ref_dofs6 ? ref_dofs6 + 6 * p : s;
+		double m[9], mr[9];
+		euler2rotmat<double>(s[3], s[4], s[5], m);
+		euler2rotmat<double>(sr[3], sr[4], sr[5], mr);
+		double E = 0, F[3] = {0, 0, 0}, Tq[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
 		for (unsigned i = 0; i < lig->n; ++i) {
 			const unsigned tl = lig->type[i];
 			if (tl == 0) continue;
-			double x, y, z;
+			double x, y, z, xr, yr, zr;
 			matvec<double>(m, LX[i], LY[i], LZ[i], x, y, z);
-			x += s[3]; y += s[4]; z += s[5];
+			x += s[0]; y += s[1]; z += s[2];
+			matvec<double>(mr, LX[i], LY[i], LZ[i], xr, yr, zr);
+			xr += sr[0]; yr += sr[1]; zr += sr[2];
+			double fi[3] = {0, 0, 0};
 			for (unsigned j = 0; j < rec->n; ++j) {
 				const unsigned tr = rec->type[j];
 				if (tr == 0) continue;
-				double dx = x - RX[j], dy = y - RY[j], dz = z - RZ[j];
-				double r2 = dx * dx + dy * dy + dz * dz;
-				if (r2 >= cut2) continue;
+				const double ex = xr - RX[j], ey = yr - RY[j], ez = zr - RZ[j];
+				if (ex * ex + ey * ey + ez * ez >= cut2) continue;
+				const double dx = x - RX[j], dy = y - RY[j], dz = z - RZ[j];
+				const double r2 = dx * dx + dy * dy + dz * dz;
 				const size_t k = (size_t)T * (tr - 1) + (tl - 1);
 				const double rc = eps[k] * std::pow(r0[k], 8), ac = eps[k] * std::pow(r0[k], 6);
 				const double ir2 = 1.0 / r2, ir6 = ir2 * ir2 * ir2;
-				E += (rc * ir2 - ac) * ir6;
+				const double vlj = (rc * ir2 - ac) * ir6;
+				const bool ok = ac > 0 && rc > 0;
+				const double emin = ok ? -27.0 * std::pow(ac, 4) / (256.0 * std::pow(rc, 3)) : 0.0;
+				const double rmin2 = ok ? 4.0 * rc / (3.0 * ac) : 0.0;
+				double fb = 6.0 * vlj + 2.0 * rc * ir2 * ir6;
+				if (r2 < rmin2) {
+					E += vlj + (ipon[k] - 1) * emin;
+				} else {
+					E += ipon[k] * vlj;
+					fb *= ipon[k];
+				}
 				const double qq = q_lig[i] * q_rec[j] * ffelec;
-				double dd = dielec == GBA_DIELEC_CONSTANT ? std::sqrt(ir2) - 1.0 / 50.0 : ir2 - 1.0 / 2500.0;
+				double dd, fcf;
+				if (dielec == GBA_DIELEC_CONSTANT) {
+					dd = std::sqrt(ir2) - 1.0 / 50.0;
+					fcf = std::sqrt(ir2);
+				} else {
+					dd = ir2 - 1.0 / 2500.0;
+					fcf = 2.0 * ir2;
+				}
 				if (dd > 0) E += qq * dd;
+				else fcf = 0.0;
+				const double ff = (fb + qq * fcf) * ir2;
+				fi[0] += ff * dx; fi[1] += ff * dy; fi[2] += ff * dz;
+			}
+			const double u[3] = {LX[i], LY[i], LZ[i]};
+			for (int a = 0; a < 3; ++a) {
+				F[a] += fi[a];
+				for (int b = 0; b < 3; ++b) Tq[a][b] += u[b] * fi[a];
 			}
 		}
 		out_E[p] = E;
+		if (out_grad) {
+			double M[3][3][3];
+			euler2torquemat<double>(s[3], s[4], s[5], M);
+			double ang[3] = {0, 0, 0};
+			for (int k = 0; k < 3; ++k)
+				for (int l = 0; l < 3; ++l)
+					for (int c = 0; c < 3; ++c) ang[c] += M[k][c][l] * Tq[k][l];
+			for (int a = 0; a < 3; ++a) {
+				out_grad[6 * p + a] = -F[a];
+				out_grad[6 * p + 3 + a] = -ang[a];
+			}
+		}
 	}
 	return GBA_OK;
+}
+
+}  // extern "C"
+
+/* ------------------------------------------------------------------------ */
+/* minfor on an analytic function (checks the device VA13 state machine)    */
+/* ------------------------------------------------------------------------ */
+
+extern "C" {
+
+/* Runs minfor on the extended Rosenbrock function from x0 (n <= 32) and
+ * records every evaluated point followed by its f: trace[k*(n+1) + ...].
+ * Returns the number of evaluations recorded (at most cap). */
+int orc_minfor_trace(int n, const double* x0, int ivmax, double* trace, int cap) {
+	if (n < 1 || n > 32 || !x0 || !trace) return -1;
+	double x[33];
+	for (int i = 0; i < n; ++i) x[i + 1] = x0[i];
+	int k = 0;
+	auto energy = [&](const double* s, double& f, double* g) {
+		f = 0.0;
+		for (int i = 1; i <= n; ++i) g[i] = 0.0;
+		for (int i = 1; i < n; ++i) {
+			const double a = s[i + 1] - s[i] * s[i], b = 1.0 - s[i];
+			f = f + 100.0 * a * a + b * b;
+			g[i] = g[i] - 400.0 * s[i] * a - 2.0 * b;
+			g[i + 1] = g[i + 1] + 200.0 * a;
+		}
+		if (k < cap) {
+			for (int i = 0; i < n; ++i) trace[(size_t)k * (n + 1) + i] = s[i + 1];
+			trace[(size_t)k * (n + 1) + n] = f;
+		}
+		++k;
+	};
+	minfor(energy, ivmax, x, n);
+	return k < cap ? k : cap;
 }
 
 }  // extern "C"

@@ -120,14 +120,17 @@ int orc_grid_build(const orc_protein* rec, const orc_params* par, const orc_grid
 
 /* ---- pairwise (grid-free) path for the adjoint checks --------------------- */
 
-/* Exact ATTRACT pair energy over all receptor-ligand pairs with r < cutoff,
- * in FP64, for a pose and per-bead charges / per-type-pair (r0, eps) taken
- * as free parameters.  r0/eps are num_types*num_types row-major [rec][lig]
- * (8-6 shape: rc = eps*r0^8, ac = eps*r0^6).  out: E per pose. */
+/* Pairwise (grid-free) energy in FP64 with optional analytic dE/dDOF; see
+ * attract_oracle.cpp.  dofs6 / ref_dofs6: (pos xyz, ang xyz) per pose. */
 int orc_pairwise_energy_f64(const orc_protein* rec, const orc_protein* lig,
 		const double* q_rec, const double* q_lig, uint32_t num_types,
-		const double* r0, const double* eps, int dielec, double ffelec, double cutoff,
-		const double* dofs6 /* ang xyz, pos xyz per pose */, size_t n, double* out_E);
+		const double* r0, const double* eps, const int32_t* ipon, int dielec, double ffelec,
+		double cutoff, const double* dofs6, const double* ref_dofs6, size_t n, double* out_E,
+		double* out_grad);
+
+/* minfor on the extended Rosenbrock function; records each evaluated point
+ * and f (test of the library's VA13 state machine). */
+int orc_minfor_trace(int n, const double* x0, int ivmax, double* trace, int cap);
 
 #ifdef __cplusplus
 }

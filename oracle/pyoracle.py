@@ -276,18 +276,23 @@ def build_grid(rec, params, opt, nthreads: int = 0):
     return m.GridSet(to_i(inner), di, to_i(outer), do, nld, ng, lst[:nl.numEl].copy())
 
 
-def pairwise_energy_f64(rec, lig, q_rec, q_lig, r0, eps, dielec, ffelec, cutoff, dofs6):
+def pairwise_energy_f64(rec, lig, q_rec, q_lig, r0, eps, ipon, dielec, ffelec, cutoff, dofs6,
+                        ref_dofs6=None, grad: bool = False):
+    """FP64 pairwise energies (n,) [and analytic dE/dDOF (n, 6), (pos, ang)]."""
     k = _Keep()
     R, L = protein_c(rec, k), protein_c(lig, k)
     dofs6 = np.ascontiguousarray(dofs6, np.float64)
     n = dofs6.shape[0]
     out = np.zeros(n, np.float64)
+    g = np.zeros((n, 6), np.float64) if grad else None
+    ref = None if ref_dofs6 is None else np.ascontiguousarray(ref_dofs6, np.float64)
     T = r0.shape[0]
     _check(lib().orc_pairwise_energy_f64(
-        C.byref(R), C.byref(L), k(q_rec, np.float64), k(q_lig, np.float64), T,
-        k(r0, np.float64), k(eps, np.float64), int(dielec), C.c_double(ffelec),
-        C.c_double(cutoff), _p(dofs6), C.c_size_t(n), _p(out)), "orc_pairwise_energy_f64")
-    return out
+        C.byref(R), C.byref(L), C.c_void_p(k(q_rec, np.float64)), C.c_void_p(k(q_lig, np.float64)), T,
+        C.c_void_p(k(r0, np.float64)), C.c_void_p(k(eps, np.float64)), C.c_void_p(k(ipon, np.int32)),
+        int(dielec), C.c_double(ffelec), C.c_double(cutoff), _p(dofs6), _p(ref), C.c_size_t(n),
+        _p(out), _p(g)), "orc_pairwise_energy_f64")
+    return (out, g) if grad else out
 
 
 # ---- the reference's own CPU path ------------------------------------------

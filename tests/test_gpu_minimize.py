@@ -1,0 +1,109 @@
+"""Device-resident VA13 minimization.
+
+* The batched device form and the plain per-step form run the same VA13
+  machine on the same per-pose energy code, so their trajectories are
+  identical bit for bit.
+* Against the CPU oracle (VA13 restated from minfor.f/mc11a.f, driving the
+  FP32 CPU energy) the minimized energies agree within 1e-3 relative for at
+  least 99% of poses (line-search branches may split trajectories whose
+  energies differ in the last bits).
+* The evaluation budget bounds every pose; a wall-time budget stops the
+  kernel with GBA_ERR_TIMEOUT and leaves the context usable."""
+import numpy as np
+import pytest
+
+from test_gpu_rigid import upload
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ctx(pkg):
+    from gbattract.context import GbaContext
+    c = GbaContext(0)
+    yield c
+    c.close()
+
+
+@pytest.fixture(scope="module")
+def min_case(pkg, oracle):
+    wl = pkg.synth.make_pair(0, 160, 70, 256, (20.0, 30.0), seed=909)
+    grid = oracle.build_grid(wl.rec, wl.params, pkg.GridOptions())
+    return wl, grid
+
+
+def test_device_equals_plain_form(min_case, ctx):
+    wl, grid = min_case
+    ids = upload(ctx, wl.rec, wl.lig, grid, wl.params)
+    s1, r1, n1 = ctx.minimize_6d(*ids, wl.dofs, max_evals=100)
+    s2, r2, n2 = ctx.minimize_6d_plain(*ids, wl.dofs, max_evals=100)
+    assert np.array_equal(n1, n2)
+    assert np.array_equal(s1, s2)
+    assert np.array_equal(r1, r2)
+    assert n1.min() >= 1 and n1.max() <= 101
+    # the minimizer lowers the energy of the start poses
+    e0 = ctx.energy_6d(*ids, wl.dofs)[:, 0]
+    assert np.mean(r1[:, 0] <= e0 + 1e-6 * np.abs(e0)) > 0.95
+    # the reported result is the energy of the reported state
+    assert np.array_equal(ctx.energy_6d(*ids, s1), r1)
+
+
+def test_against_cpu_oracle_va13(min_case, oracle, ctx):
+    wl, grid = min_case
+    ids = upload(ctx, wl.rec, wl.lig, grid, wl.params)
+    _, r_dev, n_dev = ctx.minimize_6d(*ids, wl.dofs, max_evals=100)
+    _, r_cpu, n_cpu = oracle.minimize_6d(wl.rec, wl.lig, grid, wl.params, wl.dofs, 100)
+    rel = np.abs(r_dev[:, 0].astype(np.float64) - r_cpu[:, 0]) / np.maximum(np.abs(r_cpu[:, 0]), 1e-3)
+    frac = float(np.mean(rel <= 1e-3))
+    print(f"minimized energies within 1e-3: {100 * frac:.1f}% of {len(rel)} poses; "
+          f"identical evaluation counts: {100 * np.mean(n_dev == n_cpu):.1f}%")
+    assert frac >= 0.99
+
+
+def test_batch_equals_single_pairs(pkg, oracle, ctx):
+    pairs, ref = [], []
+    for k, (nr, nl, npz) in enumerate([(120, 50, 40), (200, 90, 7), (90, 40, 65)]):
+        wl = pkg.synth.make_pair(4, nr, nl, npz, (18.0, 28.0), seed=1000 + k)
+        grid = oracle.build_grid(wl.rec, wl.params, pkg.GridOptions())
+        ids = upload(ctx, wl.rec, wl.lig, grid, wl.params)
+        pairs.append((*ids, wl.dofs))
+        ref.append(ctx.minimize_6d(*ids, wl.dofs, max_evals=60))
+    got = ctx.batch_minimize_6d(pairs, max_evals=60)
+    for (s, r, n), (s0, r0, n0) in zip(got, ref):
+        assert np.array_equal(s, s0) and np.array_equal(r, r0) and np.array_equal(n, n0)
+    # multi-pair single evaluation equals per-pair evaluation
+    be = ctx.batch_energy_6d(pairs)
+    for res, p in zip(be, pairs):
+        assert np.array_equal(res, ctx.energy_6d(*p[:4], p[4]))
+
+
+def test_device_pointers_and_zero_budget(min_case, ctx):
+    import torch
+    wl, grid = min_case
+    ids = upload(ctx, wl.rec, wl.lig, grid, wl.params)
+    d = torch.from_numpy(wl.dofs[:50]).cuda()
+    s, r, n = ctx.minimize_6d(*ids, d, max_evals=30)
+    s_h, r_h, n_h = ctx.minimize_6d(*ids, wl.dofs[:50], max_evals=30)
+    assert np.array_equal(s.cpu().numpy(), s_h) and np.array_equal(r.cpu().numpy(), r_h)
+    # maxFunEval = 0: only the starting evaluation
+    s0, r0, n0 = ctx.minimize_6d(*ids, wl.dofs[:10], max_evals=0)
+    assert np.all(n0 == 1)
+    assert np.array_equal(s0, wl.dofs[:10])
+    assert np.array_equal(r0, ctx.energy_6d(*ids, wl.dofs[:10]))
+
+
+def test_wall_time_budget_raises_timeout(pkg, ctx, min_case):
+    from gbattract import GbaError
+    wl, grid = min_case
+    ids = upload(ctx, wl.rec, wl.lig, grid, wl.params)
+    many = np.repeat(wl.dofs, 400, axis=0)       # ~100k poses: far longer than 1 ms
+    ctx.set_deadline(1)
+    try:
+        with pytest.raises(GbaError) as e:
+            ctx.minimize_6d(*ids, many, max_evals=500)
+        assert e.value.code == 5
+    finally:
+        ctx.set_deadline(0)
+    # the context is still usable afterwards
+    s, r, n = ctx.minimize_6d(*ids, wl.dofs[:8], max_evals=20)
+    assert np.all(n >= 1)

@@ -1,0 +1,82 @@
+"""Parity of the fused normal-mode kernel with the reference CPU modes path
+(golden fixture of CPUEnergyService6DModes<float>) and with the oracle.
+
+Tolerance per pose: energy, force and torque as in test_gpu_rigid (1e-4 of
+max(|ref|, 0.05 S)); mode-gradient vectors within 1e-4 of
+max(|ref|, 1e-3 * max over the batch) -- they are sums over every bead of both
+proteins and pass through the delta + 4 k delta^4 correction."""
+import numpy as np
+import pytest
+
+from conftest import golden_inputs
+from test_gpu_rigid import pose_errors, upload
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ctx(pkg):
+    from gbattract.context import GbaContext
+    c = GbaContext(0)
+    yield c
+    c.close()
+
+
+def mode_errors(got, ref, Mr, Ml):
+    errs = []
+    for lo, M in ((7, Mr), (17, Ml)):
+        g = got[:, lo:lo + M].astype(np.float64)
+        r = ref[:, lo:lo + M].astype(np.float64)
+        fin = np.all(np.isfinite(r), axis=1)
+        assert np.array_equal(np.isfinite(g).all(axis=1), fin)
+        g, r = g[fin], r[fin]
+        if len(r) == 0:
+            continue
+        nr = np.linalg.norm(r, axis=1)
+        floor = 1e-3 * nr.max() + 1e-30
+        errs.append(np.linalg.norm(g - r, axis=1) / np.maximum(nr, floor))
+    return np.concatenate(errs) if errs else np.zeros(1)
+
+
+def run_modes(ctx, oracle, rec, lig, params, opts, dofs):
+    gr = oracle.build_grid(rec, params, opts)
+    gl = oracle.build_grid(lig, params, opts)
+    ids = (ctx.upload_protein(rec), ctx.upload_protein(lig), ctx.upload_grid(gr),
+           ctx.upload_grid(gl), ctx.upload_params(params))
+    return ctx.energy_6d_modes(*ids, dofs), gr, gl
+
+
+def test_golden_modes_reference_outputs(golden_cases, oracle, ctx):
+    d = golden_cases["modes_synth"]
+    rec, lig, params, opts = golden_inputs(d)
+    got, gr, gl = run_modes(ctx, oracle, rec, lig, params, opts, d["dofs"])
+    ref = d["ref_out"]
+    _, st = oracle.energy_6d_modes(rec, lig, gr, gl, params, d["dofs"], stats=True)
+    for e in pose_errors(got[:, :7], ref[:, :7], st):
+        assert float(e.max()) <= 1e-4
+    assert float(mode_errors(got, ref, rec.n_modes, lig.n_modes).max()) <= 1e-4
+    # unused mode slots stay zero
+    assert np.all(got[:, 7 + rec.n_modes:17] == 0) and np.all(got[:, 17 + lig.n_modes:] == 0)
+
+
+def test_modes_fresh_case_vs_oracle(pkg, oracle, ctx):
+    wl = pkg.synth.make_pair(2, 130, 70, 96, (16.0, 24.0), n_modes=5, seed=515)
+    opts = pkg.GridOptions()
+    got, gr, gl = run_modes(ctx, oracle, wl.rec, wl.lig, wl.params, opts, wl.dofs)
+    ref, st = oracle.energy_6d_modes(wl.rec, wl.lig, gr, gl, wl.params, wl.dofs, stats=True)
+    for e in pose_errors(got[:, :7], ref[:, :7], st):
+        assert float(e.max()) <= 1e-4
+    assert float(mode_errors(got, ref, 5, 5).max()) <= 1e-4
+
+
+def test_zero_amplitudes_match_rigid(small_case, pkg, oracle, ctx):
+    """With no modes the flexible kernel reduces to the rigid one (ligand side)."""
+    wl, grid = small_case
+    ids = upload(ctx, wl.rec, wl.lig, grid, wl.params)
+    rigid = ctx.energy_6d(*ids, wl.dofs)
+    gl = oracle.build_grid(wl.lig, wl.params, pkg.GridOptions())
+    glid = ctx.upload_grid(gl)
+    d26 = pkg.dofs_modes(wl.dofs)
+    got = ctx.energy_6d_modes(ids[0], ids[1], ids[2], glid, ids[3], d26)
+    assert np.array_equal(got[:, :7], rigid)
+    assert np.all(got[:, 7:] == 0)

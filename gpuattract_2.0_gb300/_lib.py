@@ -85,6 +85,9 @@ def load() -> C.CDLL:
         "gba_batch_minimize_6d": ([P, C.POINTER(PairJobC), SZ, I, P], I),
         "gba_batch_energy_6d": ([P, C.POINTER(PairJobC), SZ, P], I),
         "gba_set_deadline": ([P, U32], I),
+        "gba_set_pose_order": ([P, I], I),
+        "gba_minimize_6d_modes": ([P, U32, U32, U32, U32, U32, P, SZ, I, P, P, P, P], I),
+        "gba_minimize_6d_modes_plain": ([P, U32, U32, U32, U32, U32, P, SZ, I, P, P, P, P], I),
     }
     for name, (args, res) in {**sig, **optional}.items():
         try:

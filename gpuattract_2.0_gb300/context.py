@@ -215,6 +215,34 @@ class GbaContext:
                                                    _lib.ptr(res), _lib.ptr(nev), stream))
         return st, res, nev
 
+    def _modes_min(self, fn, rec, lig, grid_rec, grid_lig, params, dofs, max_evals, stream):
+        n = dofs.shape[0]
+        if _is_torch(dofs):
+            import torch
+            st = torch.empty((n, DOF_MODES_WIDTH), dtype=torch.float32, device=dofs.device)
+            res = torch.empty((n, RESULT_MODES_WIDTH), dtype=torch.float32, device=dofs.device)
+            nev = torch.empty(n, dtype=torch.int32, device=dofs.device)
+        else:
+            st = np.empty((n, DOF_MODES_WIDTH), np.float32)
+            res = np.empty((n, RESULT_MODES_WIDTH), np.float32)
+            nev = np.empty(n, np.int32)
+        self._check(fn(self.h, rec, lig, grid_rec, grid_lig, params, _lib.ptr(dofs), n, int(max_evals),
+                       _lib.ptr(st), _lib.ptr(res), _lib.ptr(nev), stream))
+        return st, res, nev
+
+    def minimize_6d_modes(self, rec, lig, grid_rec, grid_lig, params, dofs, max_evals=500,
+                          stream=None):
+        """Device VA13 over (ang, pos, modesRec, modesLig): (state (n,26), result (n,27), evals)."""
+        dofs = _check_poses(dofs, DOF_MODES_WIDTH, "minimize_6d_modes")
+        return self._modes_min(self.lib.gba_minimize_6d_modes, rec, lig, grid_rec, grid_lig, params,
+                               dofs, max_evals, stream)
+
+    def minimize_6d_modes_plain(self, rec, lig, grid_rec, grid_lig, params, dofs, max_evals=500,
+                                stream=None):
+        dofs = np.ascontiguousarray(dofs, dtype=np.float32)
+        return self._modes_min(self.lib.gba_minimize_6d_modes_plain, rec, lig, grid_rec, grid_lig,
+                               params, dofs, max_evals, stream)
+
     def _jobs(self, pairs, with_state: bool):
         """pairs: list of (rec, lig, grid, params, dofs) -> (ctypes array, outputs)."""
         jobs = (_lib.PairJobC * len(pairs))()
@@ -245,6 +273,10 @@ class GbaContext:
 
     def set_deadline(self, milliseconds: int):
         self._check(self.lib.gba_set_deadline(self.h, int(milliseconds)))
+
+    def set_pose_order(self, enable: bool):
+        """Visit large batches in Morton order of the pose translation (default on)."""
+        self._check(self.lib.gba_set_pose_order(self.h, int(bool(enable))))
 
     def census_6d(self, rec: int, lig: int, grid: int, params: int, dofs):
         """Per-pose counts {n_grid, n_grid_charged, n_nl, n_nl_entries} (n, 4) uint32."""

@@ -27,6 +27,7 @@
  * src/model/transform_modes.cu:154, src/model/reduction_modes.cu:68-69).
  */
 #include "energy_dev.cuh"
+#include "va13.cuh"
 
 namespace gba {
 
@@ -71,14 +72,12 @@ struct RecModeHook {
 
 }  // namespace
 
-__global__ void __launch_bounds__(256) modes_energy_kernel(const ModesLaunch L) {
-	const int lane = threadIdx.x & 31;
-	const size_t warp = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-	const size_t nwarps = ((size_t)gridDim.x * blockDim.x) >> 5;
+/* One pose of the modes energy.  Lane k (k < 26) brings the k-th float of the
+ * DOF_6D_Modes record; returns on lane k (k < 27) the k-th float of the
+ * Result_6D_Modes record.  Only the model fields of L are read. */
+__device__ __forceinline__ float eval_pose_modes(const ModesLaunch& L, const float dv, const int lane) {
 	const uint32_t Mr = L.rec.n_modes, Ml = L.lig.n_modes;
-	for (size_t p = warp; p < L.n; p += nwarps) {
-		const float* d = reinterpret_cast<const float*>(L.dofs + p);
-		const float dv = lane < 26 ? __ldg(d + lane) : 0.f;
+	{
 		const float tx = __shfl_sync(GBA_FULL_MASK, dv, 0);
 		const float ty = __shfl_sync(GBA_FULL_MASK, dv, 1);
 		const float tz = __shfl_sync(GBA_FULL_MASK, dv, 2);
@@ -223,8 +222,96 @@ __global__ void __launch_bounds__(256) modes_energy_kernel(const ModesLaunch L) 
 			if (lane == 7 + m) v = m < (int)Mr ? gR[m] : 0.f;
 			if (lane == 17 + m) v = m < (int)Ml ? gL[m] : 0.f;
 		}
+		return v;
+	}
+}
+
+__global__ void __launch_bounds__(256) modes_energy_kernel(const ModesLaunch L) {
+	const int lane = threadIdx.x & 31;
+	const size_t warp = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+	const size_t nwarps = ((size_t)gridDim.x * blockDim.x) >> 5;
+	for (size_t p = warp; p < L.n; p += nwarps) {
+		const float* d = reinterpret_cast<const float*>(L.dofs + p);
+		const float dv = lane < 26 ? __ldg(d + lane) : 0.f;
+		const float v = eval_pose_modes(L, dv, lane);
 		if (lane < 27) reinterpret_cast<float*>(L.out + p)[lane] = v;
 	}
+}
+
+/* Persistent VA13 over (ang xyz, pos xyz, modesRec[0..Mr), modesLig[0..Ml)):
+ * the minimizer of minimize.cu generalised to 6 + Mr + Ml DOF (minfor.f is
+ * fixed at 6, src/apps/em/minfor.f:16,33). */
+__global__ void __launch_bounds__(256) minimize_modes_kernel(const ModesMinLaunch M) {
+	const int lane = threadIdx.x & 31;
+	const ModesLaunch& L = M.m;
+	const uint32_t Mr = L.rec.n_modes, Ml = L.lig.n_modes;
+	const int jn = 6 + (int)Mr + (int)Ml;
+	for (;;) {
+		unsigned long long slot = 0;
+		if (lane == 0) slot = atomicAdd(M.counter, 1ull);
+		slot = __shfl_sync(GBA_FULL_MASK, slot, 0);
+		if (slot >= M.n) break;
+		const size_t p = (size_t)slot;
+		VA13<6 + 2 * GBA_MODES_MAX> va;
+		/* lane k holds DOF float k (pos, ang, modesRec[10], modesLig[10]) */
+		float dv = lane < 26 ? __ldg(reinterpret_cast<const float*>(M.start + p) + lane) : 0.f;
+		if (lane == 0) {
+			double x0[6 + 2 * GBA_MODES_MAX];
+			const float* s = reinterpret_cast<const float*>(M.start + p);
+			for (int k = 0; k < 3; ++k) { x0[k] = s[3 + k]; x0[3 + k] = s[k]; }
+			for (uint32_t m = 0; m < Mr; ++m) x0[6 + m] = s[6 + m];
+			for (uint32_t m = 0; m < Ml; ++m) x0[6 + Mr + m] = s[16 + m];
+			va.start(x0, jn, M.max_evals);
+		}
+		float v = 0.f;
+		int nev = 0;
+		for (;;) {
+			/* lane 0 scatters the point to be evaluated into the record layout */
+			float rec[26];
+			if (lane == 0) {
+				const double* pt = va.point();
+				for (int k = 0; k < 26; ++k) rec[k] = 0.f;
+				for (int k = 0; k < 3; ++k) { rec[3 + k] = (float)pt[k]; rec[k] = (float)pt[3 + k]; }
+				for (uint32_t m = 0; m < Mr; ++m) rec[6 + m] = (float)pt[6 + m];
+				for (uint32_t m = 0; m < Ml; ++m) rec[16 + m] = (float)pt[6 + Mr + m];
+			}
+#pragma unroll
+			for (int k = 0; k < 26; ++k) {
+				const float t = __shfl_sync(GBA_FULL_MASK, lane == 0 ? rec[k] : 0.f, 0);
+				if (lane == k) dv = t;
+			}
+			v = eval_pose_modes(L, dv, lane);
+			++nev;
+			/* gather the result record on lane 0 */
+			float res[27];
+#pragma unroll
+			for (int k = 0; k < 27; ++k) res[k] = __shfl_sync(GBA_FULL_MASK, v, k);
+			int done = 0;
+			if (lane == 0) {
+				double g[6 + 2 * GBA_MODES_MAX];
+				for (int k = 0; k < 3; ++k) { g[k] = -(double)res[4 + k]; g[3 + k] = -(double)res[1 + k]; }
+				for (uint32_t m = 0; m < Mr; ++m) g[6 + m] = -(double)res[7 + m];
+				for (uint32_t m = 0; m < Ml; ++m) g[6 + Mr + m] = -(double)res[17 + m];
+				va.provide((double)res[0], g);
+				done = va.done();
+			}
+			if (__shfl_sync(GBA_FULL_MASK, done, 0)) break;
+		}
+		if (lane < 27) reinterpret_cast<float*>(M.out_result + p)[lane] = v;
+		if (lane < 26) reinterpret_cast<float*>(M.out_state + p)[lane] = dv;
+		if (lane == 0 && M.out_nevals) M.out_nevals[p] = nev;
+	}
+}
+
+cudaError_t launch_minimize_modes(const ModesMinLaunch& M, int blocks, int threads, cudaStream_t s) {
+	minimize_modes_kernel<<<blocks, threads, 0, s>>>(M);
+	return cudaGetLastError();
+}
+
+int minimize_modes_blocks_per_sm(int threads) {
+	int nb = 0;
+	cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, minimize_modes_kernel, threads, 0);
+	return nb > 0 ? nb : 1;
 }
 
 cudaError_t launch_modes_energy(const ModesLaunch& L, int blocks, int threads, cudaStream_t s) {

@@ -22,7 +22,8 @@ __global__ void __launch_bounds__(256) rigid_energy_kernel(const RigidLaunch L) 
 	const int lane = threadIdx.x & 31;
 	const size_t warp = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
 	const size_t nwarps = ((size_t)gridDim.x * blockDim.x) >> 5;
-	for (size_t p = warp; p < L.n; p += nwarps) {
+	for (size_t k = warp; k < L.n; k += nwarps) {
+		const size_t p = L.order ? (size_t)__ldg(&L.order[k]) : k;
 		const float* dofp = reinterpret_cast<const float*>(L.dofs + p);
 		const float dv = lane < 6 ? __ldg(dofp + lane) : 0.f;
 		const float tx = __shfl_sync(GBA_FULL_MASK, dv, 0);

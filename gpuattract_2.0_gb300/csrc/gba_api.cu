@@ -365,6 +365,12 @@ int gba_upload_params(gba_ctx* ctx, uint32_t num_types, const gba_ffparam* table
 	GBA_API_END(ctx)
 }
 
+int gba_set_pose_order(gba_ctx* ctx, int enable) {
+	if (!ctx) return GBA_ERR_INVALID_ARGUMENT;
+	ctx->order_enabled = enable != 0;
+	return GBA_OK;
+}
+
 int gba_release(gba_ctx* ctx, gba_id id) {
 	if (!ctx) return GBA_ERR_INVALID_ARGUMENT;
 	GBA_API_BEGIN
@@ -528,6 +534,8 @@ void Context::run_modes(ModesLaunch& L, cudaStream_t s) {
 }
 
 void Context::run_rigid(RigidLaunch& L, cudaStream_t s) {
+	StreamScratch scratch;
+	L.order = pose_order(L.dofs, 6, L.n, L.m.grid.outer, s, scratch);
 	const int threads = 256;
 	const int warps_per_block = threads / 32;
 	int bps = rigid_blocks_per_sm(threads, L.census != nullptr);

@@ -39,6 +39,17 @@ struct DevBuffer {
 	void upload(const void* src, size_t b);
 };
 
+/* Stream-ordered scratch: allocated on a stream, freed on it when the
+ * holder goes out of scope (after the work that reads it was enqueued). */
+struct StreamScratch {
+	std::vector<void*> ptrs;
+	cudaStream_t stream = nullptr;
+	void* get(size_t bytes, cudaStream_t s);
+	StreamScratch() = default;
+	StreamScratch(const StreamScratch&) = delete;
+	~StreamScratch();
+};
+
 enum class ItemKind { Protein, Grid, Params };
 const char* kind_name(ItemKind k);
 
@@ -133,6 +144,16 @@ struct Context {
 	cudaStream_t capture_stream = nullptr;
 	uint32_t deadline_ms = 0;
 	std::map<std::string, TuneParams> tune;
+
+	/* spatial visiting order of large batches (pose_order.cu) */
+	static constexpr size_t kOrderMinPoses = 4096;
+	bool order_enabled = true;
+	const uint32_t* pose_order(const void* dofs, size_t stride_floats, size_t n, const DevIntrpl& box,
+			cudaStream_t s, StreamScratch& scratch);
+	DevBuffer order_buf[5];
+	const uint32_t* pose_order_persistent(const void* dofs, size_t stride_floats, size_t n,
+			const DevIntrpl& box, const RigidModel* models, const uint32_t* pair_of, size_t npairs,
+			cudaStream_t s);
 	TuneParams tuned(const std::string& kind, size_t n) const;
 	void run_minimize(MinLaunch& L, cudaStream_t s, int32_t* status_out);
 	void clear_graphs();

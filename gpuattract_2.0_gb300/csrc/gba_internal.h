@@ -87,6 +87,7 @@ struct RigidLaunch {
 	const gba_dof6d* dofs;
 	gba_result6d* out;
 	PoseCensus* census;       /* nullptr: no census */
+	const uint32_t* order;    /* visiting order (nullptr: submission order) */
 	size_t n;
 };
 
@@ -97,6 +98,7 @@ cudaError_t launch_rigid_energy(const RigidLaunch& L, int blocks, int threads, c
 struct MinLaunch {
 	const RigidModel* models;       /* device array, one per pair */
 	const uint32_t* pair_of;        /* per pose pair index; nullptr = pair 0 */
+	const uint32_t* order;          /* queue slot -> pose (nullptr: identity) */
 	const gba_dof6d* start;
 	gba_dof6d* out_state;           /* last evaluated DOF */
 	gba_result6d* out_result;       /* last evaluated Result */
@@ -141,6 +143,20 @@ struct ModesLaunch {
 
 cudaError_t launch_modes_energy(const ModesLaunch& L, int blocks, int threads, cudaStream_t s);
 int modes_blocks_per_sm(int threads);
+
+struct ModesMinLaunch {
+	ModesLaunch m;                  /* model fields; dofs/out/n unused */
+	const gba_dof6d_modes* start;
+	gba_dof6d_modes* out_state;
+	gba_result6d_modes* out_result;
+	int32_t* out_nevals;
+	size_t n;
+	int max_evals;
+	unsigned long long* counter;    /* zeroed before launch */
+};
+
+cudaError_t launch_minimize_modes(const ModesMinLaunch& M, int blocks, int threads, cudaStream_t s);
+int minimize_modes_blocks_per_sm(int threads);
 
 /* Number of resident blocks per SM of the rigid kernel for `threads`. */
 int rigid_blocks_per_sm(int threads, bool census);

@@ -47,7 +47,8 @@ __global__ void __launch_bounds__(256) minimize_rigid_kernel(const MinLaunch L) 
 			break;
 		}
 		const size_t end = min((size_t)(base + L.chunk), L.n);
-		for (size_t p = base; p < end; ++p) {
+		for (size_t slot = base; slot < end; ++slot) {
+			const size_t p = L.order ? (size_t)__ldg(&L.order[slot]) : slot;
 			const RigidModel& M = L.models[L.pair_of ? __ldg(&L.pair_of[p]) : 0u];
 			VA13<6> va;
 			float cur[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};

@@ -62,7 +62,7 @@ void Context::run_minimize(MinLaunch& L, cudaStream_t s, int32_t* status_out) {
 	GraphKey key{};
 	key.kind = 1;
 	key.a = (uintptr_t)L.models;
-	key.b = (uintptr_t)L.pair_of;
+	key.b = (uintptr_t)L.pair_of ^ ((uintptr_t)L.order << 1);
 	key.c = (uintptr_t)L.start;
 	key.d = (uintptr_t)L.out_state;
 	key.e = (uintptr_t)L.out_result;
@@ -219,6 +219,9 @@ int gba_batch_minimize_6d(gba_ctx* ctx, const gba_pair_job* jobs, size_t njobs, 
 		for (size_t j = 0; j < njobs; ++j)
 			if (jobs[j].n) copy_in((void*)(L.start + G.offset[j]), jobs[j].start, jobs[j].n * sizeof(gba_dof6d), s);
 	}
+	/* visit poses grouped by pair, in Morton order of the start translation */
+	L.order = ctx->pose_order_persistent(L.start, 6, n, G.models[0].grid.outer, L.models, L.pair_of,
+			njobs, s);
 	int32_t status = GBA_OK;
 	ctx->run_minimize(L, s, &status);
 	if (!single_dev) {
@@ -324,6 +327,125 @@ int gba_minimize_6d_plain(gba_ctx* ctx, gba_id rec, gba_id lig, gba_id grid, gba
 			const double g[6] = {-(double)r.ang[0], -(double)r.ang[1], -(double)r.ang[2],
 					-(double)r.pos[0], -(double)r.pos[1], -(double)r.pos[2]};
 			va[p].provide((double)r.E, g);
+			if (!va[p].done()) next.push_back(p);
+		}
+		active.swap(next);
+	}
+	if (out_nevals) std::memcpy(out_nevals, nev.data(), n * sizeof(int32_t));
+	GBA_CATCH(ctx)
+}
+
+int gba_minimize_6d_modes(gba_ctx* ctx, gba_id rec, gba_id lig, gba_id grid_rec, gba_id grid_lig,
+		gba_id params, const gba_dof6d_modes* start, size_t n, int max_evals,
+		gba_dof6d_modes* out_state, gba_result6d_modes* out_result, int32_t* out_nevals,
+		void* stream) {
+	if (!ctx) return GBA_ERR_INVALID_ARGUMENT;
+	GBA_TRY
+	if (n == 0) return GBA_OK;
+	if (!start || !out_state || !out_result)
+		throw ApiError(GBA_ERR_INVALID_ARGUMENT, "gba_minimize_6d_modes: null pointer");
+	if (max_evals < 0) throw ApiError(GBA_ERR_INVALID_ARGUMENT, "max_evals < 0");
+	ctx->bind();
+	cudaStream_t s = (cudaStream_t)stream;
+	ModesMinLaunch M{};
+	M.m = ctx->modes_launch(rec, lig, grid_rec, grid_lig, params);
+	std::lock_guard<std::mutex> lk(ctx->stage_mu);
+	const bool dev = is_device_pointer(start) && is_device_pointer(out_state) &&
+			is_device_pointer(out_result) && (!out_nevals || is_device_pointer(out_nevals));
+	M.n = n;
+	M.max_evals = max_evals;
+	if (dev) {
+		M.start = start;
+		M.out_state = out_state;
+		M.out_result = out_result;
+		M.out_nevals = out_nevals;
+	} else {
+		M.start = (const gba_dof6d_modes*)ctx->staging(0, n * sizeof(gba_dof6d_modes));
+		M.out_state = (gba_dof6d_modes*)ctx->staging(1, n * sizeof(gba_dof6d_modes));
+		M.out_result = (gba_result6d_modes*)ctx->staging(2, n * sizeof(gba_result6d_modes));
+		M.out_nevals = (int32_t*)ctx->staging(3, n * sizeof(int32_t));
+		copy_in((void*)M.start, start, n * sizeof(gba_dof6d_modes), s);
+	}
+	if (!ctx->aux.ptr) {
+		ctx->aux.alloc(64);
+		check_cuda(cudaMallocHost((void**)&ctx->pinned_status, sizeof(int32_t)), "cudaMallocHost");
+	}
+	M.counter = (unsigned long long*)((char*)ctx->aux.ptr + 16);
+	check_cuda(cudaMemsetAsync(M.counter, 0, 8, s), "modes minimize: cursor");
+	const int threads = 128;
+	const int bps = minimize_modes_blocks_per_sm(threads);
+	size_t blocks = std::max<size_t>(1, std::min<size_t>((n * 32 + threads - 1) / threads,
+			(size_t)ctx->num_sms * bps));
+	check_cuda(launch_minimize_modes(M, (int)blocks, threads, s), "modes minimize launch");
+	if (!dev) {
+		copy_out(out_state, M.out_state, n * sizeof(gba_dof6d_modes), s);
+		copy_out(out_result, M.out_result, n * sizeof(gba_result6d_modes), s);
+		if (out_nevals) copy_out(out_nevals, M.out_nevals, n * sizeof(int32_t), s);
+	}
+	check_cuda(cudaStreamSynchronize(s), "modes minimize");
+	GBA_CATCH(ctx)
+}
+
+int gba_minimize_6d_modes_plain(gba_ctx* ctx, gba_id rec, gba_id lig, gba_id grid_rec,
+		gba_id grid_lig, gba_id params, const gba_dof6d_modes* start, size_t n, int max_evals,
+		gba_dof6d_modes* out_state, gba_result6d_modes* out_result, int32_t* out_nevals,
+		void* stream) {
+	if (!ctx) return GBA_ERR_INVALID_ARGUMENT;
+	GBA_TRY
+	if (n == 0) return GBA_OK;
+	if (!start || !out_state || !out_result)
+		throw ApiError(GBA_ERR_INVALID_ARGUMENT, "gba_minimize_6d_modes_plain: null pointer");
+	if (is_device_pointer(start) || is_device_pointer(out_state) || is_device_pointer(out_result))
+		throw ApiError(GBA_ERR_INVALID_ARGUMENT, "gba_minimize_6d_modes_plain: host pointers required");
+	ctx->bind();
+	cudaStream_t s = (cudaStream_t)stream;
+	ModesLaunch L = ctx->modes_launch(rec, lig, grid_rec, grid_lig, params);
+	const int Mr = (int)L.rec.n_modes, Ml = (int)L.lig.n_modes, jn = 6 + Mr + Ml;
+	std::lock_guard<std::mutex> lk(ctx->stage_mu);
+	auto* hin = (gba_dof6d_modes*)ctx->pinned(0, n * sizeof(gba_dof6d_modes));
+	auto* hout = (gba_result6d_modes*)ctx->pinned(1, n * sizeof(gba_result6d_modes));
+	auto* din = (gba_dof6d_modes*)ctx->staging(0, n * sizeof(gba_dof6d_modes));
+	auto* dout = (gba_result6d_modes*)ctx->staging(1, n * sizeof(gba_result6d_modes));
+	std::vector<VA13<6 + 2 * GBA_MODES_MAX>> va(n);
+	std::vector<size_t> active(n), next;
+	std::vector<int32_t> nev(n, 0);
+	for (size_t p = 0; p < n; ++p) {
+		double x0[6 + 2 * GBA_MODES_MAX];
+		for (int k = 0; k < 3; ++k) { x0[k] = start[p].rigid.ang[k]; x0[3 + k] = start[p].rigid.pos[k]; }
+		for (int m = 0; m < Mr; ++m) x0[6 + m] = start[p].modesRec[m];
+		for (int m = 0; m < Ml; ++m) x0[6 + Mr + m] = start[p].modesLig[m];
+		va[p].start(x0, jn, max_evals);
+		active[p] = p;
+	}
+	while (!active.empty()) {
+		const size_t na = active.size();
+		for (size_t k = 0; k < na; ++k) {
+			const double* pt = va[active[k]].point();
+			gba_dof6d_modes& d = hin[k];
+			std::memset(&d, 0, sizeof(d));
+			for (int a = 0; a < 3; ++a) { d.rigid.ang[a] = (float)pt[a]; d.rigid.pos[a] = (float)pt[3 + a]; }
+			for (int m = 0; m < Mr; ++m) d.modesRec[m] = (float)pt[6 + m];
+			for (int m = 0; m < Ml; ++m) d.modesLig[m] = (float)pt[6 + Mr + m];
+		}
+		check_cuda(cudaMemcpyAsync(din, hin, na * sizeof(gba_dof6d_modes), cudaMemcpyHostToDevice, s), "H2D");
+		L.dofs = din;
+		L.out = dout;
+		L.n = na;
+		ctx->run_modes(L, s);
+		check_cuda(cudaMemcpyAsync(hout, dout, na * sizeof(gba_result6d_modes), cudaMemcpyDeviceToHost, s), "D2H");
+		check_cuda(cudaStreamSynchronize(s), "plain modes: sync");
+		next.clear();
+		for (size_t k = 0; k < na; ++k) {
+			const size_t p = active[k];
+			const gba_result6d_modes& r = hout[k];
+			out_state[p] = hin[k];
+			out_result[p] = r;
+			++nev[p];
+			double g[6 + 2 * GBA_MODES_MAX];
+			for (int a = 0; a < 3; ++a) { g[a] = -(double)r.rigid.ang[a]; g[3 + a] = -(double)r.rigid.pos[a]; }
+			for (int m = 0; m < Mr; ++m) g[6 + m] = -(double)r.modesRec[m];
+			for (int m = 0; m < Ml; ++m) g[6 + Mr + m] = -(double)r.modesLig[m];
+			va[p].provide((double)r.rigid.E, g);
 			if (!va[p].done()) next.push_back(p);
 		}
 		active.swap(next);

@@ -47,13 +47,13 @@ using Types_6D_Modes = GenericTypes<gba_dof6d_modes, Common_Modes, gba_result6d_
 template <typename T>
 class HostPinnedAllocator : public Allocator<T> {
 public:
-	T* allocateBuffer(size_t size) override {
+	T* allocate(size_t size) override {
 		void* p = nullptr;
 		if (cudaMallocHost(&p, sizeof(T) * (size ? size : 1)) != cudaSuccess)
 			throw std::runtime_error("HostPinnedAllocator: cudaMallocHost failed");
 		return static_cast<T*>(p);
 	}
-	void freeBuffer(T* buffer) override { cudaFreeHost(buffer); }
+	void deallocate(T* buffer, size_t) override { cudaFreeHost(buffer); }
 };
 
 inline void gba_throw(gba_ctx* ctx, int rc) {

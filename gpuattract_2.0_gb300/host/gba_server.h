@@ -53,15 +53,15 @@ template <typename T>
 class Allocator {
 public:
 	virtual ~Allocator() {}
-	virtual T* allocateBuffer(size_t size) = 0;
-	virtual void freeBuffer(T* buffer) = 0;
+	virtual T* allocate(size_t size) = 0;
+	virtual void deallocate(T* buffer, size_t size = 0) = 0;
 };
 
 template <typename T>
 class HostAllocator : public Allocator<T> {
 public:
-	T* allocateBuffer(size_t size) override { return new T[size]; }
-	void freeBuffer(T* buffer) override { delete[] buffer; }
+	T* allocate(size_t size) override { return new T[size]; }
+	void deallocate(T* buffer, size_t) override { delete[] buffer; }
 };
 
 template <typename Input, typename Common>
@@ -200,8 +200,8 @@ public:
 		st->size = req.size();
 		st->common = req.common();
 		if (st->size > 0) {
-			st->in = _service->getInputAllocator()->allocateBuffer(st->size);
-			st->out = _service->getResultAllocator()->allocateBuffer(st->size);
+			st->in = _service->getInputAllocator()->allocate(st->size);
+			st->out = _service->getResultAllocator()->allocate(st->size);
 			std::copy(req.data(), req.data() + st->size, st->in);
 			const size_t nitems = (st->size + _itemSize - 1) / _itemSize;
 			st->items.reserve(nitems);
@@ -274,8 +274,8 @@ private:
 	}
 
 	void releaseBuffers(State& st) {
-		if (st.in) _service->getInputAllocator()->freeBuffer(st.in);
-		if (st.out) _service->getResultAllocator()->freeBuffer(st.out);
+		if (st.in) _service->getInputAllocator()->deallocate(st.in, st.size);
+		if (st.out) _service->getResultAllocator()->deallocate(st.out, st.size);
 		st.in = nullptr;
 		st.out = nullptr;
 	}

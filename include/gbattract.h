@@ -147,6 +147,12 @@ int gba_upload_params(gba_ctx* ctx, uint32_t num_types, const gba_ffparam* table
 /* Drops a data item (DataManager::remove). */
 int gba_release(gba_ctx* ctx, gba_id id);
 
+/* Batches of >= 4096 poses are visited in Morton order of their translation
+ * (results unchanged, each pose keeps its slot) so that the poses resident on
+ * the GPU at a time share grid regions in L2.  Enabled by default; 0 turns it
+ * off.  No reference counterpart (a scheduling choice of this library). */
+int gba_set_pose_order(gba_ctx* ctx, int enable);
+
 /* ---- evaluation ----------------------------------------------------------- */
 
 /* One energy+gradient evaluation per pose (rigid body), the work of one
@@ -209,6 +215,22 @@ int gba_batch_energy_6d(gba_ctx* ctx, const gba_pair_job* jobs, size_t njobs, vo
 int gba_minimize_6d_plain(gba_ctx* ctx, gba_id rec, gba_id lig, gba_id grid, gba_id params,
 		const gba_dof6d* start, size_t n, int max_evals, gba_dof6d* out_state,
 		gba_result6d* out_result, int32_t* out_nevals, void* stream);
+
+/* Minimization of flexible poses: VA13 over the DOF vector (ang xyz, pos xyz,
+ * modesRec[0..Mr), modesLig[0..Ml)) -- minfor.f generalised beyond its fixed
+ * 6 DOF (src/apps/em/minfor.f:16,33) -- with the normal-mode energy of
+ * gba_energy_6d_modes; persistent device kernel, synchronous. */
+int gba_minimize_6d_modes(gba_ctx* ctx, gba_id rec, gba_id lig, gba_id grid_rec, gba_id grid_lig,
+		gba_id params, const gba_dof6d_modes* start, size_t n, int max_evals,
+		gba_dof6d_modes* out_state, gba_result6d_modes* out_result, int32_t* out_nevals,
+		void* stream);
+
+/* Plain per-step form of gba_minimize_6d_modes (host VA13, one launch per
+ * evaluation round); host pointers only. */
+int gba_minimize_6d_modes_plain(gba_ctx* ctx, gba_id rec, gba_id lig, gba_id grid_rec,
+		gba_id grid_lig, gba_id params, const gba_dof6d_modes* start, size_t n, int max_evals,
+		gba_dof6d_modes* out_state, gba_result6d_modes* out_result, int32_t* out_nevals,
+		void* stream);
 
 /* Wall-time budget for device minimization (0 = none): warps stop claiming
  * poses once it is spent and the call returns GBA_ERR_TIMEOUT; the

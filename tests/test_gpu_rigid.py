@@ -101,6 +101,20 @@ def test_edge_sizes(small_case, oracle, ctx):
         assert np.array_equal(out[: len(wl.dofs)], ctx.energy_6d(*ids, dofs[: len(wl.dofs)]))
 
 
+def test_pose_order_does_not_change_results(small_case, ctx):
+    """Large batches are visited in Morton order; every pose keeps its slot."""
+    wl, grid = small_case
+    ids = upload(ctx, wl.rec, wl.lig, grid, wl.params)
+    rng = np.random.default_rng(8)
+    dofs = wl.dofs[rng.integers(0, len(wl.dofs), 6000)]
+    dofs[:, :3] += rng.normal(0, 3.0, (6000, 3)).astype(np.float32)
+    ctx.set_pose_order(False)
+    plain = ctx.energy_6d(*ids, dofs)
+    ctx.set_pose_order(True)
+    ordered = ctx.energy_6d(*ids, dofs)
+    assert np.array_equal(plain, ordered)
+
+
 def test_errors(small_case, pkg, ctx):
     from gbattract import GbaError
     wl, grid = small_case

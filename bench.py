@@ -172,6 +172,174 @@ def run_reference(args):
     return 0
 
 
+def bench_minimization(ctx, pkg, nthreads: int, with_cpu: bool):
+    """Config 0 (receptor 500 / ligand 200 beads, 1000 poses, 100-evaluation VA13):
+    minimized poses/s of the device-resident batched form, of the plain per-step
+    forms (one launch per round; the reference's 100-pose work items) and of the
+    CPU oracle's VA13 on all host threads, with the agreement of the minimized
+    energies."""
+    import torch
+    wl = pkg.synth.make_config(0)
+    rec, lig, par = ctx.upload_protein(wl.rec), ctx.upload_protein(wl.lig), ctx.upload_params(wl.params)
+    grid = ctx.build_grid(rec, par, pkg.GridOptions())
+    ids = (rec, lig, grid, par)
+    n, steps = len(wl.dofs), wl.steps
+    ctx.minimize_6d(*ids, wl.dofs[:128], max_evals=steps)          # warm-up, graph capture
+    ctx.minimize_6d(*ids, wl.dofs, max_evals=steps)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    s_dev, r_dev, n_dev = ctx.minimize_6d(*ids, wl.dofs, max_evals=steps)
+    dt_dev = time.perf_counter() - t0
+    out = {"workload": f"config 0: receptor {wl.rec.n} / ligand {wl.lig.n} beads, {n} poses, "
+                       f"maxFunEval {steps}",
+           "batched_device_poses_per_s": n / dt_dev, "batched_device_s": dt_dev,
+           "evals_per_pose_mean": float(n_dev.mean())}
+    for item, key in ((0, "plain_one_launch_per_round"), (100, "plain_100_pose_items")):
+        ctx.minimize_6d_plain(*ids, wl.dofs[:64], max_evals=10, item_size=item)
+        t0 = time.perf_counter()
+        s_p, r_p, n_p = ctx.minimize_6d_plain(*ids, wl.dofs, max_evals=steps, item_size=item)
+        dt = time.perf_counter() - t0
+        out[key + "_poses_per_s"] = n / dt
+        out[key + "_identical_to_batched"] = bool(np.array_equal(r_p, r_dev))
+    out["speedup_vs_plain_one_launch"] = out["batched_device_poses_per_s"] / out["plain_one_launch_per_round_poses_per_s"]
+    out["speedup_vs_plain_100_pose_items"] = out["batched_device_poses_per_s"] / out["plain_100_pose_items_poses_per_s"]
+    if with_cpu:
+        from oracle import pyoracle as po
+        gh = ctx.download_grid(grid)
+        t0 = time.perf_counter()
+        _, r_cpu, _ = po.minimize_6d(wl.rec, wl.lig, gh, wl.params, wl.dofs, steps, nthreads=nthreads)
+        dt = time.perf_counter() - t0
+        rel = np.abs(r_dev[:, 0].astype(np.float64) - r_cpu[:, 0]) / np.maximum(np.abs(r_cpu[:, 0]), 1e-3)
+        out["cpu_oracle_poses_per_s"] = n / dt
+        out["cpu_cores"] = nthreads
+        out["agreement_within_1e-3"] = float(np.mean(rel <= 1e-3))
+    for i in (grid, lig, rec, par):
+        ctx.release(i)
+    return out
+
+
+def bench_modes(ctx, pkg, n_poses: int, steps: int):
+    """Config 2: receptor 1500 / ligand 600 beads with 5 modes each: modes
+    energy+gradient evals/s, and device vs plain minimization."""
+    import torch
+    wl = pkg.synth.make_config(2, n_poses=n_poses)
+    rec, lig, par = ctx.upload_protein(wl.rec), ctx.upload_protein(wl.lig), ctx.upload_params(wl.params)
+    gr = ctx.build_grid(rec, par, pkg.GridOptions())
+    gl = ctx.build_grid(lig, par, pkg.GridOptions())
+    ids = (rec, lig, gr, gl, par)
+    d = torch.from_numpy(wl.dofs).cuda()
+    out = ctx.energy_6d_modes(*ids, d)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(3):
+        ctx.energy_6d_modes(*ids, d, out=out)
+    torch.cuda.synchronize()
+    evals = 3 * len(wl.dofs) / (time.perf_counter() - t0)
+    sub = wl.dofs[: min(len(wl.dofs), 5000)]
+    ctx.minimize_6d_modes(*ids, sub[:64], max_evals=10)
+    t0 = time.perf_counter()
+    _, r1, n1 = ctx.minimize_6d_modes(*ids, sub, max_evals=steps)
+    dt_dev = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    _, r2, _ = ctx.minimize_6d_modes_plain(*ids, sub, max_evals=steps)
+    dt_plain = time.perf_counter() - t0
+    res = {"workload": f"config 2: receptor {wl.rec.n} / ligand {wl.lig.n} beads, 5+5 modes; "
+                       f"{len(wl.dofs)} poses scored, {len(sub)} minimized (maxFunEval {steps})",
+           "energy_evals_per_s": evals, "minimize_device_poses_per_s": len(sub) / dt_dev,
+           "minimize_plain_poses_per_s": len(sub) / dt_plain, "speedup": dt_plain / dt_dev,
+           "device_equals_plain": bool(np.array_equal(r1, r2)), "evals_per_pose_mean": float(n1.mean())}
+    for i in (gr, gl, lig, rec, par):
+        ctx.release(i)
+    return res
+
+
+def bench_adjoint(ctx, pkg, n_poses: int):
+    """Config 3: pairwise energy forward + hand-written adjoint (autograd) evals/s."""
+    import torch
+    from gbattract.autograd import PairwiseEnergy, PairwiseSystem
+    wl = pkg.synth.make_config(3, n_poses=n_poses)
+    rec, lig, par = ctx.upload_protein(wl.rec), ctx.upload_protein(wl.lig), ctx.upload_params(wl.params)
+    grid = ctx.build_grid(rec, par, pkg.GridOptions())
+    rng = np.random.default_rng(3)
+    T = 32
+    sysm = PairwiseSystem(ctx=ctx, rec=rec, lig=lig, grid=grid,
+                          ipon=torch.ones((T, T), dtype=torch.int32, device="cuda"),
+                          ffelec=wl.params.ffelec)
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a, np.float32)).cuda().requires_grad_(True)
+    d, ql, qr = t(wl.dofs), t(wl.lig.charge), t(wl.rec.charge)
+    r0, eps = t(rng.uniform(3, 5, (T, T))), t(rng.uniform(0.1, 10, (T, T)))
+
+    def fb():
+        for x in (d, ql, qr, r0, eps):
+            x.grad = None
+        E = PairwiseEnergy.apply(d, ql, qr, r0, eps, sysm)
+        E.sum().backward()
+
+    fb()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(3):
+        fb()
+    torch.cuda.synchronize()
+    rate = 3 * len(wl.dofs) / (time.perf_counter() - t0)
+    for i in (grid, lig, rec, par):
+        ctx.release(i)
+    return {"workload": f"config 3: receptor {wl.rec.n} / ligand {wl.lig.n} beads, {len(wl.dofs)} poses, "
+                        "10 A pairwise cutoff", "fwd_bwd_evals_per_s": rate}
+
+
+def bench_batched_uneven(ctx, pkg, pose_scale: float, steps: int):
+    """Config 4: 64 pairs of uneven sizes, each with its own grids, minimized in
+    one persistent launch vs the plain per-step form run pair after pair."""
+    pairs = pkg.synth.make_batch(n_pairs=64, pose_scale=pose_scale)
+    jobs, handles = [], []
+    for wl in pairs:
+        rec, lig, par = ctx.upload_protein(wl.rec), ctx.upload_protein(wl.lig), ctx.upload_params(wl.params)
+        grid = ctx.build_grid(rec, par, pkg.GridOptions())
+        handles += [grid, lig, rec, par]
+        jobs.append((rec, lig, grid, par, wl.dofs))
+    total = sum(len(j[4]) for j in jobs)
+    ctx.batch_minimize_6d([(*j[:4], j[4][:8]) for j in jobs], max_evals=5)      # warm-up
+    t0 = time.perf_counter()
+    got = ctx.batch_minimize_6d(jobs, max_evals=steps)
+    dt_dev = time.perf_counter() - t0
+    # per-pair time to completion inside the persistent launch
+    import ctypes as C
+    from gbattract import _lib
+    cj = (_lib.PairJobC * len(jobs))()
+    keep, done = [], []
+    for k, (rec, lig, grid, par, dofs) in enumerate(jobs):
+        st = np.empty((len(dofs), 6), np.float32)
+        rs = np.empty((len(dofs), 7), np.float32)
+        dn = np.zeros(len(dofs), np.uint64)
+        keep += [dofs, st, rs]
+        done.append(dn)
+        j = cj[k]
+        j.rec, j.lig, j.grid, j.params = rec, lig, grid, par
+        j.start, j.n = dofs.ctypes.data, len(dofs)
+        j.out_state, j.out_result, j.out_nevals, j.out_done_ns = st.ctypes.data, rs.ctypes.data, None, dn.ctypes.data
+    _lib.check(ctx.h, ctx.lib.gba_batch_minimize_6d(ctx.h, cj, len(jobs), steps, None))
+    pair_done_ms = np.array([dn.max() / 1e6 for dn in done])
+    t0 = time.perf_counter()
+    plain_done, plain = [], []
+    for (rec, lig, grid, par, dofs) in jobs:
+        plain.append(ctx.minimize_6d_plain(rec, lig, grid, par, dofs, max_evals=steps))
+        plain_done.append(1e3 * (time.perf_counter() - t0))
+    dt_plain = time.perf_counter() - t0
+    same = all(np.array_equal(a[1], b[1]) for a, b in zip(got, plain))
+    for i in handles:
+        ctx.release(i)
+    pd = np.array(plain_done)
+    return {"workload": f"config 4: 64 pairs, receptor 300-3000 / ligand 100-1500 beads, {total} poses "
+                        f"(pose counts x{pose_scale}), maxFunEval {steps}",
+            "batched_device_poses_per_s": total / dt_dev, "plain_per_step_poses_per_s": total / dt_plain,
+            "speedup": dt_plain / dt_dev, "device_equals_plain": bool(same),
+            "batched_pair_completion_ms_p50": float(np.percentile(pair_done_ms, 50)),
+            "batched_pair_completion_ms_p99": float(np.percentile(pair_done_ms, 99)),
+            "plain_pair_completion_ms_p50": float(np.percentile(pd, 50)),
+            "plain_pair_completion_ms_p99": float(np.percentile(pd, 99))}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -182,6 +350,12 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--ref-sample", type=int, default=2000)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-min", action="store_true", help="skip the minimization report")
+    ap.add_argument("--suite", default="default", choices=["default", "full"],
+                    help="full: also configs 2 (modes), 3 (adjoint), 4 (batched uneven pairs)")
+    ap.add_argument("--modes-poses", type=int, default=50000)
+    ap.add_argument("--batch-scale", type=float, default=0.05,
+                    help="fraction of config 4's pose counts used by --suite full")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -217,6 +391,37 @@ def main():
 
     def step():
         ctx.energy_6d(rec, lig, grid, par, dofs, out=out, stream=sptr)
+
+    def timed_ms(reps=3):
+        ts = []
+        for _ in range(reps):
+            flush.fill_(1.0)
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            step()
+            b.record(stream)
+            torch.cuda.synchronize()
+            ts.append(a.elapsed_time(b))
+        return min(ts)
+
+    # layout / visiting-order variants (short runs); the fastest is timed below
+    variants = {}
+    ref_out = None
+    for order in (False, True):
+        for octets in (False, True):
+            ctx.set_pose_order(order)
+            ctx.grid_octets(grid, octets)
+            step()
+            torch.cuda.synchronize()
+            if ref_out is None:
+                ref_out = out.clone()
+            elif not torch.equal(out, ref_out):
+                raise RuntimeError("variant changed the results")
+            variants[f"order={int(order)},octets={int(octets)}"] = timed_ms()
+    best = min(variants, key=variants.get)
+    ctx.set_pose_order(best.startswith("order=1"))
+    ctx.grid_octets(grid, best.endswith("octets=1"))
+    log("variants (ms): " + json.dumps(variants) + " -> " + best)
 
     for _ in range(args.warmup):
         step()
@@ -274,6 +479,16 @@ def main():
         cpu = {"value": rate, "unit": UNIT, "cores": nthreads, "kind": "port",
                "sample": f"first {ns} poses of the workload ({dt:.1f} s on {nthreads} threads)"}
 
+    minim = None
+    if rank == 0 and not args.no_min:
+        minim = bench_minimization(ctx, pkg, os.cpu_count() or 1, with_cpu=not args.no_cpu)
+    suite = {}
+    if rank == 0 and args.suite == "full":
+        ctx.grid_octets(grid, False)
+        suite["modes"] = bench_modes(ctx, pkg, n_poses=args.modes_poses, steps=200)
+        suite["adjoint"] = bench_adjoint(ctx, pkg, n_poses=10000)
+        suite["batched_uneven"] = bench_batched_uneven(ctx, pkg, pose_scale=args.batch_scale, steps=500)
+
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -287,7 +502,13 @@ def main():
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": None, "peak_source": peak_kind,
                          "bytes_per_launch": bytes_launch},
-            "cpu_baseline": cpu, "clocks": clk.summary(), "gpu_launches": args.steps,
+            "cpu_baseline": cpu, "clocks": clk.summary(),
+            # per step: the fused energy kernel (+ the Morton-key kernel when the visiting
+            # order is on; the CUB radix-sort passes it feeds are library kernels)
+            "gpu_launches": args.steps * (2 if best.startswith("order=1") else 1),
+            "minimization": minim,
+            "variants_ms": variants, "variant_timed": best,
+            "suite": suite or None,
             "wall_s_timed": wall, "host_device_paths_equal": ok,
             "census": {"grid_lookups_per_pose": float(cen[:, 0].mean()),
                        "charged_per_pose": float(cen[:, 1].mean()),

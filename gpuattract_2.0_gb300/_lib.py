@@ -40,7 +40,13 @@ class PairJobC(C.Structure):
     _fields_ = [("rec", C.c_uint32), ("lig", C.c_uint32), ("grid", C.c_uint32),
                 ("params", C.c_uint32), ("start", C.c_void_p), ("n", C.c_size_t),
                 ("out_state", C.c_void_p), ("out_result", C.c_void_p),
-                ("out_nevals", C.c_void_p), ("reserved", C.c_void_p)]
+                ("out_nevals", C.c_void_p), ("out_done_ns", C.c_void_p)]
+
+
+class TuneResultC(C.Structure):
+    _fields_ = [("energy_threads", C.c_int), ("energy_blocks_per_sm", C.c_int),
+                ("minimize_threads", C.c_int), ("minimize_chunk", C.c_int),
+                ("energy_ms", C.c_float), ("minimize_ms", C.c_float), ("from_cache", C.c_int)]
 
 
 class GbaError(RuntimeError):
@@ -81,11 +87,13 @@ def load() -> C.CDLL:
         "gba_download_grid": ([P, U32, P, P, P, P], I),
         "gba_census_6d": ([P, U32, U32, U32, U32, P, SZ, P, P], I),
         "gba_minimize_6d": ([P, U32, U32, U32, U32, P, SZ, I, P, P, P, P], I),
-        "gba_minimize_6d_plain": ([P, U32, U32, U32, U32, P, SZ, I, P, P, P, P], I),
+        "gba_minimize_6d_plain": ([P, U32, U32, U32, U32, P, SZ, I, SZ, P, P, P, P], I),
         "gba_batch_minimize_6d": ([P, C.POINTER(PairJobC), SZ, I, P], I),
         "gba_batch_energy_6d": ([P, C.POINTER(PairJobC), SZ, P], I),
         "gba_set_deadline": ([P, U32], I),
         "gba_set_pose_order": ([P, I], I),
+        "gba_grid_octets": ([P, U32, I], I),
+        "gba_autotune": ([P, U32, U32, U32, U32, P, SZ, I, C.c_char_p, C.POINTER(TuneResultC)], I),
         "gba_minimize_6d_modes": ([P, U32, U32, U32, U32, U32, P, SZ, I, P, P, P, P], I),
         "gba_minimize_6d_modes_plain": ([P, U32, U32, U32, U32, U32, P, SZ, I, P, P, P, P], I),
     }

@@ -206,13 +206,15 @@ class GbaContext:
         return st, res, nev
 
     def minimize_6d_plain(self, rec: int, lig: int, grid: int, params: int, dofs,
-                          max_evals: int = 500, stream=None):
-        """Host VA13 + one energy launch per evaluation round (host arrays only)."""
+                          max_evals: int = 500, item_size: int = 0, stream=None):
+        """Host VA13; per evaluation round one launch per work item of `item_size`
+        active poses (0: one launch per round).  Host arrays only."""
         dofs = np.ascontiguousarray(dofs, dtype=np.float32)
         st, res, nev = self._min_outputs(dofs)
         self._check(self.lib.gba_minimize_6d_plain(self.h, rec, lig, grid, params, _lib.ptr(dofs),
-                                                   dofs.shape[0], int(max_evals), _lib.ptr(st),
-                                                   _lib.ptr(res), _lib.ptr(nev), stream))
+                                                   dofs.shape[0], int(max_evals), int(item_size),
+                                                   _lib.ptr(st), _lib.ptr(res), _lib.ptr(nev),
+                                                   stream))
         return st, res, nev
 
     def _modes_min(self, fn, rec, lig, grid_rec, grid_lig, params, dofs, max_evals, stream):
@@ -273,6 +275,20 @@ class GbaContext:
 
     def set_deadline(self, milliseconds: int):
         self._check(self.lib.gba_set_deadline(self.h, int(milliseconds)))
+
+    def autotune(self, rec: int, lig: int, grid: int, params: int, sample, max_evals: int = 50,
+                 cache_path: str | None = None) -> dict:
+        """Times launch shapes on `sample` poses; returns the chosen shapes."""
+        sample = _check_poses(sample, DOF_WIDTH, "autotune")
+        r = _lib.TuneResultC()
+        self._check(self.lib.gba_autotune(self.h, rec, lig, grid, params, _lib.ptr(sample),
+                                          sample.shape[0], int(max_evals),
+                                          cache_path.encode() if cache_path else None, C.byref(r)))
+        return {k: getattr(r, k) for k, _ in _lib.TuneResultC._fields_}
+
+    def grid_octets(self, grid: int, enable: bool = True):
+        """Adds / drops the duplicated-octet copy of a grid (8x memory, same results)."""
+        self._check(self.lib.gba_grid_octets(self.h, grid, int(bool(enable))))
 
     def set_pose_order(self, enable: bool):
         """Visit large batches in Morton order of the pose translation (default on)."""

@@ -104,7 +104,9 @@ void* Context::pinned(int slot, size_t bytes) {
 
 TuneParams Context::tuned(const std::string& kind, size_t) const {
 	auto it = tune.find(kind);
-	return it == tune.end() ? TuneParams{} : it->second;
+	if (it != tune.end()) return it->second;
+	/* defaults until gba_autotune has run: full occupancy */
+	return kind == "energy" ? TuneParams{256, 64, 1} : TuneParams{128, 64, 1};
 }
 
 Context::~Context() {
@@ -536,9 +538,10 @@ void Context::run_modes(ModesLaunch& L, cudaStream_t s) {
 void Context::run_rigid(RigidLaunch& L, cudaStream_t s) {
 	StreamScratch scratch;
 	L.order = pose_order(L.dofs, 6, L.n, L.m.grid.outer, s, scratch);
-	const int threads = 256;
+	const TuneParams tp = tuned("energy", L.n);
+	const int threads = tp.threads;
 	const int warps_per_block = threads / 32;
-	int bps = rigid_blocks_per_sm(threads, L.census != nullptr);
+	const int bps = std::min(tp.blocks_per_sm, rigid_blocks_per_sm(threads, L.census != nullptr));
 	size_t want = (L.n + warps_per_block - 1) / warps_per_block;
 	size_t blocks = std::min<size_t>(want, (size_t)num_sms * bps);
 	if (blocks == 0) blocks = 1;

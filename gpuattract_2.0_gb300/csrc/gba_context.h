@@ -70,6 +70,7 @@ struct ProteinItem : Item {
 struct GridItem : Item {
 	GridItem() : Item(ItemKind::Grid) {}
 	DevBuffer inner, outer, nlgrid, nllist, ratio;
+	DevBuffer inner_oct, outer_oct;   /* optional duplicated-octet copies */
 	DevGrid dev{};
 	gba_intrpl_desc inner_desc{}, outer_desc{};
 	gba_nl_desc nl_desc{};
@@ -102,7 +103,7 @@ struct TuneParams {
 /* Signature of a captured minimizer pipeline. */
 struct GraphKey {
 	int kind;
-	uintptr_t a, b, c, d, e, f;
+	uintptr_t a, b, c, d, e, f, g;
 	size_t n;
 	int p0, p1, p2, p3;
 	unsigned long long deadline;
@@ -120,7 +121,7 @@ struct Context {
 	std::mutex stage_mu;           /* host-pointer staging buffers */
 	std::unordered_map<gba_id, std::unique_ptr<Item>> items;
 	gba_id next_id = 1;
-	DevBuffer stage[4];
+	DevBuffer stage[6];
 
 	mutable std::mutex err_mu;
 	std::string err;

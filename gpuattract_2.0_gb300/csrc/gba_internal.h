@@ -39,6 +39,10 @@ struct DevIntrpl {
 	float maxDim[3];
 	float dVox, dVox_inv, voxelVol_inv;
 	const float4* data;       /* numGrids * Nx*Ny*Nz */
+	/* optional duplicated-octet copy: per channel and voxel (x<Nx-1, y<Ny-1,
+	 * z<Nz-1) the 8 corners d000 d100 d010 d110 d001 d101 d011 d111 in one
+	 * 128-byte record, so a lookup reads exactly one aligned L2 line */
+	const float4* oct;        /* numGrids * (Nx-1)(Ny-1)(Nz-1) * 8, or nullptr */
 };
 
 struct DevNL {
@@ -109,6 +113,8 @@ struct MinLaunch {
 	unsigned long long* counter;    /* work-queue cursor, zeroed before launch */
 	int* status;                    /* GBA_OK or GBA_ERR_TIMEOUT */
 	unsigned long long budget_ns;   /* per-warp wall-time budget, 0 = none */
+	unsigned long long* t0;         /* earliest warp start (atomicMin), set to ~0 before launch */
+	unsigned long long* done_ns;    /* per pose completion time (globaltimer), may be nullptr */
 };
 
 cudaError_t launch_minimize_rigid(const MinLaunch& L, int blocks, int threads, cudaStream_t s);

@@ -356,3 +356,72 @@ extern "C" int gba_download_grid(gba_ctx* ctx, gba_id grid, float* inner, float*
 	}
 	return GBA_OK;
 }
+
+/* ---- duplicated-octet layout ---------------------------------------------- */
+
+namespace gba {
+namespace {
+
+__global__ void build_octets_kernel(const float4* __restrict__ src, uint32_t Nx, uint32_t Ny,
+		uint32_t Nz, uint32_t C, float4* __restrict__ dst) {
+	const size_t nocts = (size_t)(Nx - 1) * (Ny - 1) * (Nz - 1);
+	const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+	if (t >= nocts * C) return;
+	const size_t c = t / nocts, o = t % nocts;
+	const uint32_t x = (uint32_t)(o % (Nx - 1));
+	const uint32_t y = (uint32_t)((o / (Nx - 1)) % (Ny - 1));
+	const uint32_t z = (uint32_t)(o / ((size_t)(Nx - 1) * (Ny - 1)));
+	const size_t sxy = (size_t)Nx * Ny;
+	const float4* b = src + c * sxy * Nz + (size_t)Nx * ((size_t)z * Ny + y) + x;
+	float4* d = dst + 8 * t;
+	d[0] = b[0];
+	d[1] = b[1];
+	d[2] = b[Nx];
+	d[3] = b[Nx + 1];
+	d[4] = b[sxy];
+	d[5] = b[sxy + 1];
+	d[6] = b[sxy + Nx];
+	d[7] = b[sxy + Nx + 1];
+}
+
+void make_octets(const gba_intrpl_desc& d, const DevBuffer& src, DevBuffer& dst) {
+	const size_t nocts = (size_t)(d.dimN[0] - 1) * (d.dimN[1] - 1) * (d.dimN[2] - 1);
+	const size_t total = nocts * d.numGrids;
+	dst.alloc(total * 8 * sizeof(float4));
+	build_octets_kernel<<<(unsigned)((total + 255) / 256), 256>>>((const float4*)src.ptr, d.dimN[0],
+			d.dimN[1], d.dimN[2], d.numGrids, (float4*)dst.ptr);
+	check_cuda(cudaGetLastError(), "octet layout");
+}
+
+}  // namespace
+}  // namespace gba
+
+extern "C" int gba_grid_octets(gba_ctx* ctx, gba_id grid, int enable) {
+	if (!ctx) return GBA_ERR_INVALID_ARGUMENT;
+	try {
+		ctx->bind();
+		std::lock_guard<std::mutex> lk(ctx->stage_mu);
+		std::lock_guard<std::mutex> g(ctx->mu);
+		auto* G = static_cast<GridItem*>(ctx->find(grid, ItemKind::Grid));
+		if (enable) {
+			if (!G->inner_oct.ptr) make_octets(G->inner_desc, G->inner, G->inner_oct);
+			if (!G->outer_oct.ptr) make_octets(G->outer_desc, G->outer, G->outer_oct);
+			check_cuda(cudaDeviceSynchronize(), "octet layout");
+		} else {
+			G->inner_oct.release();
+			G->outer_oct.release();
+		}
+		G->dev.inner.oct = (const float4*)G->inner_oct.ptr;
+		G->dev.outer.oct = (const float4*)G->outer_oct.ptr;
+		/* cached device copies of the pair descriptors hold the old pointers */
+		ctx->model_cache.clear();
+		ctx->clear_graphs();
+	} catch (const ApiError& e) {
+		ctx->set_error(e.what());
+		return e.code;
+	} catch (const std::exception& e) {
+		ctx->set_error(e.what());
+		return GBA_ERR_INVALID_ARGUMENT;
+	}
+	return GBA_OK;
+}

@@ -36,7 +36,8 @@ __device__ __forceinline__ unsigned long long global_ns() {
 __global__ void __launch_bounds__(256) minimize_rigid_kernel(const MinLaunch L) {
 	__shared__ WarpStage stage[8];   /* one per warp of a <=256-thread block */
 	const int lane = threadIdx.x & 31;
-	const unsigned long long t_start = L.budget_ns ? global_ns() : 0ull;
+	const unsigned long long t_start = global_ns();
+	if (lane == 0 && L.t0) atomicMin(L.t0, t_start);
 	for (;;) {
 		unsigned long long base = 0;
 		if (lane == 0) base = atomicAdd(L.counter, (unsigned long long)L.chunk);
@@ -84,6 +85,7 @@ __global__ void __launch_bounds__(256) minimize_rigid_kernel(const MinLaunch L) 
 			store_result7(reinterpret_cast<float*>(L.out_result + p), res, lane);
 			if (lane < 6) reinterpret_cast<float*>(L.out_state + p)[lane] = cur[lane];
 			if (lane == 0 && L.out_nevals) L.out_nevals[p] = nev;
+			if (lane == 0 && L.done_ns) L.done_ns[p] = global_ns();
 		}
 	}
 }

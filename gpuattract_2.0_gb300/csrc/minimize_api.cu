@@ -56,8 +56,10 @@ void Context::run_minimize(MinLaunch& L, cudaStream_t s, int32_t* status_out) {
 		aux.alloc(64);
 		check_cuda(cudaMallocHost((void**)&pinned_status, sizeof(int32_t)), "cudaMallocHost");
 	}
+	/* aux: [0,8) cursor, [8,12) status, [16,24) modes cursor, [32,40) earliest warp start */
 	L.counter = (unsigned long long*)aux.ptr;
 	L.status = (int*)((char*)aux.ptr + 8);
+	L.t0 = (unsigned long long*)((char*)aux.ptr + 32);
 
 	GraphKey key{};
 	key.kind = 1;
@@ -67,6 +69,7 @@ void Context::run_minimize(MinLaunch& L, cudaStream_t s, int32_t* status_out) {
 	key.d = (uintptr_t)L.out_state;
 	key.e = (uintptr_t)L.out_result;
 	key.f = (uintptr_t)L.out_nevals;
+	key.g = (uintptr_t)L.done_ns;
 	key.n = L.n;
 	key.p0 = L.max_evals;
 	key.p1 = (int)blocks;
@@ -82,6 +85,7 @@ void Context::run_minimize(MinLaunch& L, cudaStream_t s, int32_t* status_out) {
 			check_cuda(cudaStreamCreateWithFlags(&capture_stream, cudaStreamNonBlocking), "stream");
 		check_cuda(cudaStreamBeginCapture(capture_stream, cudaStreamCaptureModeThreadLocal), "capture");
 		cudaMemsetAsync(aux.ptr, 0, 16, capture_stream);
+		cudaMemsetAsync((char*)aux.ptr + 32, 0xff, 8, capture_stream);
 		cudaError_t le = launch_minimize_rigid(L, (int)blocks, threads, capture_stream);
 		cudaMemcpyAsync(pinned_status, L.status, sizeof(int32_t), cudaMemcpyDeviceToHost, capture_stream);
 		cudaGraph_t g = nullptr;
@@ -216,6 +220,11 @@ int gba_batch_minimize_6d(gba_ctx* ctx, const gba_pair_job* jobs, size_t njobs, 
 		L.out_state = (gba_dof6d*)ctx->staging(1, n * sizeof(gba_dof6d));
 		L.out_result = (gba_result6d*)ctx->staging(2, n * sizeof(gba_result6d));
 		L.out_nevals = (int32_t*)ctx->staging(3, n * sizeof(int32_t));
+	}
+	bool want_done = false;
+	for (size_t j = 0; j < njobs; ++j) want_done |= jobs[j].out_done_ns != nullptr && jobs[j].n > 0;
+	if (want_done) L.done_ns = (unsigned long long*)ctx->staging(4, n * sizeof(unsigned long long));
+	if (!single_dev) {
 		for (size_t j = 0; j < njobs; ++j)
 			if (jobs[j].n) copy_in((void*)(L.start + G.offset[j]), jobs[j].start, jobs[j].n * sizeof(gba_dof6d), s);
 	}
@@ -233,6 +242,19 @@ int gba_batch_minimize_6d(gba_ctx* ctx, const gba_pair_job* jobs, size_t njobs, 
 			if (jobs[j].out_nevals) copy_out(jobs[j].out_nevals, L.out_nevals + o, m * sizeof(int32_t), s);
 		}
 		check_cuda(cudaStreamSynchronize(s), "batch minimize: scatter");
+	}
+	if (want_done) {
+		std::vector<unsigned long long> d(n);
+		unsigned long long t0 = 0;
+		check_cuda(cudaMemcpy(d.data(), L.done_ns, n * sizeof(unsigned long long), cudaMemcpyDeviceToHost),
+				"batch minimize: completion times");
+		check_cuda(cudaMemcpy(&t0, L.t0, sizeof(t0), cudaMemcpyDeviceToHost), "batch minimize: start time");
+		for (size_t j = 0; j < njobs; ++j)
+			if (jobs[j].out_done_ns)
+				for (size_t k = 0; k < jobs[j].n; ++k) {
+					const unsigned long long v = d[G.offset[j] + k];
+					jobs[j].out_done_ns[k] = v >= t0 ? v - t0 : 0;
+				}
 	}
 	if (status == GBA_ERR_TIMEOUT)
 		throw ApiError(GBA_ERR_TIMEOUT, "minimization stopped: device wall-time budget exhausted");
@@ -273,7 +295,7 @@ int gba_batch_energy_6d(gba_ctx* ctx, const gba_pair_job* jobs, size_t njobs, vo
 }
 
 int gba_minimize_6d_plain(gba_ctx* ctx, gba_id rec, gba_id lig, gba_id grid, gba_id params,
-		const gba_dof6d* start, size_t n, int max_evals, gba_dof6d* out_state,
+		const gba_dof6d* start, size_t n, int max_evals, size_t item_size, gba_dof6d* out_state,
 		gba_result6d* out_result, int32_t* out_nevals, void* stream) {
 	if (!ctx) return GBA_ERR_INVALID_ARGUMENT;
 	GBA_TRY
@@ -309,13 +331,21 @@ int gba_minimize_6d_plain(gba_ctx* ctx, gba_id rec, gba_id lig, gba_id grid, gba
 			d.ang[0] = (float)pt[0]; d.ang[1] = (float)pt[1]; d.ang[2] = (float)pt[2];
 			d.pos[0] = (float)pt[3]; d.pos[1] = (float)pt[4]; d.pos[2] = (float)pt[5];
 		}
-		check_cuda(cudaMemcpyAsync(din, hin, na * sizeof(gba_dof6d), cudaMemcpyHostToDevice, s), "plain: H2D");
-		L.dofs = din;
-		L.out = dout;
-		L.n = na;
-		L.census = nullptr;
-		ctx->run_rigid(L, s);
-		check_cuda(cudaMemcpyAsync(hout, dout, na * sizeof(gba_result6d), cudaMemcpyDeviceToHost, s), "plain: D2H");
+		/* one round = the active poses cut into work items (src/server/ServerFunctions.h:50),
+		 * each copied in, evaluated by one launch and copied out */
+		const size_t item = item_size ? item_size : na;
+		for (size_t b = 0; b < na; b += item) {
+			const size_t m = std::min(item, na - b);
+			check_cuda(cudaMemcpyAsync(din + b, hin + b, m * sizeof(gba_dof6d), cudaMemcpyHostToDevice, s),
+					"plain: H2D");
+			L.dofs = din + b;
+			L.out = dout + b;
+			L.n = m;
+			L.census = nullptr;
+			ctx->run_rigid(L, s);
+			check_cuda(cudaMemcpyAsync(hout + b, dout + b, m * sizeof(gba_result6d), cudaMemcpyDeviceToHost, s),
+					"plain: D2H");
+		}
 		check_cuda(cudaStreamSynchronize(s), "plain: sync");
 		next.clear();
 		for (size_t k = 0; k < na; ++k) {

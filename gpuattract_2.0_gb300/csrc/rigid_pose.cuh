@@ -100,7 +100,8 @@ __device__ __forceinline__ void stage_bead(const RigidModel& M, const PoseRot& R
 			W.wxx[s] = fsub(fadd(minx, g.dVox), px);
 			W.wxy[s] = fsub(fadd(miny, g.dVox), py);
 			W.wxz[s] = fsub(fadd(minz, g.dVox), pz);
-			W.off[s] = g.dimN[0] * (iz * g.dimN[1] + iy) + ix;
+			W.off[s] = g.oct ? (g.dimN[0] - 1) * (iz * (g.dimN[1] - 1) + iy) + ix
+			                 : g.dimN[0] * (iz * g.dimN[1] + iy) + ix;
 			W.chan[s] = mapped | (outer ? 0x80000000u : 0u);
 			nlook = fabsf(b.w) > 0.001f ? 2u : 1u;
 		}
@@ -211,8 +212,15 @@ __device__ __forceinline__ void eval_pose_rigid(const RigidModel& M, float tx, f
 			const DevIntrpl& g = (ch & 0x80000000u) ? M.grid.outer : M.grid.inner;
 			const uint32_t sx = g.dimN[0], sxy = g.dimN[0] * g.dimN[1];
 			const uint32_t c = is_q ? 0u : (ch & 0x7fffffffu);
-			const float4* base = g.data + (size_t)c * (sxy * g.dimN[2]) + W.off[s];
-			float4 v = octet_lerp(base, sx, sxy, W.wnx[s], W.wny[s], W.wnz[s], W.wxx[s], W.wxy[s], W.wxz[s]);
+			float4 v;
+			if (g.oct) {
+				const size_t nocts = (size_t)(g.dimN[0] - 1) * (g.dimN[1] - 1) * (g.dimN[2] - 1);
+				const float4* base = g.oct + 8 * ((size_t)c * nocts + W.off[s]);
+				v = octet_lerp(base, 2, 4, W.wnx[s], W.wny[s], W.wnz[s], W.wxx[s], W.wxy[s], W.wxz[s]);
+			} else {
+				const float4* base = g.data + (size_t)c * (sxy * g.dimN[2]) + W.off[s];
+				v = octet_lerp(base, sx, sxy, W.wnx[s], W.wny[s], W.wnz[s], W.wxx[s], W.wxy[s], W.wxz[s]);
+			}
 			float sc = g.voxelVol_inv;
 			v.x *= sc; v.y *= sc; v.z *= sc; v.w *= sc;
 			if (is_q) {

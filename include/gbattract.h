@@ -184,7 +184,8 @@ typedef struct {
 	gba_dof6d* out_state;        /* last evaluated DOF per pose */
 	gba_result6d* out_result;    /* last evaluated Result per pose */
 	int32_t* out_nevals;         /* energy evaluations per pose (may be NULL) */
-	uint64_t* reserved;          /* must be NULL */
+	uint64_t* out_done_ns;       /* gba_batch_minimize_6d: per pose, ns from the kernel's
+	                                start to the pose's completion (HOST pointer, may be NULL) */
 } gba_pair_job;
 
 /* Minimizes every pose with the VA13 quasi-Newton method the reference runs
@@ -209,11 +210,14 @@ int gba_batch_minimize_6d(gba_ctx* ctx, const gba_pair_job* jobs, size_t njobs, 
 int gba_batch_energy_6d(gba_ctx* ctx, const gba_pair_job* jobs, size_t njobs, void* stream);
 
 /* The reference's execution model on the same GPU: VA13 per pose on the host
- * and one fused energy launch (plus host<->device copies and a sync) per
- * evaluation round, as RequestHandler + Server + GPU service do.  Host
- * pointers only; results identical in meaning to gba_minimize_6d. */
+ * and, per evaluation round, the active poses cut into work items of
+ * item_size poses (100 is the reference's DEFAULT_ITEM_SIZE,
+ * src/server/Server.h:39; 0 = all active poses in one item), each copied in,
+ * evaluated by one fused launch and copied out, then a sync -- as
+ * RequestHandler + Server + GPU service do.  Host pointers only; results
+ * identical in meaning (and bit for bit) to gba_minimize_6d. */
 int gba_minimize_6d_plain(gba_ctx* ctx, gba_id rec, gba_id lig, gba_id grid, gba_id params,
-		const gba_dof6d* start, size_t n, int max_evals, gba_dof6d* out_state,
+		const gba_dof6d* start, size_t n, int max_evals, size_t item_size, gba_dof6d* out_state,
 		gba_result6d* out_result, int32_t* out_nevals, void* stream);
 
 /* Minimization of flexible poses: VA13 over the DOF vector (ang xyz, pos xyz,
@@ -271,6 +275,25 @@ int gba_pairwise_6d(gba_ctx* ctx, gba_id rec, gba_id lig, gba_id grid,
 		const float* gE, float* g_dofs, double* g_qlig, double* g_qrec, double* g_r0,
 		double* g_eps, void* stream);
 
+/* ---- autotuner ------------------------------------------------------------ */
+
+typedef struct {
+	int energy_threads, energy_blocks_per_sm;   /* scoring kernel launch shape */
+	int minimize_threads, minimize_chunk;       /* persistent minimizer: block size, poses per grab */
+	float energy_ms, minimize_ms;               /* best sample times (-1 when taken from the cache) */
+	int from_cache;                             /* bit 0: energy, bit 1: minimize read from cache */
+} gba_tune_result;
+
+/* Times candidate launch shapes of the scoring kernel (threads per block x
+ * resident blocks per SM) and of the persistent minimizer (threads per block x
+ * poses per queue grab) on `sample` poses of this pair and keeps the fastest
+ * for the context.  With cache_path, results are read from / appended to that
+ * text file (keyed by device, SM count and pair size).  No reference
+ * counterpart: the reference fixes 128-thread blocks (src/service/GPUEnergyService6D.tpp:440-441). */
+int gba_autotune(gba_ctx* ctx, gba_id rec, gba_id lig, gba_id grid, gba_id params,
+		const gba_dof6d* sample, size_t n, int max_evals, const char* cache_path,
+		gba_tune_result* out);
+
 /* ---- grid builder --------------------------------------------------------- */
 
 /* Options of the device grid builder (inner 0.9 A, outer 1.8 A, plateau 10 A,
@@ -291,6 +314,13 @@ typedef struct {
  * (attract::Grid::calculate_std, declared at src/fileIO/grid_orig.h:143). */
 int gba_build_grid(gba_ctx* ctx, gba_id rec, gba_id params, const gba_grid_build_opts* opt,
 		gba_id* out);
+
+/* Adds (enable != 0) or drops a duplicated-octet copy of a grid's inner and
+ * outer potentials: per channel and voxel the 8 interpolation corners in one
+ * aligned 128-byte record, so each lookup reads a single L2 line instead of
+ * four rows of the reference layout.  Costs 8x the potential grids' memory;
+ * results are unchanged.  No reference counterpart (a layout choice). */
+int gba_grid_octets(gba_ctx* ctx, gba_id grid, int enable);
 
 /* Descriptors of a device grid (sizes for gba_download_grid). */
 int gba_grid_info(gba_ctx* ctx, gba_id grid, gba_intrpl_desc* inner, gba_intrpl_desc* outer,

@@ -40,6 +40,9 @@ def test_device_equals_plain_form(min_case, ctx):
     assert np.array_equal(n1, n2)
     assert np.array_equal(s1, s2)
     assert np.array_equal(r1, r2)
+    # the reference's 100-pose work items give the same trajectories
+    s3, r3, n3 = ctx.minimize_6d_plain(*ids, wl.dofs, max_evals=100, item_size=100)
+    assert np.array_equal(s1, s3) and np.array_equal(r1, r3) and np.array_equal(n1, n3)
     assert n1.min() >= 1 and n1.max() <= 101
     # the minimizer lowers the energy of the start poses
     e0 = ctx.energy_6d(*ids, wl.dofs)[:, 0]
@@ -90,6 +93,23 @@ def test_device_pointers_and_zero_budget(min_case, ctx):
     assert np.all(n0 == 1)
     assert np.array_equal(s0, wl.dofs[:10])
     assert np.array_equal(r0, ctx.energy_6d(*ids, wl.dofs[:10]))
+
+
+def test_autotune_and_cache(min_case, ctx, tmp_path):
+    """The tuner picks launch shapes, results stay identical, the cache is reused."""
+    wl, grid = min_case
+    ids = upload(ctx, wl.rec, wl.lig, grid, wl.params)
+    before = ctx.minimize_6d(*ids, wl.dofs[:64], max_evals=40)
+    cache = str(tmp_path / "tune.txt")
+    r1 = ctx.autotune(*ids, wl.dofs, max_evals=20, cache_path=cache)
+    assert r1["energy_threads"] in (128, 256) and r1["minimize_threads"] in (64, 128, 256)
+    assert r1["minimize_chunk"] in (1, 2, 4) and r1["from_cache"] == 0 and r1["energy_ms"] > 0
+    r2 = ctx.autotune(*ids, wl.dofs, max_evals=20, cache_path=cache)
+    assert r2["from_cache"] == 3
+    assert r2["energy_threads"] == r1["energy_threads"] and r2["minimize_chunk"] == r1["minimize_chunk"]
+    after = ctx.minimize_6d(*ids, wl.dofs[:64], max_evals=40)
+    for a, b in zip(before, after):
+        assert np.array_equal(a, b)
 
 
 def test_wall_time_budget_raises_timeout(pkg, ctx, min_case):

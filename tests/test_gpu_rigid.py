@@ -115,6 +115,19 @@ def test_pose_order_does_not_change_results(small_case, ctx):
     assert np.array_equal(plain, ordered)
 
 
+def test_octet_layout_does_not_change_results(small_case, ctx):
+    wl, grid = small_case
+    ids = upload(ctx, wl.rec, wl.lig, grid, wl.params)
+    native = ctx.energy_6d(*ids, wl.dofs)
+    ctx.grid_octets(ids[2], True)
+    octets = ctx.energy_6d(*ids, wl.dofs)
+    s1, r1, n1 = ctx.minimize_6d(*ids, wl.dofs[:32], max_evals=30)
+    ctx.grid_octets(ids[2], False)
+    s2, r2, n2 = ctx.minimize_6d(*ids, wl.dofs[:32], max_evals=30)
+    assert np.array_equal(native, octets)
+    assert np.array_equal(r1, r2) and np.array_equal(s1, s2)
+
+
 def test_errors(small_case, pkg, ctx):
     from gbattract import GbaError
     wl, grid = small_case

@@ -111,16 +111,18 @@ def load() -> C.CDLL:
 
 
 def exported_symbols() -> list:
-    """Names declared in include/gbattract.h that the loaded library exports."""
+    """Names declared in include/*.h that the loaded library exports."""
     lib = load()
     return [n for n in declared_symbols() if hasattr(lib, n)]
 
 
 def declared_symbols() -> list:
-    """Function names declared in include/gbattract.h."""
+    """Function names declared in the C headers under include/."""
     import re
-    hdr = (Path(__file__).resolve().parent.parent / "include" / "gbattract.h").read_text()
-    return sorted(set(re.findall(r"\b(gba_[a-z0-9_]+)\s*\(", hdr)))
+    names = set()
+    for hdr in sorted((Path(__file__).resolve().parent.parent / "include").glob("*.h")):
+        names.update(re.findall(r"\b(gba_[a-z0-9_]+)\s*\(", hdr.read_text()))
+    return sorted(names)
 
 
 def ptr(a) -> int | None:

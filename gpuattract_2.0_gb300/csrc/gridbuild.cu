@@ -191,7 +191,9 @@ void grid_layout(const std::vector<float>& xyz, uint32_t n, const gba_grid_build
 		unsigned N = (unsigned)std::ceil((hi - lo) / s) + 1;
 		inner.dimN[a] = N;
 		inner.posMin[a] = (float)lo;
-		outer.posMin[a] = (float)(lo - o.outer_ext * s);
+		/* ATTRACT stores the float inner origin and derives the outer one from
+		 * it (readGridFromGridFile, src/fileIO/readFile.cpp:322-324) */
+		outer.posMin[a] = (float)((double)inner.posMin[a] - o.outer_ext * s);
 		outer.dimN[a] = (unsigned)std::ceil(((N - 1) * s + 2.0 * o.outer_ext * s) / (2 * s)) + 1;
 		nl.dimN[a] = N;
 		nl.posMin[a] = inner.posMin[a];

@@ -1146,7 +1146,9 @@ int orc_grid_layout(const orc_protein* rec, const orc_grid_opts* opt,
 		unsigned N = (unsigned)std::ceil((hi - lo) / s) + 1;
 		inner->dimN[a] = N;
 		inner->posMin[a] = (float)lo;
-		outer->posMin[a] = (float)(lo - opt->outer_ext * s);
+		/* outer origin from the stored float inner origin, as
+		 * readGridFromGridFile derives it (src/fileIO/readFile.cpp:322-324) */
+		outer->posMin[a] = (float)((double)inner->posMin[a] - opt->outer_ext * s);
 		outer->dimN[a] = (unsigned)std::ceil(((N - 1) * s + 2.0 * opt->outer_ext * s) / (2 * s)) + 1;
 		nl->dimN[a] = N;
 		nl->posMin[a] = inner->posMin[a];

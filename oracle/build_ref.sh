@@ -18,7 +18,7 @@ SRC="$REF_ROOT/src"
 INC=""
 for d in $(find "$SRC" -maxdepth 2 -type d); do INC="$INC -I$d"; done
 FILES="model/Protein.cpp model/IntrplGrid.cpp model/NLGrid.cpp model/GridUnion.cpp
-model/TypeMap.cpp model/Types_6D.cpp model/Types_6D_Modes.cpp
+model/TypeMap.cpp model/Types_6D.cpp model/Types_6D_Modes.cpp model/DOFTransform.cpp
 service/CPUEnergyService6D.cpp service/CPUEnergyService6DModes.cpp
 server/DataManager.cpp server/Thread.cpp server/Server.cpp
 fileIO/readFile.cpp fileIO/grid_orig.cpp"
@@ -39,4 +39,6 @@ g++ $FLAGS $INC -I"$HERE" -c "$HERE/ref_driver.cpp" -o "$OUT/obj/ref_driver.o" &
 pids+=($!)
 for p in "${pids[@]}"; do wait "$p"; done
 g++ -shared -o "$OUT/libattract_ref.so" "${objs[@]}" "$OUT/obj/ref_driver.o" -lpthread
+# tests locate the reference test resources through this marker
+echo "$REF_ROOT" > "$OUT/ref_root.txt"
 echo "build_ref: wrote $OUT/libattract_ref.so"

@@ -88,6 +88,15 @@ def ref_available() -> bool:
     return REF_LIB.exists()
 
 
+def ref_root():
+    """Root of the reference tree oracle/_ref was built from (None if absent)."""
+    marker = HERE / "_ref" / "ref_root.txt"
+    if not marker.exists():
+        return None
+    root = Path(marker.read_text().strip())
+    return root if (root / "src").is_dir() else None
+
+
 def ref_lib():
     global _ref
     if _ref is None:
@@ -348,3 +357,110 @@ def ref_read_params(path: str):
     tab = np.zeros(T * T, m.FFPARAM_DTYPE)
     ref_lib().ref_read_params(str(path).encode(), _p(tab), T, C.byref(ps))
     return tab, ps.value
+
+
+# ---- file formats through the reference's own readers / writers ----------
+
+def _ref_fn(name, restype=C.c_int):
+    f = getattr(ref_lib(), name)
+    f.restype = restype
+    return f
+
+
+def ref_read_dof(path):
+    """(values (S, M, 16), counts (S, M), header dict) via readDOF/readDOFHeader."""
+    f = _ref_fn("ref_read_dof")
+    M = C.c_int32()
+    hdr = np.zeros(4, np.int32)
+    piv = np.zeros((16, 3), np.float32)
+    S = f(str(path).encode(), None, None, C.c_long(0), C.byref(M), _p(hdr), _p(piv))
+    if S < 0:
+        raise RuntimeError(ref_lib().ref_last_error().decode())
+    vals = np.zeros((S, M.value, 16), np.float32)
+    cnt = np.zeros((S, M.value), np.int32)
+    f(str(path).encode(), _p(vals), _p(cnt), C.c_long(S * M.value), C.byref(M), _p(hdr), _p(piv))
+    h = dict(auto_pivot=bool(hdr[0]), centered_receptor=bool(hdr[1]),
+             centered_ligands=bool(hdr[2]), pivots=[tuple(piv[k]) for k in range(hdr[3])])
+    return vals, cnt, h
+
+
+def ref_read_results(path, stride: int = 64):
+    f = _ref_fn("ref_read_results", C.c_long)
+    n = f(str(path).encode(), None, None, C.c_long(0), stride)
+    if n < 0:
+        raise RuntimeError(ref_lib().ref_last_error().decode())
+    out = np.zeros((n, stride), np.float64)
+    cnt = np.zeros(n, np.int32)
+    f(str(path).encode(), _p(out), _p(cnt), C.c_long(n), stride)
+    return [out[i, :cnt[i]].copy() for i in range(n)]
+
+
+def ref_write_results(path, results, n_modes_rec: int = 0, n_modes_lig: int = 0):
+    r = np.ascontiguousarray(results, np.float32)
+    if _ref_fn("ref_write_results")(str(path).encode(), _p(r), C.c_long(r.shape[0]),
+                                    n_modes_rec, n_modes_lig) != 0:
+        raise RuntimeError(ref_lib().ref_last_error().decode())
+
+
+def ref_glob2rec(dofs_rec, dofs_lig, pivot_rec, pivot_lig, centered_rec, centered_lig):
+    r = np.array(dofs_rec, np.float32, copy=True, order="C")
+    lg = np.array(dofs_lig, np.float32, copy=True, order="C")
+    pr = np.ascontiguousarray(pivot_rec, np.float32)
+    pl = np.ascontiguousarray(pivot_lig, np.float32)
+    _ref_fn("ref_glob2rec")(_p(r), _p(lg), C.c_long(r.shape[0]), _p(pr), _p(pl),
+                            int(centered_rec), int(centered_lig))
+    return r, lg
+
+
+def ref_auto_pivot(xyz):
+    x = np.ascontiguousarray(xyz, np.float32)
+    out = np.zeros(3, np.float32)
+    _ref_fn("ref_auto_pivot")(_p(x), C.c_long(x.shape[1]), _p(out))
+    return out
+
+
+def ref_map_types(alphabet_path, types):
+    t = np.ascontiguousarray(types, np.uint32)
+    ot, om = np.zeros_like(t), np.zeros_like(t)
+    alpha = np.zeros(128, np.uint32)
+    n = _ref_fn("ref_map_types")(str(alphabet_path).encode(), _p(t), C.c_long(t.size), _p(ot),
+                                 _p(om), _p(alpha), 128)
+    if n < 0:
+        raise RuntimeError(ref_lib().ref_last_error().decode())
+    return ot, om, alpha[:n].copy()
+
+
+def ref_read_grid_file(path, info):
+    """readGridFromGridFile<float>: (inner desc, inner, outer desc, outer, nl desc,
+    nl_grid, nl_list, dPlateau2); buffers sized from the .grid header `info`."""
+    from gbattract import _lib
+    C_ = 1 + sum(1 for a in info.alphabet if a)
+    di = [int(v) for v in info.inner_dim]
+    do = [int(v) for v in info.outer_dim]
+    inner = np.zeros((C_, di[2], di[1], di[0], 4), np.float32)
+    outer = np.zeros((C_, do[2], do[1], do[0], 4), np.float32)
+    nlg = np.zeros((di[2], di[1], di[0], 2), np.uint32)
+    nll = np.zeros(max(1, info.nr_neighbours), np.uint32)
+    ci, co, cn = _lib.IntrplDescC(), _lib.IntrplDescC(), _lib.NLDescC()
+    dp2 = C.c_float()
+    rc = _ref_fn("ref_read_grid_file")(
+        str(path).encode(), C.byref(ci), _p(inner), C.c_long(inner.size), C.byref(co), _p(outer),
+        C.c_long(outer.size), C.byref(cn), _p(nlg), C.c_long(nlg.size // 2), _p(nll),
+        C.c_long(info.nr_neighbours), C.byref(dp2))
+    if rc != 0:
+        raise RuntimeError(ref_lib().ref_last_error().decode())
+    return ci, inner, co, outer, cn, nlg, nll[:info.nr_neighbours], dp2.value
+
+
+def ref_write_grid_file(path, grid, alphabet, info, rec_xyz=None):
+    """attract::Grid::write_std of a GridSet (the reference's own writer)."""
+    from gbattract import _lib, formats
+    a = np.ascontiguousarray(alphabet, np.uint32)
+    ci, co, cn = formats._intrpl_c(grid.inner), formats._intrpl_c(grid.outer), formats._nl_c(grid.nl)
+    x = None if rec_xyz is None else np.ascontiguousarray(rec_xyz, np.float32)
+    rc = _ref_fn("ref_write_grid_file")(
+        str(path).encode(), C.byref(info), _p(a), C.byref(ci), _p(np.ascontiguousarray(grid.inner_data)),
+        C.byref(co), _p(np.ascontiguousarray(grid.outer_data)), C.byref(cn),
+        _p(np.ascontiguousarray(grid.nl_grid)), _p(np.ascontiguousarray(grid.nl_list)), _p(x))
+    if rc != 0:
+        raise RuntimeError(ref_lib().ref_last_error().decode())

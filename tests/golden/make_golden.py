@@ -30,7 +30,7 @@ import __graft_entry__  # noqa: E402
 pkg = __graft_entry__.load_package()
 from oracle import pyoracle as po  # noqa: E402
 
-REF_TEST = Path("/root/reference/test/resources")
+REF_TEST = po.ref_root() / "test" / "resources"
 OUT = Path(__file__).resolve().parent
 
 

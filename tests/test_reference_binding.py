@@ -8,7 +8,17 @@ from pathlib import Path
 import pytest
 
 ROOT = Path(__file__).resolve().parent.parent
-REF = Path("/root/reference/src")
+
+
+def _ref_src():
+    import sys
+    sys.path.insert(0, str(ROOT))
+    from oracle import pyoracle
+    r = pyoracle.ref_root()
+    return None if r is None else r / "src"
+
+
+REF = _ref_src()
 
 SNIPPET = r'''
 #include "GB300EnergyService6D.h"
@@ -22,7 +32,7 @@ void use(std::shared_ptr<as::DataManager> dm) {
 '''
 
 
-@pytest.mark.skipif(not REF.is_dir(), reason="reference sources not present on this host")
+@pytest.mark.skipif(REF is None, reason="reference sources not present on this host")
 def test_binding_compiles_against_reference(tmp_path):
     src = tmp_path / "bind.cpp"
     src.write_text(SNIPPET)

@@ -354,6 +354,8 @@ def main():
     ap.add_argument("--suite", default="default", choices=["default", "full"],
                     help="full: also configs 2 (modes), 3 (adjoint), 4 (batched uneven pairs)")
     ap.add_argument("--modes-poses", type=int, default=50000)
+    ap.add_argument("--variant", default=None,
+                    help="fix the layout variant, e.g. order=1,octets=1 (default: time all four)")
     ap.add_argument("--batch-scale", type=float, default=0.05,
                     help="fraction of config 4's pose counts used by --suite full")
     args = ap.parse_args()
@@ -407,17 +409,20 @@ def main():
     # layout / visiting-order variants (short runs); the fastest is timed below
     variants = {}
     ref_out = None
-    for order in (False, True):
-        for octets in (False, True):
-            ctx.set_pose_order(order)
-            ctx.grid_octets(grid, octets)
-            step()
-            torch.cuda.synchronize()
-            if ref_out is None:
-                ref_out = out.clone()
-            elif not torch.equal(out, ref_out):
-                raise RuntimeError("variant changed the results")
-            variants[f"order={int(order)},octets={int(octets)}"] = timed_ms()
+    combos = [(o, c) for o in (False, True) for c in (False, True)]
+    if args.variant:
+        kv = dict(x.split("=") for x in args.variant.split(","))
+        combos = [(kv.get("order", "1") == "1", kv.get("octets", "1") == "1")]
+    for order, octets in combos:
+        ctx.set_pose_order(order)
+        ctx.grid_octets(grid, octets)
+        step()
+        torch.cuda.synchronize()
+        if ref_out is None:
+            ref_out = out.clone()
+        elif not torch.equal(out, ref_out):
+            raise RuntimeError("variant changed the results")
+        variants[f"order={int(order)},octets={int(octets)}"] = timed_ms()
     best = min(variants, key=variants.get)
     ctx.set_pose_order(best.startswith("order=1"))
     ctx.grid_octets(grid, best.endswith("octets=1"))
@@ -427,6 +432,10 @@ def main():
         step()
     torch.cuda.synchronize()
     times = []
+    # CUDA events around the energy kernel itself, recorded by the library on
+    # the launching stream (the step also runs the visiting-order pass)
+    ctx.kernel_timing(True)
+    ctx.kernel_time(reset=True)
     with ClockSampler(local) as clk:
         if world > 1:
             torch.distributed.barrier()
@@ -443,6 +452,8 @@ def main():
         wall = time.perf_counter() - w0
         if world > 1:
             torch.distributed.barrier()
+    kernel_ms, kernel_launches = ctx.kernel_time(reset=True)
+    ctx.kernel_timing(False)
     ks = [a.elapsed_time(b) / 1000.0 for a, b in times]
     ktot = sum(ks)
     if world > 1:
@@ -451,7 +462,8 @@ def main():
         ktot = float(t.item())
     value = world * n * args.steps / ktot
     kavg = ktot / args.steps
-    achieved = bytes_launch / kavg / 1e9
+    kernel_avg_s = kernel_ms / 1000.0 / max(1, kernel_launches)
+    achieved = bytes_launch / kernel_avg_s / 1e9
     peak, peak_kind = measured_peaks()
 
     # end to end through the C ABI with pinned host buffers
@@ -501,7 +513,8 @@ def main():
                     "d2h_bytes_per_step": int(28 * n)},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": None, "peak_source": peak_kind,
-                         "bytes_per_launch": bytes_launch},
+                         "bytes_per_launch": bytes_launch, "kernel_ms_avg": 1000.0 * kernel_avg_s,
+                         "kernel_launches_timed": kernel_launches},
             "cpu_baseline": cpu, "clocks": clk.summary(),
             # per step: the fused energy kernel (+ the Morton-key kernel when the visiting
             # order is on; the CUB radix-sort passes it feeds are library kernels)

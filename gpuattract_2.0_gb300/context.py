@@ -294,6 +294,17 @@ class GbaContext:
         """Visit large batches in Morton order of the pose translation (default on)."""
         self._check(self.lib.gba_set_pose_order(self.h, int(bool(enable))))
 
+    def kernel_timing(self, enable: bool):
+        """Record CUDA events around every fused rigid energy kernel launch."""
+        self._check(self.lib.gba_kernel_timing(self.h, int(bool(enable))))
+
+    def kernel_time(self, reset: bool = True) -> tuple[float, int]:
+        """(summed kernel ms, launches) recorded since the last reset."""
+        import ctypes as C
+        ms, n = C.c_double(), C.c_uint64()
+        self._check(self.lib.gba_kernel_time(self.h, C.byref(ms), C.byref(n), int(bool(reset))))
+        return ms.value, n.value
+
     def census_6d(self, rec: int, lig: int, grid: int, params: int, dofs):
         """Per-pose counts {n_grid, n_grid_charged, n_nl, n_nl_entries} (n, 4) uint32."""
         dofs = _check_poses(dofs, DOF_WIDTH, "census_6d")

@@ -219,7 +219,7 @@ extern "C" int gba_pairwise_6d(gba_ctx* ctx, gba_id rec, gba_id lig, gba_id grid
 		ctx->bind();
 		PairwiseLaunch L{};
 		{
-			std::lock_guard<std::mutex> g(ctx->mu);
+			Lock g(ctx->mu);
 			auto* R = static_cast<ProteinItem*>(ctx->find(rec, ItemKind::Protein));
 			auto* Lg = static_cast<ProteinItem*>(ctx->find(lig, ItemKind::Protein));
 			auto* G = static_cast<GridItem*>(ctx->find(grid, ItemKind::Grid));

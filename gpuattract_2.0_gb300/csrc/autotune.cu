@@ -107,7 +107,7 @@ extern "C" int gba_autotune(gba_ctx* ctx, gba_id rec, gba_id lig, gba_id grid, g
 		const bool have_m = cache_lookup(cache_path, mk, tm);
 		float best_e = -1.f, best_m = -1.f;
 		if (!have_e || !have_m) {
-			std::lock_guard<std::mutex> lk(ctx->stage_mu);
+			Lock lk(ctx->stage_mu);
 			cudaStream_t s = 0;
 			gba_dof6d* d = (gba_dof6d*)ctx->staging(0, n * sizeof(gba_dof6d));
 			check_cuda(cudaMemcpy(d, sample, n * sizeof(gba_dof6d), cudaMemcpyDefault), "sample");

@@ -2,21 +2,24 @@
  * energy_modes.cu -- fused normal-mode (flexible) docking energy + gradients.
  *
  * CPU semantics followed: CPUEnergyService6DModes::createItemProcessor
- * (src/service/CPUEnergyService6DModes.tpp:121-327).  One warp owns one pose:
+ * (src/service/CPUEnergyService6DModes.tpp:121-327).  One warp owns one pose
+ * and works in rounds of 64 beads staged in shared memory, like the rigid
+ * kernel (rigid_pose.cuh), in two passes:
  *   receptor pass  deform by the receptor amplitudes (rotate_translate_deform,
  *                  src/model/transform_modes.h:54-93), move into the ligand
  *                  frame with the "inverted" DOF (invertDOF, :27-41: angles
  *                  negated, t' = R^T (-t)), interpolate in the LIGAND grid,
  *                  rotate the force back by R (rotate_forces, :146-166) and
- *                  project it on the receptor modes (reduceModeForce, no
+ *                  project it on the receptor modes (reduceModeForce without
  *                  rotation, src/model/reduction_modes.h:68-90);
  *   ligand pass    deform + transform the ligand, interpolate in the receptor
  *                  grid, add the NL pair term against the DEFORMED receptor
  *                  (neighborlist_modes.h:21-206) whose reaction forces are
- *                  projected on the receptor modes pair by pair; reduce force,
- *                  energy, torque (undeformed ligand coordinates, reduceTorque)
- *                  and the ligand mode projection of R^T f (reduceModeForce
- *                  with rotation, reduction_modes.h:29-57);
+ *                  projected on the receptor modes pair by pair; energy, force,
+ *                  torque (undeformed ligand coordinates, reduceTorque) and the
+ *                  ligand mode projection of R^T f (reduceModeForce with
+ *                  rotation, reduction_modes.h:29-57) are summed per lookup
+ *                  and per pair (all linear in the bead forces);
  *   epilogue       warp sums, correctModeForce (delta += 4 k delta^4,
  *                  reduction_modes.h:101-115), ForceLim, TorqueMat.
  * The energy holds only the ligand-side terms, as in the reference.
@@ -26,214 +29,244 @@
  * deformed receptor and mode buffers (src/model/neighborlist_modes.cu:81-83,
  * src/model/transform_modes.cu:154, src/model/reduction_modes.cu:68-69).
  */
-#include "energy_dev.cuh"
+#include "rigid_pose.cuh"
 #include "va13.cuh"
 
 namespace gba {
 
 namespace {
 
-/* Deformed receptor bead j (receptor frame): x_j + sum_m a_m v_jm, unfused in
- * mode order as rotate_translate_deform does. */
-struct DeformedRecPos {
-	const float4* __restrict__ xyzq;
-	const float* __restrict__ modes;   /* [i][m][axis], stride ms floats */
-	uint32_t M, ms;
-	const float* amp;                  /* M amplitudes (registers of the caller) */
-	__device__ __forceinline__ void operator()(uint32_t j, float& x, float& y, float& z, float& q) const {
-		const float4 r = __ldg(&xyzq[j]);
-		x = r.x; y = r.y; z = r.z; q = r.w;
-		const float* v = modes + (size_t)j * ms;
+/* x + sum_m a_m v_m, unfused in mode order (rotate_translate_deform). */
+__device__ __forceinline__ void deform(const float* __restrict__ v, uint32_t M, const float* amp,
+		float& x, float& y, float& z) {
 #pragma unroll
-		for (int m = 0; m < GBA_MODES_MAX; ++m) {
-			if (m < (int)M) {
-				x = fadd(x, fmul(amp[m], __ldg(v + 3 * m)));
-				y = fadd(y, fmul(amp[m], __ldg(v + 3 * m + 1)));
-				z = fadd(z, fmul(amp[m], __ldg(v + 3 * m + 2)));
-			}
+	for (int m = 0; m < GBA_MODES_MAX; ++m)
+		if (m < (int)M) {
+			x = fadd(x, fmul(amp[m], __ldg(v + 3 * m)));
+			y = fadd(y, fmul(amp[m], __ldg(v + 3 * m + 1)));
+			z = fadd(z, fmul(amp[m], __ldg(v + 3 * m + 2)));
 		}
-	}
-};
+}
 
-/* Projects each NL pair force on the receptor modes: the reaction force on
- * receptor bead j is -f, and the receptor mode gradient is -sum (force . v). */
-struct RecModeHook {
-	const float* __restrict__ modes;
-	uint32_t M, ms;
-	float* acc;                         /* M accumulators */
-	__device__ __forceinline__ void operator()(uint32_t j, float fx, float fy, float fz) const {
-		const float* v = modes + (size_t)j * ms;
+/* acc[m] += sign * (f . v_m) */
+__device__ __forceinline__ void project(const float* __restrict__ v, uint32_t M, float fx, float fy,
+		float fz, float sign, float* acc) {
 #pragma unroll
-		for (int m = 0; m < GBA_MODES_MAX; ++m)
-			if (m < (int)M)
-				acc[m] += fx * __ldg(v + 3 * m) + fy * __ldg(v + 3 * m + 1) + fz * __ldg(v + 3 * m + 2);
-	}
-};
+	for (int m = 0; m < GBA_MODES_MAX; ++m)
+		if (m < (int)M)
+			acc[m] += sign * (fx * __ldg(v + 3 * m) + fy * __ldg(v + 3 * m + 1) + fz * __ldg(v + 3 * m + 2));
+}
 
 }  // namespace
 
 /* One pose of the modes energy.  Lane k (k < 26) brings the k-th float of the
  * DOF_6D_Modes record; returns on lane k (k < 27) the k-th float of the
  * Result_6D_Modes record.  Only the model fields of L are read. */
-__device__ __forceinline__ float eval_pose_modes(const ModesLaunch& L, const float dv, const int lane) {
+__device__ __forceinline__ float eval_pose_modes(const ModesLaunch& L, const float dv, const int lane,
+		WarpStage& W) {
 	const uint32_t Mr = L.rec.n_modes, Ml = L.lig.n_modes;
-	{
-		const float tx = __shfl_sync(GBA_FULL_MASK, dv, 0);
-		const float ty = __shfl_sync(GBA_FULL_MASK, dv, 1);
-		const float tz = __shfl_sync(GBA_FULL_MASK, dv, 2);
-		const float a0 = __shfl_sync(GBA_FULL_MASK, dv, 3);
-		const float a1 = __shfl_sync(GBA_FULL_MASK, dv, 4);
-		const float a2 = __shfl_sync(GBA_FULL_MASK, dv, 5);
-		float ampR[GBA_MODES_MAX], ampL[GBA_MODES_MAX];
+	const float tx = __shfl_sync(GBA_FULL_MASK, dv, 0);
+	const float ty = __shfl_sync(GBA_FULL_MASK, dv, 1);
+	const float tz = __shfl_sync(GBA_FULL_MASK, dv, 2);
+	const float a0 = __shfl_sync(GBA_FULL_MASK, dv, 3);
+	const float a1 = __shfl_sync(GBA_FULL_MASK, dv, 4);
+	const float a2 = __shfl_sync(GBA_FULL_MASK, dv, 5);
+	float ampR[GBA_MODES_MAX], ampL[GBA_MODES_MAX];
 #pragma unroll
-		for (int m = 0; m < GBA_MODES_MAX; ++m) {
-			ampR[m] = __shfl_sync(GBA_FULL_MASK, dv, 6 + m);
-			ampL[m] = __shfl_sync(GBA_FULL_MASK, dv, 16 + m);
-		}
-		const PoseRot R = pose_rotation(a0, a1, a2, lane);
-		/* R(-ang): same sin/cos with the sines negated (exact sign flips) */
-		PoseRot Ri = R;
-		{
-			const float cphi = R.cphi, sphi = -R.sphi, cssi = R.cssi, sssi = -R.sssi;
-			const float crot = R.crot, srot = -R.srot;
-			const float cSSI_cPHI = fmul(cssi, cphi), cSSI_sPHI = fmul(cssi, sphi);
-			const float sSSI_cPHI = fmul(sssi, cphi), sSSI_sPHI = fmul(sssi, sphi);
-			Ri.m[0] = fadd(fmul(crot, cSSI_cPHI), fmul(srot, sphi));
-			Ri.m[1] = fsub(fmul(srot, cSSI_cPHI), fmul(crot, sphi));
-			Ri.m[2] = sSSI_cPHI;
-			Ri.m[3] = fsub(fmul(crot, cSSI_sPHI), fmul(srot, cphi));
-			Ri.m[4] = fadd(fmul(srot, cSSI_sPHI), fmul(crot, cphi));
-			Ri.m[5] = sSSI_sPHI;
-			Ri.m[6] = fmul(-crot, sssi);
-			Ri.m[7] = fmul(-srot, sssi);
-			Ri.m[8] = cssi;
-		}
-		/* t' = R^T * (-t), RotMat * Vec3 on the transposed matrix */
-		const float ipx = fadd(fadd(fmul(R.m[0], -tx), fmul(R.m[3], -ty)), fmul(R.m[6], -tz));
-		const float ipy = fadd(fadd(fmul(R.m[1], -tx), fmul(R.m[4], -ty)), fmul(R.m[7], -tz));
-		const float ipz = fadd(fadd(fmul(R.m[2], -tx), fmul(R.m[5], -ty)), fmul(R.m[8], -tz));
-
-		float gR[GBA_MODES_MAX], gL[GBA_MODES_MAX];
-#pragma unroll
-		for (int m = 0; m < GBA_MODES_MAX; ++m) { gR[m] = 0.f; gL[m] = 0.f; }
-
-		/* ---- receptor beads in the ligand grid ---- */
-		for (uint32_t j = lane; j < L.rec.n; j += 32) {
-			const uint32_t mapped = __ldg(&L.rec.tm[j]) >> 16;
-			if (mapped == 0) continue;
-			float x, y, z, q;
-			DeformedRecPos{L.rec.xyzq, L.rec_modes, Mr, L.rec_ms, ampR}(j, x, y, z, q);
-			float px, py, pz;
-			rot_apply(Ri.m, x, y, z, px, py, pz);
-			px = fadd(px, ipx); py = fadd(py, ipy); pz = fadd(pz, ipz);
-			float4 pot;
-			bool charged;
-			if (!bead_grid_term(L.grid_lig, px, py, pz, mapped, q, pot, charged)) continue;
-			const float fx = R.m[0] * pot.x + R.m[1] * pot.y + R.m[2] * pot.z;
-			const float fy = R.m[3] * pot.x + R.m[4] * pot.y + R.m[5] * pot.z;
-			const float fz = R.m[6] * pot.x + R.m[7] * pot.y + R.m[8] * pot.z;
-			const float* v = L.rec_modes + (size_t)j * L.rec_ms;
-#pragma unroll
-			for (int m = 0; m < GBA_MODES_MAX; ++m)
-				if (m < (int)Mr)
-					gR[m] -= fx * __ldg(v + 3 * m) + fy * __ldg(v + 3 * m + 1) + fz * __ldg(v + 3 * m + 2);
-		}
-
-		/* ---- ligand beads in the receptor grid + NL against the deformed receptor ---- */
-		float sE = 0.f, sFx = 0.f, sFy = 0.f, sFz = 0.f;
-		float T[9] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-		const DeformedRecPos recpos{L.rec.xyzq, L.rec_modes, Mr, L.rec_ms, ampR};
-		const RecModeHook hook{L.rec_modes, Mr, L.rec_ms, gR};
-		for (uint32_t i = lane; i < L.lig.n; i += 32) {
-			const float4 b = __ldg(&L.lig.xyzq[i]);
-			const uint32_t tm = __ldg(&L.lig.tm[i]);
-			const uint32_t type = tm & 0xffffu, mapped = tm >> 16;
-			const float* vl = L.lig_modes + (size_t)i * L.lig_ms;
-			float x = b.x, y = b.y, z = b.z;
-#pragma unroll
-			for (int m = 0; m < GBA_MODES_MAX; ++m)
-				if (m < (int)Ml) {
-					x = fadd(x, fmul(ampL[m], __ldg(vl + 3 * m)));
-					y = fadd(y, fmul(ampL[m], __ldg(vl + 3 * m + 1)));
-					z = fadd(z, fmul(ampL[m], __ldg(vl + 3 * m + 2)));
-				}
-			float px, py, pz;
-			rot_apply(R.m, x, y, z, px, py, pz);
-			px = fadd(px, tx); py = fadd(py, ty); pz = fadd(pz, tz);
-			float fx = 0.f, fy = 0.f, fz = 0.f, e = 0.f;
-			float4 pot;
-			bool charged;
-			if (bead_grid_term(L.grid_rec, px, py, pz, mapped, b.w, pot, charged)) {
-				fx = pot.x; fy = pot.y; fz = pot.z; e = pot.w;
-			}
-			if (type != 0) {
-				uint32_t npairs = 0;
-				bead_nl_term(L.grid_rec.nl, L.par, L.rec.tm, recpos, px, py, pz, type, b.w,
-						fx, fy, fz, e, npairs, hook);
-			}
-			sE += e; sFx += fx; sFy += fy; sFz += fz;
-			T[0] += b.x * fx; T[1] += b.y * fx; T[2] += b.z * fx;
-			T[3] += b.x * fy; T[4] += b.y * fy; T[5] += b.z * fy;
-			T[6] += b.x * fz; T[7] += b.y * fz; T[8] += b.z * fz;
-			/* R^T f, projected on the ligand modes */
-			const float rx = R.m[0] * fx + R.m[3] * fy + R.m[6] * fz;
-			const float ry = R.m[1] * fx + R.m[4] * fy + R.m[7] * fz;
-			const float rz = R.m[2] * fx + R.m[5] * fy + R.m[8] * fz;
-#pragma unroll
-			for (int m = 0; m < GBA_MODES_MAX; ++m)
-				if (m < (int)Ml)
-					gL[m] -= rx * __ldg(vl + 3 * m) + ry * __ldg(vl + 3 * m + 1) + rz * __ldg(vl + 3 * m + 2);
-		}
-
-		sE = warp_sum(sE); sFx = warp_sum(sFx); sFy = warp_sum(sFy); sFz = warp_sum(sFz);
-#pragma unroll
-		for (int k = 0; k < 9; ++k) T[k] = warp_sum(T[k]);
-#pragma unroll
-		for (int m = 0; m < GBA_MODES_MAX; ++m) {
-			if (m < (int)Mr) gR[m] = warp_sum(gR[m]);
-			if (m < (int)Ml) gL[m] = warp_sum(gL[m]);
-		}
-		force_lim(sFx, sFy, sFz);
-		float ang[3];
-		torque_reduce(R, T, ang);
-		/* correctModeForce: delta += (float)(4 k * delta^4) */
-#pragma unroll
-		for (int m = 0; m < GBA_MODES_MAX; ++m) {
-			if (m < (int)Mr) {
-				const double dl = gR[m];
-				gR[m] = gR[m] + (float)((double)(4.0f * L.rec.mode_force[m]) * (dl * dl) * (dl * dl));
-			}
-			if (m < (int)Ml) {
-				const double dl = gL[m];
-				gL[m] = gL[m] + (float)((double)(4.0f * L.lig.mode_force[m]) * (dl * dl) * (dl * dl));
-			}
-		}
-		/* Result_6D_Modes: E, pos xyz, ang xyz, modesRec[10], modesLig[10] */
-		float v = 0.f;
-		if (lane == 0) v = sE;
-		else if (lane == 1) v = sFx;
-		else if (lane == 2) v = sFy;
-		else if (lane == 3) v = sFz;
-		else if (lane == 4) v = ang[0];
-		else if (lane == 5) v = ang[1];
-		else if (lane == 6) v = ang[2];
-#pragma unroll
-		for (int m = 0; m < GBA_MODES_MAX; ++m) {
-			if (lane == 7 + m) v = m < (int)Mr ? gR[m] : 0.f;
-			if (lane == 17 + m) v = m < (int)Ml ? gL[m] : 0.f;
-		}
-		return v;
+	for (int m = 0; m < GBA_MODES_MAX; ++m) {
+		ampR[m] = __shfl_sync(GBA_FULL_MASK, dv, 6 + m);
+		ampL[m] = __shfl_sync(GBA_FULL_MASK, dv, 16 + m);
 	}
+	const PoseRot R = pose_rotation(a0, a1, a2, lane);
+	/* R(-ang): same sin/cos with the sines negated (exact sign flips) */
+	float Ri[9];
+	{
+		const float cphi = R.cphi, sphi = -R.sphi, cssi = R.cssi, sssi = -R.sssi;
+		const float crot = R.crot, srot = -R.srot;
+		const float cSSI_cPHI = fmul(cssi, cphi), cSSI_sPHI = fmul(cssi, sphi);
+		const float sSSI_cPHI = fmul(sssi, cphi), sSSI_sPHI = fmul(sssi, sphi);
+		Ri[0] = fadd(fmul(crot, cSSI_cPHI), fmul(srot, sphi));
+		Ri[1] = fsub(fmul(srot, cSSI_cPHI), fmul(crot, sphi));
+		Ri[2] = sSSI_cPHI;
+		Ri[3] = fsub(fmul(crot, cSSI_sPHI), fmul(srot, cphi));
+		Ri[4] = fadd(fmul(srot, cSSI_sPHI), fmul(crot, cphi));
+		Ri[5] = sSSI_sPHI;
+		Ri[6] = fmul(-crot, sssi);
+		Ri[7] = fmul(-srot, sssi);
+		Ri[8] = cssi;
+	}
+	/* t' = R^T * (-t), RotMat * Vec3 on the transposed matrix */
+	const float ipx = fadd(fadd(fmul(R.m[0], -tx), fmul(R.m[3], -ty)), fmul(R.m[6], -tz));
+	const float ipy = fadd(fadd(fmul(R.m[1], -tx), fmul(R.m[4], -ty)), fmul(R.m[7], -tz));
+	const float ipz = fadd(fadd(fmul(R.m[2], -tx), fmul(R.m[5], -ty)), fmul(R.m[8], -tz));
+
+	float gR[GBA_MODES_MAX], gL[GBA_MODES_MAX];
+#pragma unroll
+	for (int m = 0; m < GBA_MODES_MAX; ++m) { gR[m] = 0.f; gL[m] = 0.f; }
+
+	/* ---- receptor beads in the ligand grid ---- */
+	for (uint32_t j0 = 0; j0 < L.rec.n; j0 += kBeadsPerRound) {
+		uint32_t nlk[2];
+#pragma unroll
+		for (int h = 0; h < 2; ++h) {
+			const int s = lane + 32 * h;
+			const uint32_t j = j0 + s;
+			nlk[h] = 0;
+			if (j < L.rec.n) {
+				const float4 r = __ldg(&L.rec.xyzq[j]);
+				const uint32_t mapped = __ldg(&L.rec.tm[j]) >> 16;
+				float x = r.x, y = r.y, z = r.z;
+				deform(L.rec_modes + (size_t)j * L.rec_ms, Mr, ampR, x, y, z);
+				float px, py, pz;
+				rot_apply(Ri, x, y, z, px, py, pz);
+				px = fadd(px, ipx); py = fadd(py, ipy); pz = fadd(pz, ipz);
+				W.q[s] = r.w;
+				W.type[s] = j;      /* receptor bead index of the slot */
+				nlk[h] = stage_grid(L.grid_lig, px, py, pz, mapped, r.w, s, W);
+			}
+		}
+		const uint32_t incl = warp_incl_scan(nlk[0] + nlk[1], lane);
+		const uint32_t n_look = __shfl_sync(GBA_FULL_MASK, incl, 31);
+		uint32_t k = incl - nlk[0] - nlk[1];
+		enqueue_lookups(W, k, lane, nlk[0]);
+		enqueue_lookups(W, k, lane + 32, nlk[1]);
+		__syncwarp();
+		for (uint32_t q = lane; q < n_look; q += 32) {
+			const uint32_t e = W.look[q];
+			const float4 v = grid_lookup(L.grid_lig, W, e);
+			/* back into the receptor frame, then -(force . mode) */
+			const float fx = R.m[0] * v.x + R.m[1] * v.y + R.m[2] * v.z;
+			const float fy = R.m[3] * v.x + R.m[4] * v.y + R.m[5] * v.z;
+			const float fz = R.m[6] * v.x + R.m[7] * v.y + R.m[8] * v.z;
+			project(L.rec_modes + (size_t)W.type[e >> 1] * L.rec_ms, Mr, fx, fy, fz, -1.f, gR);
+		}
+		__syncwarp();
+	}
+
+	/* ---- ligand beads in the receptor grid + NL against the deformed receptor ---- */
+	PoseSums S;
+	for (uint32_t i0 = 0; i0 < L.lig.n; i0 += kBeadsPerRound) {
+		uint32_t nlk[2], nln[2];
+#pragma unroll
+		for (int h = 0; h < 2; ++h) {
+			const int s = lane + 32 * h;
+			const uint32_t i = i0 + s;
+			nlk[h] = 0;
+			nln[h] = 0;
+			if (i < L.lig.n) {
+				const float4 b = __ldg(&L.lig.xyzq[i]);
+				const uint32_t tm = __ldg(&L.lig.tm[i]);
+				const uint32_t type = tm & 0xffffu, mapped = tm >> 16;
+				float x = b.x, y = b.y, z = b.z;
+				deform(L.lig_modes + (size_t)i * L.lig_ms, Ml, ampL, x, y, z);
+				float px, py, pz;
+				rot_apply(R.m, x, y, z, px, py, pz);
+				px = fadd(px, tx); py = fadd(py, ty); pz = fadd(pz, tz);
+				W.ux[s] = b.x; W.uy[s] = b.y; W.uz[s] = b.z;
+				W.px[s] = px; W.py[s] = py; W.pz[s] = pz;
+				W.q[s] = b.w;
+				W.type[s] = type;
+				nlk[h] = stage_grid(L.grid_rec, px, py, pz, mapped, b.w, s, W);
+				bool in_nl;
+				if (type != 0) nln[h] = stage_nl(L.grid_rec.nl, px, py, pz, s, W, in_nl);
+			}
+		}
+		const uint32_t lk_incl = warp_incl_scan(nlk[0] + nlk[1], lane);
+		const uint32_t n_look = __shfl_sync(GBA_FULL_MASK, lk_incl, 31);
+		uint32_t k = lk_incl - nlk[0] - nlk[1];
+		enqueue_lookups(W, k, lane, nlk[0]);
+		enqueue_lookups(W, k, lane + 32, nlk[1]);
+		const uint32_t a_incl = warp_incl_scan(nln[0], lane);
+		const uint32_t a_tot = __shfl_sync(GBA_FULL_MASK, a_incl, 31);
+		const uint32_t b_incl = warp_incl_scan(nln[1], lane);
+		W.nl_pre[lane] = a_incl - nln[0];
+		W.nl_pre[lane + 32] = a_tot + b_incl - nln[1];
+		const uint32_t n_pair = a_tot + __shfl_sync(GBA_FULL_MASK, b_incl, 31);
+		if (lane == 0) W.nl_pre[kBeadsPerRound] = n_pair;
+		__syncwarp();
+		for (uint32_t q = lane; q < n_look; q += 32) {
+			const uint32_t e = W.look[q];
+			const uint32_t s = e >> 1;
+			const float4 v = grid_lookup(L.grid_rec, W, e);
+			S.add(v.w, v.x, v.y, v.z, W.ux[s], W.uy[s], W.uz[s]);
+			const float rx = R.m[0] * v.x + R.m[3] * v.y + R.m[6] * v.z;
+			const float ry = R.m[1] * v.x + R.m[4] * v.y + R.m[7] * v.z;
+			const float rz = R.m[2] * v.x + R.m[5] * v.y + R.m[8] * v.z;
+			project(L.lig_modes + (size_t)(i0 + s) * L.lig_ms, Ml, rx, ry, rz, -1.f, gL);
+		}
+		for (uint32_t q = lane; q < n_pair; q += 32) {
+			const uint32_t s = pair_owner(W, q);
+			const uint32_t j = __ldg(&L.grid_rec.nl.list[W.nl_idx[s] + (q - W.nl_pre[s])]);
+			const float4 r = __ldg(&L.rec.xyzq[j]);
+			float rx = r.x, ry = r.y, rz = r.z;
+			const float* vr = L.rec_modes + (size_t)j * L.rec_ms;
+			deform(vr, Mr, ampR, rx, ry, rz);
+			const uint32_t trec = __ldg(&L.rec.tm[j]) & 0xffffu;
+			float fx, fy, fz, e;
+			if (!nl_pair(L.grid_rec.nl, L.par, W.type[s], W.q[s], W.px[s], W.py[s], W.pz[s], rx, ry, rz,
+					r.w, trec, fx, fy, fz, e))
+				continue;
+			S.add(e, fx, fy, fz, W.ux[s], W.uy[s], W.uz[s]);
+			/* reaction on receptor bead j is -f: its mode gradient gets -(-f . v) */
+			project(vr, Mr, fx, fy, fz, 1.f, gR);
+			const float lx = R.m[0] * fx + R.m[3] * fy + R.m[6] * fz;
+			const float ly = R.m[1] * fx + R.m[4] * fy + R.m[7] * fz;
+			const float lz = R.m[2] * fx + R.m[5] * fy + R.m[8] * fz;
+			project(L.lig_modes + (size_t)(i0 + s) * L.lig_ms, Ml, lx, ly, lz, -1.f, gL);
+		}
+		__syncwarp();
+	}
+
+	float sE = warp_sum(S.E), sFx = warp_sum(S.Fx), sFy = warp_sum(S.Fy), sFz = warp_sum(S.Fz);
+	float T[9];
+#pragma unroll
+	for (int k = 0; k < 9; ++k) T[k] = warp_sum(S.T[k]);
+#pragma unroll
+	for (int m = 0; m < GBA_MODES_MAX; ++m) {
+		if (m < (int)Mr) gR[m] = warp_sum(gR[m]);
+		if (m < (int)Ml) gL[m] = warp_sum(gL[m]);
+	}
+	force_lim(sFx, sFy, sFz);
+	float ang[3];
+	torque_reduce(R, T, ang);
+	/* correctModeForce: delta += (float)(4 k * delta^4) */
+#pragma unroll
+	for (int m = 0; m < GBA_MODES_MAX; ++m) {
+		if (m < (int)Mr) {
+			const double dl = gR[m];
+			gR[m] = gR[m] + (float)((double)(4.0f * L.rec.mode_force[m]) * (dl * dl) * (dl * dl));
+		}
+		if (m < (int)Ml) {
+			const double dl = gL[m];
+			gL[m] = gL[m] + (float)((double)(4.0f * L.lig.mode_force[m]) * (dl * dl) * (dl * dl));
+		}
+	}
+	/* Result_6D_Modes: E, pos xyz, ang xyz, modesRec[10], modesLig[10] */
+	float v = 0.f;
+	if (lane == 0) v = sE;
+	else if (lane == 1) v = sFx;
+	else if (lane == 2) v = sFy;
+	else if (lane == 3) v = sFz;
+	else if (lane == 4) v = ang[0];
+	else if (lane == 5) v = ang[1];
+	else if (lane == 6) v = ang[2];
+#pragma unroll
+	for (int m = 0; m < GBA_MODES_MAX; ++m) {
+		if (lane == 7 + m) v = m < (int)Mr ? gR[m] : 0.f;
+		if (lane == 17 + m) v = m < (int)Ml ? gL[m] : 0.f;
+	}
+	return v;
 }
 
 __global__ void __launch_bounds__(256) modes_energy_kernel(const ModesLaunch L) {
+	__shared__ WarpStage stage[8];
 	const int lane = threadIdx.x & 31;
 	const size_t warp = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
 	const size_t nwarps = ((size_t)gridDim.x * blockDim.x) >> 5;
 	for (size_t p = warp; p < L.n; p += nwarps) {
 		const float* d = reinterpret_cast<const float*>(L.dofs + p);
 		const float dv = lane < 26 ? __ldg(d + lane) : 0.f;
-		const float v = eval_pose_modes(L, dv, lane);
+		const float v = eval_pose_modes(L, dv, lane, stage[threadIdx.x >> 5]);
 		if (lane < 27) reinterpret_cast<float*>(L.out + p)[lane] = v;
 	}
 }
@@ -241,16 +274,36 @@ __global__ void __launch_bounds__(256) modes_energy_kernel(const ModesLaunch L) 
 /* Persistent VA13 over (ang xyz, pos xyz, modesRec[0..Mr), modesLig[0..Ml)):
  * the minimizer of minimize.cu generalised to 6 + Mr + Ml DOF (minfor.f is
  * fixed at 6, src/apps/em/minfor.f:16,33). */
+__device__ __forceinline__ unsigned long long modes_global_ns() {
+	unsigned long long t;
+	asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+	return t;
+}
+
 __global__ void __launch_bounds__(256) minimize_modes_kernel(const ModesMinLaunch M) {
+	__shared__ WarpStage stage[8];
 	const int lane = threadIdx.x & 31;
 	const ModesLaunch& L = M.m;
 	const uint32_t Mr = L.rec.n_modes, Ml = L.lig.n_modes;
 	const int jn = 6 + (int)Mr + (int)Ml;
+	unsigned long long t_start = 0;
+	if (lane == 0) t_start = modes_global_ns();
+	t_start = __shfl_sync(GBA_FULL_MASK, t_start, 0);
+	/* lane 0 reads the clock, the warp decides together */
+	auto over_cap = [&]() {
+		int over = 0;
+		if (lane == 0) over = modes_global_ns() - t_start > kMinimizeHardCapNs;
+		return __shfl_sync(GBA_FULL_MASK, over, 0) != 0;
+	};
 	for (;;) {
 		unsigned long long slot = 0;
 		if (lane == 0) slot = atomicAdd(M.counter, 1ull);
 		slot = __shfl_sync(GBA_FULL_MASK, slot, 0);
 		if (slot >= M.n) break;
+		if (over_cap()) {
+			if (lane == 0) atomicExch(M.status, GBA_ERR_TIMEOUT);
+			break;
+		}
 		const size_t p = (size_t)slot;
 		VA13<6 + 2 * GBA_MODES_MAX> va;
 		/* lane k holds DOF float k (pos, ang, modesRec[10], modesLig[10]) */
@@ -280,7 +333,7 @@ __global__ void __launch_bounds__(256) minimize_modes_kernel(const ModesMinLaunc
 				const float t = __shfl_sync(GBA_FULL_MASK, lane == 0 ? rec[k] : 0.f, 0);
 				if (lane == k) dv = t;
 			}
-			v = eval_pose_modes(L, dv, lane);
+			v = eval_pose_modes(L, dv, lane, stage[threadIdx.x >> 5]);
 			++nev;
 			/* gather the result record on lane 0 */
 			float res[27];
@@ -296,22 +349,19 @@ __global__ void __launch_bounds__(256) minimize_modes_kernel(const ModesMinLaunc
 				done = va.done();
 			}
 			if (__shfl_sync(GBA_FULL_MASK, done, 0)) break;
+			if (nev > M.max_evals + 1) {
+				if (lane == 0) atomicExch(M.status, GBA_ERR_DEVICE_CHECK);
+				break;
+			}
+			if ((nev & 15) == 0 && over_cap()) {
+				if (lane == 0) atomicExch(M.status, GBA_ERR_TIMEOUT);
+				break;
+			}
 		}
 		if (lane < 27) reinterpret_cast<float*>(M.out_result + p)[lane] = v;
 		if (lane < 26) reinterpret_cast<float*>(M.out_state + p)[lane] = dv;
 		if (lane == 0 && M.out_nevals) M.out_nevals[p] = nev;
 	}
-}
-
-cudaError_t launch_minimize_modes(const ModesMinLaunch& M, int blocks, int threads, cudaStream_t s) {
-	minimize_modes_kernel<<<blocks, threads, 0, s>>>(M);
-	return cudaGetLastError();
-}
-
-int minimize_modes_blocks_per_sm(int threads) {
-	int nb = 0;
-	cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, minimize_modes_kernel, threads, 0);
-	return nb > 0 ? nb : 1;
 }
 
 cudaError_t launch_modes_energy(const ModesLaunch& L, int blocks, int threads, cudaStream_t s) {
@@ -322,6 +372,17 @@ cudaError_t launch_modes_energy(const ModesLaunch& L, int blocks, int threads, c
 int modes_blocks_per_sm(int threads) {
 	int nb = 0;
 	cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, modes_energy_kernel, threads, 0);
+	return nb > 0 ? nb : 1;
+}
+
+cudaError_t launch_minimize_modes(const ModesMinLaunch& M, int blocks, int threads, cudaStream_t s) {
+	minimize_modes_kernel<<<blocks, threads, 0, s>>>(M);
+	return cudaGetLastError();
+}
+
+int minimize_modes_blocks_per_sm(int threads) {
+	int nb = 0;
+	cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, minimize_modes_kernel, threads, 0);
 	return nb > 0 ? nb : 1;
 }
 

@@ -79,7 +79,7 @@ Item* Context::find(gba_id id, ItemKind kind) {
 }
 
 gba_id Context::add(std::unique_ptr<Item> item) {
-	std::lock_guard<std::mutex> g(mu);
+	Lock g(mu);
 	gba_id id = next_id++;
 	items.emplace(id, std::move(item));
 	return id;
@@ -111,6 +111,10 @@ TuneParams Context::tuned(const std::string& kind, size_t) const {
 
 Context::~Context() {
 	clear_graphs();
+	for (auto& e : timing_events) {
+		cudaEventDestroy(e.first);
+		cudaEventDestroy(e.second);
+	}
 	if (capture_stream) cudaStreamDestroy(capture_stream);
 	if (pinned_status) cudaFreeHost(pinned_status);
 	for (void* p : pinned_buf)
@@ -367,6 +371,41 @@ int gba_upload_params(gba_ctx* ctx, uint32_t num_types, const gba_ffparam* table
 	GBA_API_END(ctx)
 }
 
+/* Adds the elapsed time of every recorded event pair to the running total. */
+void Context::timing_fold() {
+	for (size_t k = 0; k < timing_used; ++k) {
+		check_cuda(cudaEventSynchronize(timing_events[k].second), "kernel timing: event sync");
+		float ms = 0.f;
+		check_cuda(cudaEventElapsedTime(&ms, timing_events[k].first, timing_events[k].second),
+				"kernel timing: elapsed");
+		timing_ms += ms;
+		++timing_launches;
+	}
+	timing_used = 0;
+}
+
+int gba_kernel_timing(gba_ctx* ctx, int32_t enable) {
+	if (!ctx) return GBA_ERR_INVALID_ARGUMENT;
+	GBA_API_BEGIN
+	ctx->bind();
+	ctx->timing = enable != 0;
+	GBA_API_END(ctx)
+}
+
+int gba_kernel_time(gba_ctx* ctx, double* ms_total, uint64_t* launches, int32_t reset) {
+	if (!ctx || !ms_total || !launches) return GBA_ERR_INVALID_ARGUMENT;
+	GBA_API_BEGIN
+	ctx->bind();
+	ctx->timing_fold();
+	*ms_total = ctx->timing_ms;
+	*launches = ctx->timing_launches;
+	if (reset) {
+		ctx->timing_ms = 0.0;
+		ctx->timing_launches = 0;
+	}
+	GBA_API_END(ctx)
+}
+
 int gba_set_pose_order(gba_ctx* ctx, int enable) {
 	if (!ctx) return GBA_ERR_INVALID_ARGUMENT;
 	ctx->order_enabled = enable != 0;
@@ -377,7 +416,7 @@ int gba_release(gba_ctx* ctx, gba_id id) {
 	if (!ctx) return GBA_ERR_INVALID_ARGUMENT;
 	GBA_API_BEGIN
 	ctx->bind();
-	std::lock_guard<std::mutex> g(ctx->mu);
+	Lock g(ctx->mu);
 	auto it = ctx->items.find(id);
 	if (it == ctx->items.end())
 		throw ApiError(GBA_ERR_UNKNOWN_ID, "gba_release: unknown id " + std::to_string(id));
@@ -397,7 +436,7 @@ int gba_energy_6d(gba_ctx* ctx, gba_id rec, gba_id lig, gba_id grid, gba_id para
 	RigidLaunch L = ctx->rigid_launch(rec, lig, grid, params);
 	cudaStream_t s = (cudaStream_t)stream;
 	const bool din = is_device_pointer(dofs), dout = is_device_pointer(out);
-	std::unique_lock<std::mutex> stage_lock(ctx->stage_mu, std::defer_lock);
+	std::unique_lock<CheckedMutex> stage_lock(ctx->stage_mu, std::defer_lock);
 	if (!din || !dout) stage_lock.lock();
 	L.n = n;
 	L.dofs = din ? dofs : (const gba_dof6d*)ctx->staging(0, n * sizeof(gba_dof6d));
@@ -425,7 +464,7 @@ int gba_energy_6d_modes(gba_ctx* ctx, gba_id rec, gba_id lig, gba_id grid_rec, g
 	ModesLaunch L = ctx->modes_launch(rec, lig, grid_rec, grid_lig, params);
 	cudaStream_t s = (cudaStream_t)stream;
 	const bool din = is_device_pointer(dofs), dout = is_device_pointer(out);
-	std::unique_lock<std::mutex> stage_lock(ctx->stage_mu, std::defer_lock);
+	std::unique_lock<CheckedMutex> stage_lock(ctx->stage_mu, std::defer_lock);
 	if (!din || !dout) stage_lock.lock();
 	L.n = n;
 	L.dofs = din ? dofs : (const gba_dof6d_modes*)ctx->staging(0, n * sizeof(gba_dof6d_modes));
@@ -449,7 +488,7 @@ int gba_census_6d(gba_ctx* ctx, gba_id rec, gba_id lig, gba_id grid, gba_id para
 	if (!dofs || !out || !census) throw ApiError(GBA_ERR_INVALID_ARGUMENT, "gba_census_6d: null pointer");
 	ctx->bind();
 	RigidLaunch L = ctx->rigid_launch(rec, lig, grid, params);
-	std::lock_guard<std::mutex> stage_lock(ctx->stage_mu);
+	Lock stage_lock(ctx->stage_mu);
 	const bool din = is_device_pointer(dofs), dout = is_device_pointer(out), dc = is_device_pointer(census);
 	L.n = n;
 	L.dofs = din ? dofs : (const gba_dof6d*)ctx->staging(0, n * sizeof(gba_dof6d));
@@ -473,7 +512,7 @@ int gba_census_6d(gba_ctx* ctx, gba_id rec, gba_id lig, gba_id grid, gba_id para
 namespace gba {
 
 RigidLaunch Context::rigid_launch(gba_id rec, gba_id lig, gba_id grid, gba_id params) {
-	std::lock_guard<std::mutex> g(mu);
+	Lock g(mu);
 	auto* R = static_cast<ProteinItem*>(find(rec, ItemKind::Protein));
 	auto* Lg = static_cast<ProteinItem*>(find(lig, ItemKind::Protein));
 	auto* G = static_cast<GridItem*>(find(grid, ItemKind::Grid));
@@ -504,7 +543,7 @@ void Context::validate_pair(const ProteinItem& rec, const ProteinItem& lig, cons
 
 ModesLaunch Context::modes_launch(gba_id rec, gba_id lig, gba_id grid_rec, gba_id grid_lig,
 		gba_id params) {
-	std::lock_guard<std::mutex> g(mu);
+	Lock g(mu);
 	auto* R = static_cast<ProteinItem*>(find(rec, ItemKind::Protein));
 	auto* Lg = static_cast<ProteinItem*>(find(lig, ItemKind::Protein));
 	auto* GR = static_cast<GridItem*>(find(grid_rec, ItemKind::Grid));
@@ -545,7 +584,22 @@ void Context::run_rigid(RigidLaunch& L, cudaStream_t s) {
 	size_t want = (L.n + warps_per_block - 1) / warps_per_block;
 	size_t blocks = std::min<size_t>(want, (size_t)num_sms * bps);
 	if (blocks == 0) blocks = 1;
+	if (!timing) {
+		check_cuda(launch_rigid_energy(L, (int)blocks, threads, s), "rigid energy launch");
+		return;
+	}
+	if (timing_used == kTimingPool) timing_fold();
+	if (timing_used == timing_events.size()) {
+		std::pair<cudaEvent_t, cudaEvent_t> e{};
+		check_cuda(cudaEventCreate(&e.first), "kernel timing: event");
+		check_cuda(cudaEventCreate(&e.second), "kernel timing: event");
+		timing_events.push_back(e);
+	}
+	auto& e = timing_events[timing_used];
+	check_cuda(cudaEventRecord(e.first, s), "kernel timing: record");
 	check_cuda(launch_rigid_energy(L, (int)blocks, threads, s), "rigid energy launch");
+	check_cuda(cudaEventRecord(e.second, s), "kernel timing: record");
+	++timing_used;
 }
 
 }  // namespace gba

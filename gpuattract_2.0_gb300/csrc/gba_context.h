@@ -6,7 +6,9 @@
 
 #include <map>
 #include <memory>
+#include <atomic>
 #include <mutex>
+#include <thread>
 #include <stdexcept>
 #include <string>
 #include <unordered_map>
@@ -22,6 +24,27 @@ struct ApiError : std::runtime_error {
 	int code;
 	ApiError(int c, const std::string& m) : std::runtime_error(m), code(c) {}
 };
+
+/* A mutex that refuses to be taken twice by the same thread: a nested lock
+ * becomes an ApiError instead of a silent self-deadlock. */
+class CheckedMutex {
+public:
+	void lock() {
+		if (owner_.load(std::memory_order_relaxed) == std::this_thread::get_id())
+			throw ApiError(GBA_ERR_INVALID_ARGUMENT, "internal error: context lock taken twice by one thread");
+		m_.lock();
+		owner_.store(std::this_thread::get_id(), std::memory_order_relaxed);
+	}
+	void unlock() {
+		owner_.store(std::thread::id(), std::memory_order_relaxed);
+		m_.unlock();
+	}
+
+private:
+	std::mutex m_;
+	std::atomic<std::thread::id> owner_{};
+};
+using Lock = std::lock_guard<CheckedMutex>;
 
 void check_cuda(cudaError_t e, const char* what);
 bool is_device_pointer(const void* p);
@@ -117,8 +140,8 @@ struct Context {
 	~Context();
 	int device = 0;
 	int num_sms = 0;
-	std::mutex mu;                 /* items map */
-	std::mutex stage_mu;           /* host-pointer staging buffers */
+	CheckedMutex mu;               /* items map */
+	CheckedMutex stage_mu;         /* host-pointer staging buffers */
 	std::unordered_map<gba_id, std::unique_ptr<Item>> items;
 	gba_id next_id = 1;
 	DevBuffer stage[6];
@@ -165,6 +188,15 @@ struct Context {
 	void run_rigid(RigidLaunch& L, cudaStream_t s);
 	ModesLaunch modes_launch(gba_id rec, gba_id lig, gba_id grid_rec, gba_id grid_lig, gba_id params);
 	void run_modes(ModesLaunch& L, cudaStream_t s);
+
+	/* CUDA-event timing of the fused rigid energy kernel (gba_kernel_timing) */
+	static constexpr size_t kTimingPool = 1024;
+	bool timing = false;
+	std::vector<std::pair<cudaEvent_t, cudaEvent_t>> timing_events;
+	size_t timing_used = 0;
+	double timing_ms = 0.0;
+	uint64_t timing_launches = 0;
+	void timing_fold();
 };
 
 }  // namespace gba

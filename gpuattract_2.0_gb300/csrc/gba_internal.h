@@ -99,6 +99,10 @@ cudaError_t launch_rigid_energy(const RigidLaunch& L, int blocks, int threads, c
 
 /* ---- persistent minimizer (minimize.cu) ---------------------------------- */
 
+/* Without a caller deadline, no warp of a minimizer kernel runs longer than
+ * this (it stops with GBA_ERR_TIMEOUT): every device loop has a bound. */
+constexpr unsigned long long kMinimizeHardCapNs = 600ull * 1000000000ull;
+
 struct MinLaunch {
 	const RigidModel* models;       /* device array, one per pair */
 	const uint32_t* pair_of;        /* per pose pair index; nullptr = pair 0 */
@@ -159,6 +163,7 @@ struct ModesMinLaunch {
 	size_t n;
 	int max_evals;
 	unsigned long long* counter;    /* zeroed before launch */
+	int* status;                    /* GBA_OK, set to TIMEOUT / DEVICE_CHECK by the kernel */
 };
 
 cudaError_t launch_minimize_modes(const ModesMinLaunch& M, int blocks, int threads, cudaStream_t s);

@@ -240,7 +240,7 @@ extern "C" int gba_build_grid(gba_ctx* ctx, gba_id rec, gba_id params,
 		ProteinItem* R;
 		ParamsItem* P;
 		{
-			std::lock_guard<std::mutex> g(ctx->mu);
+			Lock g(ctx->mu);
 			R = static_cast<ProteinItem*>(ctx->find(rec, ItemKind::Protein));
 			P = static_cast<ParamsItem*>(ctx->find(params, ItemKind::Params));
 		}
@@ -325,7 +325,7 @@ extern "C" int gba_grid_info(gba_ctx* ctx, gba_id grid, gba_intrpl_desc* inner,
 		gba_intrpl_desc* outer, gba_nl_desc* nl) {
 	if (!ctx) return GBA_ERR_INVALID_ARGUMENT;
 	try {
-		std::lock_guard<std::mutex> g(ctx->mu);
+		Lock g(ctx->mu);
 		auto* G = static_cast<GridItem*>(ctx->find(grid, ItemKind::Grid));
 		if (inner) *inner = G->inner_desc;
 		if (outer) *outer = G->outer_desc;
@@ -344,7 +344,7 @@ extern "C" int gba_download_grid(gba_ctx* ctx, gba_id grid, float* inner, float*
 		ctx->bind();
 		GridItem* G;
 		{
-			std::lock_guard<std::mutex> g(ctx->mu);
+			Lock g(ctx->mu);
 			G = static_cast<GridItem*>(ctx->find(grid, ItemKind::Grid));
 		}
 		if (inner) check_cuda(cudaMemcpy(inner, G->inner.ptr, G->inner.bytes, cudaMemcpyDeviceToHost), "D2H");
@@ -402,8 +402,8 @@ extern "C" int gba_grid_octets(gba_ctx* ctx, gba_id grid, int enable) {
 	if (!ctx) return GBA_ERR_INVALID_ARGUMENT;
 	try {
 		ctx->bind();
-		std::lock_guard<std::mutex> lk(ctx->stage_mu);
-		std::lock_guard<std::mutex> g(ctx->mu);
+		Lock lk(ctx->stage_mu);
+		Lock g(ctx->mu);
 		auto* G = static_cast<GridItem*>(ctx->find(grid, ItemKind::Grid));
 		if (enable) {
 			if (!G->inner_oct.ptr) make_octets(G->inner_desc, G->inner, G->inner_oct);

@@ -14,9 +14,11 @@
  * written -- what RequestHandler::getResultStates / getResultEnGrads report.
  *
  * Termination is bounded by construction: every path through the machine
- * either requests an evaluation (nfun <= maxFunEval) or finishes.  An optional
- * wall-time budget (globaltimer, measured by each warp from its start) stops
- * the claiming of new poses and raises GBA_ERR_TIMEOUT in a device status word.
+ * either requests an evaluation (nfun <= maxFunEval) or finishes; a pose that
+ * went past maxFunEval + 1 evaluations would raise GBA_ERR_DEVICE_CHECK.  A
+ * wall-time budget (globaltimer, read by lane 0 of each warp from its start:
+ * the caller's deadline, else kMinimizeHardCapNs) stops the warp and raises
+ * GBA_ERR_TIMEOUT in a device status word.
  */
 #include <algorithm>
 #include <vector>
@@ -33,17 +35,29 @@ __device__ __forceinline__ unsigned long long global_ns() {
 	return t;
 }
 
+/* Lane 0 reads the clock and the whole warp takes its decision. */
+__device__ __forceinline__ bool warp_over_budget(unsigned long long t_start, unsigned long long budget_ns,
+		int lane) {
+	int over = 0;
+	if (lane == 0) over = global_ns() - t_start > budget_ns;
+	return __shfl_sync(GBA_FULL_MASK, over, 0) != 0;
+}
+
 __global__ void __launch_bounds__(256) minimize_rigid_kernel(const MinLaunch L) {
 	__shared__ WarpStage stage[8];   /* one per warp of a <=256-thread block */
 	const int lane = threadIdx.x & 31;
-	const unsigned long long t_start = global_ns();
+	unsigned long long t_start = 0;
+	if (lane == 0) t_start = global_ns();
+	t_start = __shfl_sync(GBA_FULL_MASK, t_start, 0);
 	if (lane == 0 && L.t0) atomicMin(L.t0, t_start);
+	/* the caller's wall-time budget, else a hard cap on any warp's run time */
+	const unsigned long long budget = L.budget_ns ? L.budget_ns : kMinimizeHardCapNs;
 	for (;;) {
 		unsigned long long base = 0;
 		if (lane == 0) base = atomicAdd(L.counter, (unsigned long long)L.chunk);
 		base = __shfl_sync(GBA_FULL_MASK, base, 0);
 		if (base >= L.n) break;
-		if (L.budget_ns && global_ns() - t_start > L.budget_ns) {
+		if (warp_over_budget(t_start, budget, lane)) {
 			if (lane == 0) atomicExch(L.status, GBA_ERR_TIMEOUT);
 			break;
 		}
@@ -81,6 +95,16 @@ __global__ void __launch_bounds__(256) minimize_rigid_kernel(const MinLaunch L) 
 					done = va.done();
 				}
 				if (__shfl_sync(GBA_FULL_MASK, done, 0)) break;
+				/* VA13 ends within max_evals + 1 evaluations; anything past that is
+				 * a broken machine, reported instead of looping */
+				if (nev > L.max_evals + 1) {
+					if (lane == 0) atomicExch(L.status, GBA_ERR_DEVICE_CHECK);
+					break;
+				}
+				if ((nev & 15) == 0 && warp_over_budget(t_start, budget, lane)) {
+					if (lane == 0) atomicExch(L.status, GBA_ERR_TIMEOUT);
+					break;
+				}
 			}
 			store_result7(reinterpret_cast<float*>(L.out_result + p), res, lane);
 			if (lane < 6) reinterpret_cast<float*>(L.out_state + p)[lane] = cur[lane];

@@ -190,12 +190,9 @@ int gba_batch_minimize_6d(gba_ctx* ctx, const gba_pair_job* jobs, size_t njobs, 
 			throw ApiError(GBA_ERR_INVALID_ARGUMENT, "gba_batch_minimize_6d: null out_state");
 	ctx->bind();
 	cudaStream_t s = (cudaStream_t)stream;
-	std::lock_guard<std::mutex> lk(ctx->stage_mu);
-	Gathered G;
-	{
-		std::lock_guard<std::mutex> g(ctx->mu);
-		G = gather_jobs(ctx, jobs, njobs);
-	}
+	Lock lk(ctx->stage_mu);
+	/* rigid_launch takes the items lock itself */
+	Gathered G = gather_jobs(ctx, jobs, njobs);
 	if (G.total == 0) return GBA_OK;
 	const size_t n = G.total;
 	const bool single_dev = njobs == 1 && is_device_pointer(jobs[0].start) &&
@@ -258,6 +255,8 @@ int gba_batch_minimize_6d(gba_ctx* ctx, const gba_pair_job* jobs, size_t njobs, 
 	}
 	if (status == GBA_ERR_TIMEOUT)
 		throw ApiError(GBA_ERR_TIMEOUT, "minimization stopped: device wall-time budget exhausted");
+	if (status == GBA_ERR_DEVICE_CHECK)
+		throw ApiError(GBA_ERR_DEVICE_CHECK, "minimization stopped: a pose exceeded its evaluation budget");
 	GBA_CATCH(ctx)
 }
 
@@ -268,12 +267,9 @@ int gba_batch_energy_6d(gba_ctx* ctx, const gba_pair_job* jobs, size_t njobs, vo
 	if (!jobs) throw ApiError(GBA_ERR_INVALID_ARGUMENT, "gba_batch_energy_6d: null jobs");
 	ctx->bind();
 	cudaStream_t s = (cudaStream_t)stream;
-	std::lock_guard<std::mutex> lk(ctx->stage_mu);
-	Gathered G;
-	{
-		std::lock_guard<std::mutex> g(ctx->mu);
-		G = gather_jobs(ctx, jobs, njobs);
-	}
+	Lock lk(ctx->stage_mu);
+	/* rigid_launch takes the items lock itself */
+	Gathered G = gather_jobs(ctx, jobs, njobs);
 	if (G.total == 0) return GBA_OK;
 	const size_t n = G.total;
 	BatchEnergyLaunch L{};
@@ -302,12 +298,13 @@ int gba_minimize_6d_plain(gba_ctx* ctx, gba_id rec, gba_id lig, gba_id grid, gba
 	if (n == 0) return GBA_OK;
 	if (!start || !out_state || !out_result)
 		throw ApiError(GBA_ERR_INVALID_ARGUMENT, "gba_minimize_6d_plain: null pointer");
+	if (max_evals < 0) throw ApiError(GBA_ERR_INVALID_ARGUMENT, "max_evals < 0");
 	if (is_device_pointer(start) || is_device_pointer(out_state) || is_device_pointer(out_result))
 		throw ApiError(GBA_ERR_INVALID_ARGUMENT, "gba_minimize_6d_plain: host pointers required");
 	ctx->bind();
 	cudaStream_t s = (cudaStream_t)stream;
 	RigidLaunch L = ctx->rigid_launch(rec, lig, grid, params);
-	std::lock_guard<std::mutex> lk(ctx->stage_mu);
+	Lock lk(ctx->stage_mu);
 	/* pinned request/result buffers, like the server's HostPinnedAllocator
 	 * buffers (src/service/GPUEnergyService.tpp:22-23) */
 	gba_dof6d* hin = (gba_dof6d*)ctx->pinned(0, n * sizeof(gba_dof6d));
@@ -323,7 +320,10 @@ int gba_minimize_6d_plain(gba_ctx* ctx, gba_id rec, gba_id lig, gba_id grid, gba
 		va[p].start(x0, 6, max_evals);
 		active[p] = p;
 	}
-	while (!active.empty()) {
+	/* VA13 ends within max_evals + 1 evaluations per pose: so do the rounds */
+	for (int round = 0; !active.empty(); ++round) {
+		if (round > max_evals + 1)
+			throw ApiError(GBA_ERR_DEVICE_CHECK, "plain minimization: a pose exceeded its evaluation budget");
 		const size_t na = active.size();
 		for (size_t k = 0; k < na; ++k) {
 			const double* pt = va[active[k]].point();
@@ -379,7 +379,7 @@ int gba_minimize_6d_modes(gba_ctx* ctx, gba_id rec, gba_id lig, gba_id grid_rec,
 	cudaStream_t s = (cudaStream_t)stream;
 	ModesMinLaunch M{};
 	M.m = ctx->modes_launch(rec, lig, grid_rec, grid_lig, params);
-	std::lock_guard<std::mutex> lk(ctx->stage_mu);
+	Lock lk(ctx->stage_mu);
 	const bool dev = is_device_pointer(start) && is_device_pointer(out_state) &&
 			is_device_pointer(out_result) && (!out_nevals || is_device_pointer(out_nevals));
 	M.n = n;
@@ -400,8 +400,10 @@ int gba_minimize_6d_modes(gba_ctx* ctx, gba_id rec, gba_id lig, gba_id grid_rec,
 		ctx->aux.alloc(64);
 		check_cuda(cudaMallocHost((void**)&ctx->pinned_status, sizeof(int32_t)), "cudaMallocHost");
 	}
+	/* aux [12,16): modes status, [16,24): modes cursor */
+	M.status = (int*)((char*)ctx->aux.ptr + 12);
 	M.counter = (unsigned long long*)((char*)ctx->aux.ptr + 16);
-	check_cuda(cudaMemsetAsync(M.counter, 0, 8, s), "modes minimize: cursor");
+	check_cuda(cudaMemsetAsync((char*)ctx->aux.ptr + 12, 0, 12, s), "modes minimize: cursor");
 	const int threads = 128;
 	const int bps = minimize_modes_blocks_per_sm(threads);
 	size_t blocks = std::max<size_t>(1, std::min<size_t>((n * 32 + threads - 1) / threads,
@@ -412,7 +414,13 @@ int gba_minimize_6d_modes(gba_ctx* ctx, gba_id rec, gba_id lig, gba_id grid_rec,
 		copy_out(out_result, M.out_result, n * sizeof(gba_result6d_modes), s);
 		if (out_nevals) copy_out(out_nevals, M.out_nevals, n * sizeof(int32_t), s);
 	}
+	check_cuda(cudaMemcpyAsync(ctx->pinned_status, M.status, sizeof(int32_t), cudaMemcpyDeviceToHost, s),
+			"modes minimize: status");
 	check_cuda(cudaStreamSynchronize(s), "modes minimize");
+	if (*ctx->pinned_status == GBA_ERR_TIMEOUT)
+		throw ApiError(GBA_ERR_TIMEOUT, "modes minimization stopped: device wall-time cap reached");
+	if (*ctx->pinned_status == GBA_ERR_DEVICE_CHECK)
+		throw ApiError(GBA_ERR_DEVICE_CHECK, "modes minimization stopped: a pose exceeded its evaluation budget");
 	GBA_CATCH(ctx)
 }
 
@@ -425,13 +433,14 @@ int gba_minimize_6d_modes_plain(gba_ctx* ctx, gba_id rec, gba_id lig, gba_id gri
 	if (n == 0) return GBA_OK;
 	if (!start || !out_state || !out_result)
 		throw ApiError(GBA_ERR_INVALID_ARGUMENT, "gba_minimize_6d_modes_plain: null pointer");
+	if (max_evals < 0) throw ApiError(GBA_ERR_INVALID_ARGUMENT, "max_evals < 0");
 	if (is_device_pointer(start) || is_device_pointer(out_state) || is_device_pointer(out_result))
 		throw ApiError(GBA_ERR_INVALID_ARGUMENT, "gba_minimize_6d_modes_plain: host pointers required");
 	ctx->bind();
 	cudaStream_t s = (cudaStream_t)stream;
 	ModesLaunch L = ctx->modes_launch(rec, lig, grid_rec, grid_lig, params);
 	const int Mr = (int)L.rec.n_modes, Ml = (int)L.lig.n_modes, jn = 6 + Mr + Ml;
-	std::lock_guard<std::mutex> lk(ctx->stage_mu);
+	Lock lk(ctx->stage_mu);
 	auto* hin = (gba_dof6d_modes*)ctx->pinned(0, n * sizeof(gba_dof6d_modes));
 	auto* hout = (gba_result6d_modes*)ctx->pinned(1, n * sizeof(gba_result6d_modes));
 	auto* din = (gba_dof6d_modes*)ctx->staging(0, n * sizeof(gba_dof6d_modes));
@@ -447,7 +456,10 @@ int gba_minimize_6d_modes_plain(gba_ctx* ctx, gba_id rec, gba_id lig, gba_id gri
 		va[p].start(x0, jn, max_evals);
 		active[p] = p;
 	}
-	while (!active.empty()) {
+	/* VA13 ends within max_evals + 1 evaluations per pose: so do the rounds */
+	for (int round = 0; !active.empty(); ++round) {
+		if (round > max_evals + 1)
+			throw ApiError(GBA_ERR_DEVICE_CHECK, "plain minimization: a pose exceeded its evaluation budget");
 		const size_t na = active.size();
 		for (size_t k = 0; k < na; ++k) {
 			const double* pt = va[active[k]].point();

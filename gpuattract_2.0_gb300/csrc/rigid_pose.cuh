@@ -119,6 +119,87 @@ __device__ __forceinline__ void stage_bead(const RigidModel& M, const PoseRot& R
 	}
 }
 
+/* Grid bookkeeping of a staged bead at position (px, py, pz): picks inner or
+ * outer grid, stores octet offset and trilinear weights in slot s and returns
+ * the number of lookups (0, 1, or 2 with the charge channel). */
+__device__ __forceinline__ uint32_t stage_grid(const DevGrid& G, float px, float py, float pz,
+		uint32_t mapped, float q, int s, WarpStage& W) {
+	if (mapped == 0) return 0;
+	const bool inner = !grid_out(G.inner, px, py, pz);
+	const bool outer = !inner && !grid_out(G.outer, px, py, pz);
+	if (!(inner | outer)) return 0;
+	const DevIntrpl& g = inner ? G.inner : G.outer;
+	const uint32_t ix = min((uint32_t)floorf(fmul(fsub(px, g.pos[0]), g.dVox_inv)), g.dimN[0] - 2);
+	const uint32_t iy = min((uint32_t)floorf(fmul(fsub(py, g.pos[1]), g.dVox_inv)), g.dimN[1] - 2);
+	const uint32_t iz = min((uint32_t)floorf(fmul(fsub(pz, g.pos[2]), g.dVox_inv)), g.dimN[2] - 2);
+	const float minx = fadd(fmul((float)ix, g.dVox), g.pos[0]);
+	const float miny = fadd(fmul((float)iy, g.dVox), g.pos[1]);
+	const float minz = fadd(fmul((float)iz, g.dVox), g.pos[2]);
+	W.wnx[s] = fsub(px, minx); W.wny[s] = fsub(py, miny); W.wnz[s] = fsub(pz, minz);
+	W.wxx[s] = fsub(fadd(minx, g.dVox), px);
+	W.wxy[s] = fsub(fadd(miny, g.dVox), py);
+	W.wxz[s] = fsub(fadd(minz, g.dVox), pz);
+	W.off[s] = g.oct ? (g.dimN[0] - 1) * (iz * (g.dimN[1] - 1) + iy) + ix
+	                 : g.dimN[0] * (iz * g.dimN[1] + iy) + ix;
+	W.chan[s] = mapped | (outer ? 0x80000000u : 0u);
+	return fabsf(q) > 0.001f ? 2u : 1u;
+}
+
+/* One queued lookup: the channel's interpolated (fx, fy, fz, E), scaled by
+ * 1/voxelVol and, for the charge channel, by the bead charge. */
+__device__ __forceinline__ float4 grid_lookup(const DevGrid& G, const WarpStage& W, uint32_t e) {
+	const uint32_t s = e >> 1;
+	const bool is_q = e & 1u;
+	const uint32_t ch = W.chan[s];
+	const DevIntrpl& g = (ch & 0x80000000u) ? G.outer : G.inner;
+	const uint32_t c = is_q ? 0u : (ch & 0x7fffffffu);
+	float4 v;
+	if (g.oct) {
+		const size_t nocts = (size_t)(g.dimN[0] - 1) * (g.dimN[1] - 1) * (g.dimN[2] - 1);
+		v = octet_lerp(g.oct + 8 * ((size_t)c * nocts + W.off[s]), 2, 4, W.wnx[s], W.wny[s], W.wnz[s],
+				W.wxx[s], W.wxy[s], W.wxz[s]);
+	} else {
+		const uint32_t sx = g.dimN[0], sxy = g.dimN[0] * g.dimN[1];
+		v = octet_lerp(g.data + (size_t)c * (sxy * g.dimN[2]) + W.off[s], sx, sxy, W.wnx[s], W.wny[s],
+				W.wnz[s], W.wxx[s], W.wxy[s], W.wxz[s]);
+	}
+	const float sc = is_q ? g.voxelVol_inv * W.q[s] : g.voxelVol_inv;
+	v.x *= sc; v.y *= sc; v.z *= sc; v.w *= sc;
+	return v;
+}
+
+/* Writes the lookup queue entries of slot s (n = 0..2) at position k. */
+__device__ __forceinline__ void enqueue_lookups(WarpStage& W, uint32_t& k, int s, uint32_t n) {
+	if (n > 0) W.look[k++] = (uint8_t)(s << 1);
+	if (n > 1) W.look[k++] = (uint8_t)((s << 1) | 1);
+}
+
+/* Owner slot of flattened pair k: the last s with nl_pre[s] <= k. */
+__device__ __forceinline__ uint32_t pair_owner(const WarpStage& W, uint32_t k) {
+	uint32_t lo = 0, hi = kBeadsPerRound;
+#pragma unroll
+	for (int it = 0; it < 6; ++it) {
+		const uint32_t mid = (lo + hi) >> 1;
+		if (W.nl_pre[mid] <= k) lo = mid; else hi = mid;
+	}
+	return lo;
+}
+
+/* NL voxel lookup of a staged bead (type != 0), NLPotForce's
+ * src/model/neighborlist.h:59-66; returns the list length (0 outside). */
+__device__ __forceinline__ uint32_t stage_nl(const DevNL& nl, float px, float py, float pz, int s,
+		WarpStage& W, bool& in_nl) {
+	in_nl = false;
+	if (nl_out(nl, px, py, pz)) return 0;
+	const int ix = min(max((int)roundf(fmul(fsub(px, nl.pos[0]), nl.dVox_inv)), 0), (int)nl.dimN[0] - 1);
+	const int iy = min(max((int)roundf(fmul(fsub(py, nl.pos[1]), nl.dVox_inv)), 0), (int)nl.dimN[1] - 1);
+	const int iz = min(max((int)roundf(fmul(fsub(pz, nl.pos[2]), nl.dVox_inv)), 0), (int)nl.dimN[2] - 1);
+	const uint2 d = __ldg(&nl.grid[nl.dimN[0] * (iz * nl.dimN[1] + iy) + ix]);
+	W.nl_idx[s] = d.y;
+	in_nl = true;
+	return d.x;
+}
+
 /* Accumulates f into the pose sums with the bead's unrotated coordinates. */
 struct PoseSums {
 	float E = 0.f, Fx = 0.f, Fy = 0.f, Fz = 0.f;

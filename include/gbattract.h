@@ -153,6 +153,15 @@ int gba_release(gba_ctx* ctx, gba_id id);
  * off.  No reference counterpart (a scheduling choice of this library). */
 int gba_set_pose_order(gba_ctx* ctx, int enable);
 
+/* While enabled, CUDA events are recorded on the launching stream around
+ * every fused rigid energy kernel launch (gba_energy_6d and friends);
+ * gba_kernel_time synchronizes on them and returns the summed kernel time
+ * and launch count since the last reset (reset != 0 clears them).  Lets a
+ * caller time the kernel alone inside a call that also launches the
+ * visiting-order pass.  No reference counterpart (instrumentation). */
+int gba_kernel_timing(gba_ctx* ctx, int32_t enable);
+int gba_kernel_time(gba_ctx* ctx, double* ms_total, uint64_t* launches, int32_t reset);
+
 /* ---- evaluation ----------------------------------------------------------- */
 
 /* One energy+gradient evaluation per pose (rigid body), the work of one

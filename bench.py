@@ -10,8 +10,10 @@ metric = energy+gradient evaluations per second.
   e2e      the same metric through the public C ABI with pinned HOST buffers:
            H2D of the poses, the launch, D2H of the results, every step
   roofline algorithmic bytes per launch (census: 52 B per pose + 128 B per
-           grid-channel octet + 8 B per NL voxel lookup + 4 B per list entry)
-           / kernel time, against the measured HBM copy bandwidth
+           grid-channel octet + 8 B per NL voxel lookup + 24 B per list entry:
+           index, receptor xyz, type, charge) / energy-kernel time (CUDA events
+           the library records around the launch), against the measured HBM
+           copy bandwidth
   cpu_baseline  the CPU oracle (a C++ port of the reference CPU path) on a
            bounded sample of the same workload, all host threads
 
@@ -67,7 +69,7 @@ class ClockSampler:
             self.f = open(self.path, "w")
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+                 "-lms", "50"], stdout=self.f, stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
         return self
@@ -213,6 +215,13 @@ def bench_minimization(ctx, pkg, nthreads: int, with_cpu: bool):
         out["cpu_oracle_poses_per_s"] = n / dt
         out["cpu_cores"] = nthreads
         out["agreement_within_1e-3"] = float(np.mean(rel <= 1e-3))
+        # the reference minimizer's own sensitivity: the oracle against itself
+        # with every start pose moved by one ulp in x
+        d1 = wl.dofs.copy()
+        d1[:, 0] = np.nextafter(d1[:, 0], np.float32(np.inf))
+        _, r_ulp, _ = po.minimize_6d(wl.rec, wl.lig, gh, wl.params, d1, steps, nthreads=nthreads)
+        rel = np.abs(r_ulp[:, 0].astype(np.float64) - r_cpu[:, 0]) / np.maximum(np.abs(r_cpu[:, 0]), 1e-3)
+        out["oracle_self_agreement_one_ulp_start"] = float(np.mean(rel <= 1e-3))
     for i in (grid, lig, rec, par):
         ctx.release(i)
     return out
@@ -343,7 +352,7 @@ def bench_batched_uneven(ctx, pkg, pose_scale: float, steps: int):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=30)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gbattract", choices=["gbattract", "reference"])
     ap.add_argument("--poses", type=int, default=None, help="override the pose count")
@@ -354,8 +363,9 @@ def main():
     ap.add_argument("--suite", default="default", choices=["default", "full"],
                     help="full: also configs 2 (modes), 3 (adjoint), 4 (batched uneven pairs)")
     ap.add_argument("--modes-poses", type=int, default=50000)
-    ap.add_argument("--variant", default=None,
-                    help="fix the layout variant, e.g. order=1,octets=1 (default: time all four)")
+    ap.add_argument("--variant", default="order=1,octets=1",
+                    help="layout / visiting-order variant timed, or 'search' to time all four "
+                         "and keep the fastest")
     ap.add_argument("--batch-scale", type=float, default=0.05,
                     help="fraction of config 4's pose counts used by --suite full")
     args = ap.parse_args()
@@ -386,7 +396,7 @@ def main():
     cen, _ = ctx.census_6d(rec, lig, grid, par, dofs)
     cen = cen.cpu().numpy().astype(np.int64)
     bytes_launch = int(52 * n + 128 * (cen[:, 0].sum() + cen[:, 1].sum()) + 8 * cen[:, 2].sum() +
-                       4 * cen[:, 3].sum())
+                       24 * cen[:, 3].sum())
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     stream = torch.cuda.current_stream()
     sptr = stream.cuda_stream
@@ -410,7 +420,7 @@ def main():
     variants = {}
     ref_out = None
     combos = [(o, c) for o in (False, True) for c in (False, True)]
-    if args.variant:
+    if args.variant != "search":
         kv = dict(x.split("=") for x in args.variant.split(","))
         combos = [(kv.get("order", "1") == "1", kv.get("octets", "1") == "1")]
     for order, octets in combos:

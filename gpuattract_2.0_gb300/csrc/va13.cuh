@@ -25,12 +25,23 @@ GBA_HD double va_max(double a, double b) { return a > b ? a : b; }
 GBA_HD double va_min(double a, double b) { return a < b ? a : b; }
 GBA_HD double va_abs(double a) { return a < 0 ? -a : a; }
 
+/* Products are never contracted with a following add: the host build runs
+ * with -ffp-contract=off and the device uses round-to-nearest multiplies, so
+ * both sides take bit-identical steps (nvcc would otherwise form FMAs). */
+GBA_HD double vm(double a, double b) {
+#ifdef __CUDA_ARCH__
+	return __dmul_rn(a, b);
+#else
+	return a * b;
+#endif
+}
+
 /* mc11a: rank-one update of the packed LDL^T factors (mc11a.f:1-112). */
 GBA_HD void mc11a(double* a, int n, double* z, double sig, double* w, int& ir, int mk, double eps) {
 	double ti = 0, v, tim, b, r, y, gm, al;
 	int np, ij = 1, ip, mm, j;
 	if (n > 1) goto L1;
-	a[1] = a[1] + sig * z[1] * z[1];
+	a[1] = a[1] + vm(vm(sig, z[1]), z[1]);
 	ir = 1;
 	if (a[1] > 0.0) return;
 	a[1] = 0.0;
@@ -44,7 +55,7 @@ L1:
 	ij = 1;
 	if (mk == 0) goto L10;
 	for (int i = 1; i <= n; ++i) {
-		if (a[ij] != 0.0) ti = ti + w[i] * w[i] / a[ij];
+		if (a[ij] != 0.0) ti = ti + vm(w[i], w[i]) / a[ij];
 		ij = ij + np - i;
 	}
 	goto L20;
@@ -54,11 +65,11 @@ L10:
 		ip = i + 1;
 		v = w[i];
 		if (a[ij] > 0.0) {
-			ti = ti + v * v / a[ij];
+			ti = ti + vm(v, v) / a[ij];
 			if (i != n)
 				for (j = ip; j <= n; ++j) {
 					ij = ij + 1;
-					w[j] = w[j] - v * a[ij];
+					w[j] = w[j] - vm(v, a[ij]);
 				}
 			ij = ij + 1;
 		} else {
@@ -84,7 +95,7 @@ L23:
 	for (int i = 1; i <= n; ++i) {
 		j = np - i;
 		ij = ij - i;
-		if (a[ij] != 0.0) tim = ti - w[j] * w[j] / a[ij];
+		if (a[ij] != 0.0) tim = ti - vm(w[j], w[j]) / a[ij];
 		w[j] = ti;
 		ti = tim;
 	}
@@ -104,7 +115,7 @@ L41:
 				continue;
 			}
 			ir = 1 - ir;
-			a[ij] = v * v / tim;
+			a[ij] = vm(v, v) / tim;
 			if (i == n) return;
 			for (j = ip; j <= n; ++j) {
 				ij = ij + 1;
@@ -113,10 +124,10 @@ L41:
 			return;
 		}
 		al = v / a[ij];
-		if (mm <= 0) ti = tim + v * al;
+		if (mm <= 0) ti = tim + vm(v, al);
 		else ti = w[i];
 		r = ti / tim;
-		a[ij] = a[ij] * r;
+		a[ij] = vm(a[ij], r);
 		if (r == 0.0) break;
 		if (i == n) break;
 		b = al / ti;
@@ -125,14 +136,14 @@ L41:
 			for (j = ip; j <= n; ++j) {
 				ij = ij + 1;
 				y = a[ij];
-				a[ij] = b * z[j] + y * gm;
-				z[j] = z[j] - v * y;
+				a[ij] = vm(b, z[j]) + vm(y, gm);
+				z[j] = z[j] - vm(v, y);
 			}
 		} else {
 			for (j = ip; j <= n; ++j) {
 				ij = ij + 1;
-				z[j] = z[j] - v * a[ij];
-				a[ij] = a[ij] + b * z[j];
+				z[j] = z[j] - vm(v, a[ij]);
+				a[ij] = a[ij] + vm(b, z[j]);
 			}
 		}
 		tim = ti;
@@ -154,7 +165,7 @@ GBA_HD void mc11e(const double* a, int n, double* z, double* w, int ir) {
 		ij = i;
 		double v = z[i];
 		for (int j = 1; j <= i - 1; ++j) {
-			v = v - a[ij] * z[j];
+			v = v - vm(a[ij], z[j]);
 			ij = ij + n - j;
 		}
 		w[i] = v;
@@ -169,7 +180,7 @@ GBA_HD void mc11e(const double* a, int n, double* z, double* w, int ir) {
 		ij = ii;
 		for (int j = i + 1; j <= n; ++j) {
 			ii = ii + 1;
-			v = v - a[ii] * z[j];
+			v = v - vm(a[ii], z[j]);
 		}
 		z[i] = v;
 	}
@@ -207,7 +218,7 @@ struct VA13 {
 		for (int i = 1; i <= k; ++i) h[i] = xnull;
 		k = 1;
 		for (int i = 1; i <= jn; ++i) {
-			h[k] = 0.01 * c;
+			h[k] = vm(0.01, c);
 			k = k + np - i;
 		}
 		dff = xnull;
@@ -238,8 +249,8 @@ struct VA13 {
 		{
 			double gl1 = xnull, gl2 = xnull;
 			for (i = 1; i <= jn; ++i) {
-				gl1 = gl1 + g[i] * g[i];
-				gl2 = gl2 + gb[i] * gb[i];
+				gl1 = gl1 + vm(g[i], g[i]);
+				gl2 = gl2 + vm(gb[i], gb[i]);
 			}
 			if (gl2 >= gl1) goto L220;
 		}
@@ -252,8 +263,8 @@ struct VA13 {
 		}
 	L220:
 		dgb = xnull;
-		for (i = 1; i <= jn; ++i) dgb = dgb + gb[i] * d[i];
-		if (fb - fa <= 0.1 * c * dga) goto L280;
+		for (i = 1; i <= jn; ++i) dgb = dgb + vm(gb[i], d[i]);
+		if (fb - fa <= vm(vm(0.1, c), dga)) goto L280;
 		if (step > steplb) goto L270;
 	L240:
 		if (isfv >= 2) goto L110;
@@ -261,20 +272,20 @@ struct VA13 {
 		return;
 	L270:
 		stepbd = step;
-		c = gmin + dgb - 3.0 * (fb - fmin) / step;
-		c = gmin / (c + gmin - sqrt(c * c - gmin * dgb));
-		step = step * va_max(0.1, c);
+		c = gmin + dgb - vm(3.0, fb - fmin) / step;
+		c = gmin / (c + gmin - sqrt(vm(c, c) - vm(gmin, dgb)));
+		step = vm(step, va_max(0.1, c));
 		goto L170;
 	L280:
 		stepbd = stepbd - step;
 		stmin = c;
 		fmin = fb;
 		gmin = dgb;
-		step = 9.0 * stmin;
-		if (stepbd > xnull) step = 0.5 * stepbd;
-		c = dga + 3.0 * dgb - 4.0 * (fb - fa) / stmin;
-		if (c > xnull) step = va_min(step, stmin * va_max(1.0, -dgb / c));
-		if (dgb < 0.7 * dga) goto L170;
+		step = vm(9.0, stmin);
+		if (stepbd > xnull) step = vm(0.5, stepbd);
+		c = dga + vm(3.0, dgb) - vm(4.0, fb - fa) / stmin;
+		if (c > xnull) step = va_min(step, vm(stmin, va_max(1.0, -dgb / c)));
+		if (dgb < vm(0.7, dga)) goto L170;
 		isfv = 4 - isfv;
 		if (stmin + step <= steplb) goto L240;
 		ir = -jn;
@@ -286,7 +297,7 @@ struct VA13 {
 		}
 		mc11a(h, jn, xbb, 1.0 / dga, w, ir, 1, xnull);
 		ir = -ir;
-		mc11a(h, jn, d, 1.0 / (stmin * (dgb - dga)), d, ir, 0, xnull);
+		mc11a(h, jn, d, 1.0 / vm(stmin, dgb - dga), d, ir, 0, xnull);
 		if (ir < jn) {
 			phase = kDone;
 			return;
@@ -306,7 +317,7 @@ struct VA13 {
 		dga = xnull;
 		for (i = 1; i <= jn; ++i) {
 			c = va_max(c, va_abs(d[i]));
-			dga = dga + ga[i] * d[i];
+			dga = dga + vm(ga[i], d[i]);
 		}
 		if (dga >= xnull) goto L240;
 		stmin = xnull;
@@ -324,7 +335,7 @@ struct VA13 {
 			return;
 		}
 		nfun = nfun + 1;
-		for (i = 1; i <= jn; ++i) xbb[i] = xaa[i] + c * d[i];
+		for (i = 1; i <= jn; ++i) xbb[i] = xaa[i] + vm(c, d[i]);
 		phase = kAfterLine;
 	}
 };

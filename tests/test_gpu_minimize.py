@@ -4,14 +4,15 @@
   machine on the same per-pose energy code, so their trajectories are
   identical bit for bit.
 * Against the CPU oracle (VA13 restated from minfor.f/mc11a.f, driving the
-  FP32 CPU energy) the minimized energies agree within 1e-3 relative for at
-  least 99% of poses (line-search branches may split trajectories whose
-  energies differ in the last bits).
+  FP32 CPU energy) the minimized energies agree as closely as the oracle
+  agrees with itself under a one-ulp change of the start pose (the reference
+  minimizer is chaotic at FP32 noise level; see test_against_cpu_oracle_va13).
 * The evaluation budget bounds every pose; a wall-time budget stops the
   kernel with GBA_ERR_TIMEOUT and leaves the context usable."""
 import numpy as np
 import pytest
 
+from conftest import minimized_agreement
 from test_gpu_rigid import upload
 
 pytestmark = pytest.mark.gpu
@@ -52,15 +53,33 @@ def test_device_equals_plain_form(min_case, ctx):
 
 
 def test_against_cpu_oracle_va13(min_case, oracle, ctx):
+    """Minimized energies against the CPU oracle's VA13 (FP32 CPU energies).
+
+    The reference's minimizer is chaotic at the FP32 noise level: moving one
+    start coordinate by one ulp changes the minimized energy by more than 1e-3
+    for about a fifth of these poses on the oracle itself (the floor measured
+    below), and glibc's sinf/cosf differ from correctly rounded values in about
+    1% of calls, so no GPU path can follow the CPU trajectories bit for bit.
+    The GPU must agree with the oracle as well as the oracle agrees with
+    itself under that one-ulp perturbation (5 points of slack), and the oracle
+    re-evaluated at the GPU's minimized states must reproduce the GPU's
+    reported energies and gradients (the energy parity bound, 1e-4 scaled)."""
+    from test_gpu_rigid import pose_errors
     wl, grid = min_case
     ids = upload(ctx, wl.rec, wl.lig, grid, wl.params)
-    _, r_dev, n_dev = ctx.minimize_6d(*ids, wl.dofs, max_evals=100)
+    s_dev, r_dev, n_dev = ctx.minimize_6d(*ids, wl.dofs, max_evals=100)
     _, r_cpu, n_cpu = oracle.minimize_6d(wl.rec, wl.lig, grid, wl.params, wl.dofs, 100)
-    rel = np.abs(r_dev[:, 0].astype(np.float64) - r_cpu[:, 0]) / np.maximum(np.abs(r_cpu[:, 0]), 1e-3)
-    frac = float(np.mean(rel <= 1e-3))
-    print(f"minimized energies within 1e-3: {100 * frac:.1f}% of {len(rel)} poses; "
-          f"identical evaluation counts: {100 * np.mean(n_dev == n_cpu):.1f}%")
-    assert frac >= 0.99
+    d1 = wl.dofs.copy()
+    d1[:, 0] = np.nextafter(d1[:, 0], np.float32(np.inf))
+    _, r_ulp, _ = oracle.minimize_6d(wl.rec, wl.lig, grid, wl.params, d1, 100)
+    frac = minimized_agreement(r_dev, r_cpu)
+    floor = minimized_agreement(r_ulp, r_cpu)
+    print(f"minimized energies within 1e-3 of the oracle: GPU {100 * frac:.1f}%, oracle with a "
+          f"one-ulp start perturbation {100 * floor:.1f}% of {len(r_dev)} poses")
+    assert frac >= floor - 0.05
+    ref, st = oracle.energy_6d(wl.rec, wl.lig, grid, wl.params, s_dev, stats=True)
+    for e in pose_errors(r_dev, ref, st):
+        assert float(e.max()) <= 1e-4
 
 
 def test_batch_equals_single_pairs(pkg, oracle, ctx):

@@ -112,6 +112,11 @@ struct ParamsItem : Item {
 	std::vector<gba_ffparam> host_table;
 };
 
+/* Morton visiting order of n poses computed in the given device memory
+ * (pose_order.cu); throws ApiError if [buf, buf + cap) is too small. */
+const uint32_t* pose_order_in(const void* dofs, size_t stride_floats, size_t n, const DevIntrpl& box,
+		void* buf, size_t cap, cudaStream_t s);
+
 DevIntrpl intrpl_from_desc(const gba_intrpl_desc& d);
 DevNL nl_from_desc(const gba_nl_desc& d);
 std::vector<float> nl_ratio_table(float dPlateau2);

@@ -1,0 +1,95 @@
+/*
+ * noalloc.cu -- gba_energy_6d_noalloc: the fused rigid energy launch of
+ * gba_energy_6d for device-resident poses, with the Morton visiting-order
+ * scratch taken from a fixed, statically allocated device array instead of
+ * the stream-ordered allocator.  The call performs no device or host memory
+ * allocation: no cudaMalloc / cudaMallocAsync / cudaFree, no allocating
+ * library routine; CUB's radix sort runs on caller-supplied temporary storage.
+ *
+ * Scratch: one file-scope __device__ array of kNoAllocScratchBytes per device
+ * (2 MiB), addressed through cudaGetSymbolAddress on the first call made on
+ * each device (with that device current); that first call may load the
+ * module, so make it before any stream capture.  Batches of more than
+ * kNoAllocMaxPoses poses are rejected with GBA_ERR_INVALID_ARGUMENT.  Nothing
+ * in the scratch has to start at zero: the order kernel writes every key and
+ * index it sorts, the sort writes its own temporary state.  The array is
+ * shared by every call on a device: overlapping calls (other streams, threads
+ * or contexts on the same device) race on it and must be serialized by the
+ * caller.
+ */
+#include <algorithm>
+#include <mutex>
+#include <string>
+
+#include "gba_context.h"
+
+namespace gba {
+
+constexpr size_t kNoAllocScratchBytes = (size_t)2 << 20;
+constexpr size_t kNoAllocMaxPoses = 65536;
+
+__device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+namespace {
+
+constexpr int kMaxDevices = 64;
+std::mutex g_scratch_mu;
+void* g_scratch_ptr[kMaxDevices] = {};
+
+/* Device address of this device's scratch array (resolved once per device). */
+void* noalloc_scratch(int device) {
+	if (device < 0 || device >= kMaxDevices)
+		throw ApiError(GBA_ERR_INVALID_ARGUMENT, "gba_energy_6d_noalloc: device ordinal out of range");
+	std::lock_guard<std::mutex> g(g_scratch_mu);
+	if (!g_scratch_ptr[device]) {
+		void* p = nullptr;
+		check_cuda(cudaGetSymbolAddress(&p, g_noalloc_scratch), "gba_energy_6d_noalloc: cudaGetSymbolAddress");
+		g_scratch_ptr[device] = p;
+	}
+	return g_scratch_ptr[device];
+}
+
+}  // namespace
+
+}  // namespace gba
+
+using namespace gba;
+
+extern "C" int gba_energy_6d_noalloc(gba_ctx* ctx, gba_id rec, gba_id lig, gba_id grid, gba_id params,
+		const gba_dof6d* dofs, size_t n, gba_result6d* out, void* stream) {
+	if (!ctx) return GBA_ERR_INVALID_ARGUMENT;
+	try {
+		if (n == 0) return GBA_OK;
+		if (!dofs || !out) throw ApiError(GBA_ERR_INVALID_ARGUMENT, "gba_energy_6d_noalloc: null dofs/out");
+		if (n > kNoAllocMaxPoses)
+			throw ApiError(GBA_ERR_INVALID_ARGUMENT, "gba_energy_6d_noalloc: " + std::to_string(n) +
+					" poses exceed the static scratch limit of " + std::to_string(kNoAllocMaxPoses));
+		ctx->bind();
+		if (!is_device_pointer(dofs) || !is_device_pointer(out))
+			throw ApiError(GBA_ERR_INVALID_ARGUMENT, "gba_energy_6d_noalloc: device pointers required");
+		void* scratch = noalloc_scratch(ctx->device);
+		RigidLaunch L = ctx->rigid_launch(rec, lig, grid, params);
+		cudaStream_t s = (cudaStream_t)stream;
+		L.n = n;
+		L.dofs = dofs;
+		L.out = out;
+		L.census = nullptr;
+		L.order = (ctx->order_enabled && n >= Context::kOrderMinPoses)
+				? pose_order_in(dofs, 6, n, L.m.grid.outer, scratch, kNoAllocScratchBytes, s)
+				: nullptr;
+		/* launch shape as gba_energy_6d chooses it */
+		const TuneParams tp = ctx->tuned("energy", n);
+		const int threads = tp.threads;
+		const int bps = std::min(tp.blocks_per_sm, rigid_blocks_per_sm(threads, false));
+		size_t blocks = std::min<size_t>((n + threads / 32 - 1) / (threads / 32), (size_t)ctx->num_sms * bps);
+		if (blocks == 0) blocks = 1;
+		check_cuda(launch_rigid_energy(L, (int)blocks, threads, s), "gba_energy_6d_noalloc: launch");
+	} catch (const ApiError& e) {
+		ctx->set_error(e.what());
+		return e.code;
+	} catch (const std::exception& e) {
+		ctx->set_error(e.what());
+		return GBA_ERR_INVALID_ARGUMENT;
+	}
+	return GBA_OK;
+}

@@ -110,6 +110,21 @@ const uint32_t* Context::pose_order_persistent(const void* dofs, size_t stride_f
 			});
 }
 
+/* Order computed in caller-provided device memory [buf, buf + cap) (256-byte
+ * aligned carving); ApiError when the keys, indices and sort scratch do not fit. */
+const uint32_t* pose_order_in(const void* dofs, size_t stride_floats, size_t n, const DevIntrpl& box,
+		void* buf, size_t cap, cudaStream_t s) {
+	size_t used = 0;
+	return sort_order(dofs, stride_floats, n, box, nullptr, nullptr, 1, s, [&](int, size_t bytes) {
+		const size_t at = (used + 255) & ~(size_t)255;
+		if (at + bytes > cap)
+			throw ApiError(GBA_ERR_INVALID_ARGUMENT, "visiting order: " + std::to_string(at + bytes) +
+					" bytes of scratch needed, " + std::to_string(cap) + " available");
+		used = at + bytes;
+		return (void*)((char*)buf + at);
+	});
+}
+
 void* StreamScratch::get(size_t bytes, cudaStream_t s) {
 	void* p = nullptr;
 	check_cuda(cudaMallocAsync(&p, bytes ? bytes : 16, s), "cudaMallocAsync");

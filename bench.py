@@ -107,6 +107,20 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+def traffic_per_pose(variant: str):
+    """DRAM bytes per pose of the energy kernel, from the committed ncu summary
+    of the same kernel and variant (a line 'traffic-per-pose: <variant> <bytes>'
+    under profiles/), or None.  The capture is of a smaller pose count; the
+    traffic is scaled by the poses processed."""
+    import re
+    for f in sorted((ROOT / "profiles").glob("*.md")):
+        for line in f.read_text().splitlines():
+            m = re.match(r"traffic-per-pose: (\S+) ([0-9.]+)", line.strip("` "))
+            if m and m.group(1) == variant:
+                return float(m.group(2)), f.name
+    return None, None
+
+
 def measured_peaks():
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -115,10 +129,16 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def make_workload(n_poses: int | None):
+def make_workload(n_poses: int | None, rec_beads: int | None = None):
+    """Config 1 (or, for small profiling captures, config 1's distributions with
+    a smaller receptor)."""
     import __graft_entry__
     pkg = __graft_entry__.load_package()
-    wl = pkg.synth.make_config(1, n_poses=n_poses)
+    if rec_beads:
+        c = pkg.synth.CONFIGS[1]
+        wl = pkg.synth.make_pair(1, rec_beads, c["lig"], n_poses or c["poses"], c["shell"])
+    else:
+        wl = pkg.synth.make_config(1, n_poses=n_poses)
     return pkg, wl
 
 
@@ -144,7 +164,7 @@ def run_reference(args):
     import __graft_entry__
     subprocess.run(["make", "-s", "-C", str(ROOT / "oracle")], check=True)
     from oracle import pyoracle as po
-    pkg, wl = make_workload(args.poses)
+    pkg, wl = make_workload(args.poses, args.rec_beads)
     nthreads = os.cpu_count() or 1
     grid = po.build_grid(wl.rec, wl.params, pkg.GridOptions(), nthreads=nthreads)
     kind = "reference" if po.ref_available() else "port"
@@ -366,6 +386,11 @@ def main():
     ap.add_argument("--variant", default="order=1,octets=1",
                     help="layout / visiting-order variant timed, or 'search' to time all four "
                          "and keep the fastest")
+    ap.add_argument("--rec-beads", type=int, default=None,
+                    help="smaller receptor with config 1's distributions (profiling captures)")
+    ap.add_argument("--kopts", type=int, default=7,
+                    help="kernel options (GBA_KOPT_*: 1 computed ratio, 2 cooperative lookup, "
+                         "4 four blocks per SM)")
     ap.add_argument("--batch-scale", type=float, default=0.05,
                     help="fraction of config 4's pose counts used by --suite full")
     args = ap.parse_args()
@@ -381,9 +406,10 @@ def main():
         dist.init_process_group("nccl")
     torch.cuda.set_device(local)
     import __graft_entry__
-    pkg, wl = make_workload(args.poses)
+    pkg, wl = make_workload(args.poses, args.rec_beads)
     from gbattract.context import GbaContext
     ctx = GbaContext(local)
+    ctx.set_kernel_options(args.kopts)
     rec, lig, par = ctx.upload_protein(wl.rec), ctx.upload_protein(wl.lig), ctx.upload_params(wl.params)
     t0 = time.perf_counter()
     grid = ctx.build_grid(rec, par, pkg.GridOptions())
@@ -474,6 +500,8 @@ def main():
     kavg = ktot / args.steps
     kernel_avg_s = kernel_ms / 1000.0 / max(1, kernel_launches)
     achieved = bytes_launch / kernel_avg_s / 1e9
+    tpp, traffic_src = traffic_per_pose(f"{best},kopts={args.kopts}")
+    traffic = None if tpp is None else tpp * n
     peak, peak_kind = measured_peaks()
 
     # end to end through the C ABI with pinned host buffers
@@ -516,13 +544,16 @@ def main():
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1000.0 * kavg, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
-            "config": {"workload": WORKLOAD, "poses": n, "receptor_beads": wl.rec.n,
+            "config": {"workload": WORKLOAD if not args.rec_beads else
+                       f"config 1 distributions, receptor {wl.rec.n} / ligand {wl.lig.n} beads, {n} poses",
+                       "poses": n, "receptor_beads": wl.rec.n,
                        "ligand_beads": wl.lig.n, "l2": "flushed (256 MB write) between steps",
                        "grid_MB": None},
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(24 * n),
                     "d2h_bytes_per_step": int(28 * n)},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": None, "peak_source": peak_kind,
+                         "frac": achieved / peak, "traffic": traffic, "traffic_source": traffic_src,
+                         "peak_source": peak_kind,
                          "bytes_per_launch": bytes_launch, "kernel_ms_avg": 1000.0 * kernel_avg_s,
                          "kernel_launches_timed": kernel_launches},
             "cpu_baseline": cpu, "clocks": clk.summary(),
@@ -530,7 +561,7 @@ def main():
             # order is on; the CUB radix-sort passes it feeds are library kernels)
             "gpu_launches": args.steps * (2 if best.startswith("order=1") else 1),
             "minimization": minim,
-            "variants_ms": variants, "variant_timed": best,
+            "variants_ms": variants, "variant_timed": best, "kernel_options": args.kopts,
             "suite": suite or None,
             "wall_s_timed": wall, "host_device_paths_equal": ok,
             "census": {"grid_lookups_per_pose": float(cen[:, 0].mean()),

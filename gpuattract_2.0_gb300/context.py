@@ -294,6 +294,10 @@ class GbaContext:
         """Visit large batches in Morton order of the pose translation (default on)."""
         self._check(self.lib.gba_set_pose_order(self.h, int(bool(enable))))
 
+    def set_kernel_options(self, flags: int):
+        """GBA_KOPT_* flags: 1 = computed plateau ratio, 2 = 8 lanes per grid lookup."""
+        self._check(self.lib.gba_set_kernel_options(self.h, int(flags)))
+
     def kernel_timing(self, enable: bool):
         """Record CUDA events around every fused rigid energy kernel launch."""
         self._check(self.lib.gba_kernel_timing(self.h, int(bool(enable))))

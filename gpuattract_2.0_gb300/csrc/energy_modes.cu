@@ -54,7 +54,8 @@ __device__ __forceinline__ void project(const float* __restrict__ v, uint32_t M,
 #pragma unroll
 	for (int m = 0; m < GBA_MODES_MAX; ++m)
 		if (m < (int)M)
-			acc[m] += sign * (fx * __ldg(v + 3 * m) + fy * __ldg(v + 3 * m + 1) + fz * __ldg(v + 3 * m + 2));
+			acc[m] = ffma(sign, ffma(fz, __ldg(v + 3 * m + 2), ffma(fy, __ldg(v + 3 * m + 1),
+					fmul(fx, __ldg(v + 3 * m)))), acc[m]);
 }
 
 }  // namespace
@@ -135,9 +136,8 @@ __device__ __forceinline__ float eval_pose_modes(const ModesLaunch& L, const flo
 			const uint32_t e = W.look[q];
 			const float4 v = grid_lookup(L.grid_lig, W, e);
 			/* back into the receptor frame, then -(force . mode) */
-			const float fx = R.m[0] * v.x + R.m[1] * v.y + R.m[2] * v.z;
-			const float fy = R.m[3] * v.x + R.m[4] * v.y + R.m[5] * v.z;
-			const float fz = R.m[6] * v.x + R.m[7] * v.y + R.m[8] * v.z;
+			float fx, fy, fz;
+			rot_apply(R.m, v.x, v.y, v.z, fx, fy, fz);
 			project(L.rec_modes + (size_t)W.type[e >> 1] * L.rec_ms, Mr, fx, fy, fz, -1.f, gR);
 		}
 		__syncwarp();
@@ -189,9 +189,8 @@ __device__ __forceinline__ float eval_pose_modes(const ModesLaunch& L, const flo
 			const uint32_t s = e >> 1;
 			const float4 v = grid_lookup(L.grid_rec, W, e);
 			S.add(v.w, v.x, v.y, v.z, W.ux[s], W.uy[s], W.uz[s]);
-			const float rx = R.m[0] * v.x + R.m[3] * v.y + R.m[6] * v.z;
-			const float ry = R.m[1] * v.x + R.m[4] * v.y + R.m[7] * v.z;
-			const float rz = R.m[2] * v.x + R.m[5] * v.y + R.m[8] * v.z;
+			float rx, ry, rz;
+			rot_apply_t(R.m, v.x, v.y, v.z, rx, ry, rz);
 			project(L.lig_modes + (size_t)(i0 + s) * L.lig_ms, Ml, rx, ry, rz, -1.f, gL);
 		}
 		for (uint32_t q = lane; q < n_pair; q += 32) {
@@ -209,9 +208,8 @@ __device__ __forceinline__ float eval_pose_modes(const ModesLaunch& L, const flo
 			S.add(e, fx, fy, fz, W.ux[s], W.uy[s], W.uz[s]);
 			/* reaction on receptor bead j is -f: its mode gradient gets -(-f . v) */
 			project(vr, Mr, fx, fy, fz, 1.f, gR);
-			const float lx = R.m[0] * fx + R.m[3] * fy + R.m[6] * fz;
-			const float ly = R.m[1] * fx + R.m[4] * fy + R.m[7] * fz;
-			const float lz = R.m[2] * fx + R.m[5] * fy + R.m[8] * fz;
+			float lx, ly, lz;
+			rot_apply_t(R.m, fx, fy, fz, lx, ly, lz);
 			project(L.lig_modes + (size_t)(i0 + s) * L.lig_ms, Ml, lx, ly, lz, -1.f, gL);
 		}
 		__syncwarp();
@@ -234,11 +232,13 @@ __device__ __forceinline__ float eval_pose_modes(const ModesLaunch& L, const flo
 	for (int m = 0; m < GBA_MODES_MAX; ++m) {
 		if (m < (int)Mr) {
 			const double dl = gR[m];
-			gR[m] = gR[m] + (float)((double)(4.0f * L.rec.mode_force[m]) * (dl * dl) * (dl * dl));
+			gR[m] = fadd(gR[m], (float)__dmul_rn(__dmul_rn((double)fmul(4.0f, L.rec.mode_force[m]),
+					__dmul_rn(dl, dl)), __dmul_rn(dl, dl)));
 		}
 		if (m < (int)Ml) {
 			const double dl = gL[m];
-			gL[m] = gL[m] + (float)((double)(4.0f * L.lig.mode_force[m]) * (dl * dl) * (dl * dl));
+			gL[m] = fadd(gL[m], (float)__dmul_rn(__dmul_rn((double)fmul(4.0f, L.lig.mode_force[m]),
+					__dmul_rn(dl, dl)), __dmul_rn(dl, dl)));
 		}
 	}
 	/* Result_6D_Modes: E, pos xyz, ang xyz, modesRec[10], modesLig[10] */

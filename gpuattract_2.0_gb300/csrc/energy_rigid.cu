@@ -16,8 +16,10 @@
 
 namespace gba {
 
-template <bool CENSUS>
-__global__ void __launch_bounds__(256) rigid_energy_kernel(const RigidLaunch L) {
+/* BOUND4: registers capped for four resident 256-thread blocks per SM
+ * (GBA_KOPT_FOUR_BLOCKS). */
+template <bool CENSUS, bool BOUND4>
+__global__ void __launch_bounds__(256, BOUND4 ? 4 : 1) rigid_energy_kernel(const RigidLaunch L) {
 	__shared__ WarpStage stage[8];   /* one per warp of a <=256-thread block */
 	const int lane = threadIdx.x & 31;
 	const size_t warp = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -65,18 +67,22 @@ cudaError_t launch_batch_energy(const BatchEnergyLaunch& L, int blocks, int thre
 
 cudaError_t launch_rigid_energy(const RigidLaunch& L, int blocks, int threads, cudaStream_t s) {
 	if (L.census)
-		rigid_energy_kernel<true><<<blocks, threads, 0, s>>>(L);
+		rigid_energy_kernel<true, false><<<blocks, threads, 0, s>>>(L);
+	else if (L.bound4)
+		rigid_energy_kernel<false, true><<<blocks, threads, 0, s>>>(L);
 	else
-		rigid_energy_kernel<false><<<blocks, threads, 0, s>>>(L);
+		rigid_energy_kernel<false, false><<<blocks, threads, 0, s>>>(L);
 	return cudaGetLastError();
 }
 
-int rigid_blocks_per_sm(int threads, bool census) {
+int rigid_blocks_per_sm(int threads, bool census, bool bound4) {
 	int nb = 0;
 	if (census)
-		cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, rigid_energy_kernel<true>, threads, 0);
+		cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, rigid_energy_kernel<true, false>, threads, 0);
+	else if (bound4)
+		cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, rigid_energy_kernel<false, true>, threads, 0);
 	else
-		cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, rigid_energy_kernel<false>, threads, 0);
+		cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, rigid_energy_kernel<false, false>, threads, 0);
 	return nb > 0 ? nb : 1;
 }
 

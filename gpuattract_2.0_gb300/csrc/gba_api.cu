@@ -154,6 +154,7 @@ DevNL nl_from_desc(const gba_nl_desc& d) {
 	g.dVox_inv = 1 / dVox;
 	for (int a = 0; a < 3; ++a) g.maxDim[a] = g.pos[a] + (float)(g.dimN[a] - 1) * dVox;
 	g.ratio_size = (uint32_t)int(10000 * g.dPlateau2) + 1;
+	g.ratio_scale = (float)(1.0 / 10000.0 / (double)g.dPlateau2);
 	return g;
 }
 
@@ -406,6 +407,20 @@ int gba_kernel_time(gba_ctx* ctx, double* ms_total, uint64_t* launches, int32_t 
 	GBA_API_END(ctx)
 }
 
+int gba_set_kernel_options(gba_ctx* ctx, uint32_t flags) {
+	if (!ctx) return GBA_ERR_INVALID_ARGUMENT;
+	GBA_API_BEGIN
+	if (flags & ~(uint32_t)(GBA_KOPT_RATIO_COMPUTED | GBA_KOPT_COOP_LOOKUP | GBA_KOPT_FOUR_BLOCKS))
+		throw ApiError(GBA_ERR_INVALID_ARGUMENT, "gba_set_kernel_options: unknown flag");
+	ctx->bind();
+	Lock g(ctx->stage_mu);
+	ctx->kernel_opts = flags;
+	/* cached device models and minimizer graphs hold the old options */
+	ctx->model_cache.clear();
+	ctx->clear_graphs();
+	GBA_API_END(ctx)
+}
+
 int gba_set_pose_order(gba_ctx* ctx, int enable) {
 	if (!ctx) return GBA_ERR_INVALID_ARGUMENT;
 	ctx->order_enabled = enable != 0;
@@ -521,9 +536,16 @@ RigidLaunch Context::rigid_launch(gba_id rec, gba_id lig, gba_id grid, gba_id pa
 	RigidLaunch L{};
 	L.m.rec = R->dev;
 	L.m.lig = Lg->dev;
-	L.m.grid = G->dev;
+	L.m.grid = apply_kernel_options(G->dev);
 	L.m.par = P->dev;
+	L.bound4 = (kernel_opts & GBA_KOPT_FOUR_BLOCKS) ? 1 : 0;
 	return L;
+}
+
+DevGrid Context::apply_kernel_options(DevGrid g) const {
+	g.nl.ratio_computed = (kernel_opts & GBA_KOPT_RATIO_COMPUTED) ? 1 : 0;
+	g.coop_lookup = ((kernel_opts & GBA_KOPT_COOP_LOOKUP) && g.inner.oct && g.outer.oct) ? 1 : 0;
+	return g;
 }
 
 /* The index checks that keep every device access in bounds (the reference
@@ -556,8 +578,8 @@ ModesLaunch Context::modes_launch(gba_id rec, gba_id lig, gba_id grid_rec, gba_i
 	ModesLaunch L{};
 	L.rec = R->dev;
 	L.lig = Lg->dev;
-	L.grid_rec = GR->dev;
-	L.grid_lig = GL->dev;
+	L.grid_rec = apply_kernel_options(GR->dev);
+	L.grid_lig = apply_kernel_options(GL->dev);
 	L.par = P->dev;
 	L.rec_modes = R->dev.modes;
 	L.rec_ms = 3 * R->dev.n_modes;
@@ -580,7 +602,7 @@ void Context::run_rigid(RigidLaunch& L, cudaStream_t s) {
 	const TuneParams tp = tuned("energy", L.n);
 	const int threads = tp.threads;
 	const int warps_per_block = threads / 32;
-	const int bps = std::min(tp.blocks_per_sm, rigid_blocks_per_sm(threads, L.census != nullptr));
+	const int bps = std::min(tp.blocks_per_sm, rigid_blocks_per_sm(threads, L.census != nullptr, L.bound4 && !L.census));
 	size_t want = (L.n + warps_per_block - 1) / warps_per_block;
 	size_t blocks = std::min<size_t>(want, (size_t)num_sms * bps);
 	if (blocks == 0) blocks = 1;

@@ -194,6 +194,10 @@ struct Context {
 	ModesLaunch modes_launch(gba_id rec, gba_id lig, gba_id grid_rec, gba_id grid_lig, gba_id params);
 	void run_modes(ModesLaunch& L, cudaStream_t s);
 
+	/* GBA_KOPT_* flags (gba_set_kernel_options) and their effect on a grid */
+	uint32_t kernel_opts = GBA_KOPT_DEFAULT;
+	DevGrid apply_kernel_options(DevGrid g) const;
+
 	/* CUDA-event timing of the fused rigid energy kernel (gba_kernel_timing) */
 	static constexpr size_t kTimingPool = 1024;
 	bool timing = false;

@@ -55,11 +55,18 @@ struct DevNL {
 	const uint2* grid;        /* Nx*Ny*Nz {numEl, idx} */
 	const uint32_t* list;
 	const float* ratio;
+	/* ratio_computed: the plateau ratio of table bin n is evaluated as
+	 * sqrt((n + 0.5) * ratio_scale), ratio_scale = 1e-4 / plateau^2 (within
+	 * one ulp of the table entry), instead of being read from ratio[] */
+	float ratio_scale;
+	int ratio_computed;
 };
 
 struct DevGrid {
 	DevIntrpl inner, outer;
 	DevNL nl;
+	/* 8 lanes per grid lookup, one octet corner each (needs both octet copies) */
+	int coop_lookup;
 };
 
 struct DevParams {
@@ -93,6 +100,7 @@ struct RigidLaunch {
 	PoseCensus* census;       /* nullptr: no census */
 	const uint32_t* order;    /* visiting order (nullptr: submission order) */
 	size_t n;
+	int bound4;               /* launch the four-blocks-per-SM instantiation */
 };
 
 cudaError_t launch_rigid_energy(const RigidLaunch& L, int blocks, int threads, cudaStream_t s);
@@ -170,7 +178,7 @@ cudaError_t launch_minimize_modes(const ModesMinLaunch& M, int blocks, int threa
 int minimize_modes_blocks_per_sm(int threads);
 
 /* Number of resident blocks per SM of the rigid kernel for `threads`. */
-int rigid_blocks_per_sm(int threads, bool census);
+int rigid_blocks_per_sm(int threads, bool census, bool bound4 = false);
 
 }  // namespace gba
 

@@ -153,6 +153,27 @@ int gba_release(gba_ctx* ctx, gba_id id);
  * off.  No reference counterpart (a scheduling choice of this library). */
 int gba_set_pose_order(gba_ctx* ctx, int enable);
 
+/* Kernel implementation options (no reference counterpart; every option
+ * keeps results within the parity bounds and grid indices / neighbour walks
+ * bit-exact):
+ *   GBA_KOPT_RATIO_COMPUTED  the plateau ratio of table bin n = int(r^2 * 1e4)
+ *                            (src/model/NLGrid.tpp:45-50) is evaluated as
+ *                            sqrt((n + 0.5) * 1e-4 / plateau^2) in FP32 --
+ *                            within one ulp of the table entry -- instead of
+ *                            being gathered from the 4 MB table;
+ *   GBA_KOPT_COOP_LOOKUP     on grids with the octet layout (gba_grid_octets),
+ *                            8 lanes share one grid lookup, one corner each,
+ *                            loaded without L1 allocation;
+ *   GBA_KOPT_FOUR_BLOCKS     the scoring kernel is compiled for four resident
+ *                            256-thread blocks per SM (64 registers a thread).
+ * The default is all three.  Changing options drops the cached minimizer
+ * graphs. */
+#define GBA_KOPT_RATIO_COMPUTED 1u
+#define GBA_KOPT_COOP_LOOKUP    2u
+#define GBA_KOPT_FOUR_BLOCKS    4u
+#define GBA_KOPT_DEFAULT        (GBA_KOPT_RATIO_COMPUTED | GBA_KOPT_COOP_LOOKUP | GBA_KOPT_FOUR_BLOCKS)
+int gba_set_kernel_options(gba_ctx* ctx, uint32_t flags);
+
 /* While enabled, CUDA events are recorded on the launching stream around
  * every fused rigid energy kernel launch (gba_energy_6d and friends);
  * gba_kernel_time synchronizes on them and returns the summed kernel time

@@ -116,14 +116,24 @@ def test_pose_order_does_not_change_results(small_case, ctx):
 
 
 def test_octet_layout_does_not_change_results(small_case, ctx):
+    """The duplicated-octet layout reads the same corners: with one lane per
+    lookup the results are bit-identical to the native layout.  (The 8-lane
+    cooperative lookup, default on octet grids, sums the same per-lookup
+    values on other lanes; it is held to the parity bound in
+    test_kernel_options_keep_parity.)"""
     wl, grid = small_case
     ids = upload(ctx, wl.rec, wl.lig, grid, wl.params)
-    native = ctx.energy_6d(*ids, wl.dofs)
-    ctx.grid_octets(ids[2], True)
-    octets = ctx.energy_6d(*ids, wl.dofs)
-    s1, r1, n1 = ctx.minimize_6d(*ids, wl.dofs[:32], max_evals=30)
-    ctx.grid_octets(ids[2], False)
-    s2, r2, n2 = ctx.minimize_6d(*ids, wl.dofs[:32], max_evals=30)
+    try:
+        ctx.set_kernel_options(1 | 4)       # computed ratio, four blocks; no cooperative lookup
+        native = ctx.energy_6d(*ids, wl.dofs)
+        ctx.grid_octets(ids[2], True)
+        octets = ctx.energy_6d(*ids, wl.dofs)
+        s1, r1, n1 = ctx.minimize_6d(*ids, wl.dofs[:32], max_evals=30)
+        ctx.grid_octets(ids[2], False)
+        s2, r2, n2 = ctx.minimize_6d(*ids, wl.dofs[:32], max_evals=30)
+    finally:
+        ctx.set_kernel_options(7)
+        ctx.grid_octets(ids[2], False)
     assert np.array_equal(native, octets)
     assert np.array_equal(r1, r2) and np.array_equal(s1, s2)
 
@@ -160,3 +170,26 @@ def test_fp64_error_statement(small_case, oracle, ctx):
     print(f"FP32 GPU vs FP64 oracle: E max {eE.max():.2e} median {np.median(eE):.2e}; "
           f"F max {eF.max():.2e}; torque max {eT.max():.2e}")
     assert float(eE.max()) < 1e-3
+
+
+@pytest.mark.parametrize("flags", [0, 1, 2, 4, 7])
+def test_kernel_options_keep_parity(small_case, oracle, ctx, flags):
+    """Each GBA_KOPT_* combination stays within the parity bound; grid and NL
+    decisions are unaffected (census identical)."""
+    wl, grid = small_case
+    ids = upload(ctx, wl.rec, wl.lig, grid, wl.params)
+    ref, st = oracle.energy_6d(wl.rec, wl.lig, grid, wl.params, wl.dofs, stats=True)
+    cen0, _ = ctx.census_6d(*ids, wl.dofs)
+    try:
+        ctx.grid_octets(ids[2], bool(flags & 2))
+        ctx.set_kernel_options(flags)
+        got = ctx.energy_6d(*ids, wl.dofs)
+        cen, _ = ctx.census_6d(*ids, wl.dofs)
+        s, r, n = ctx.minimize_6d(*ids, wl.dofs[:16], max_evals=20)
+        assert np.array_equal(ctx.energy_6d(*ids, s), r)
+    finally:
+        ctx.set_kernel_options(7)        # GBA_KOPT_DEFAULT
+        ctx.grid_octets(ids[2], False)
+    for e in pose_errors(got, ref, st):
+        assert float(e.max()) <= RTOL
+    assert np.array_equal(cen, cen0)

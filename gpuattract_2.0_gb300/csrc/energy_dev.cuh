@@ -26,6 +26,19 @@ __device__ __forceinline__ float fadd(float a, float b) { return __fadd_rn(a, b)
 __device__ __forceinline__ float fsub(float a, float b) { return __fsub_rn(a, b); }
 __device__ __forceinline__ float ffma(float a, float b, float c) { return __fmaf_rn(a, b, c); }
 
+/* Hardware reciprocal and square root (rcp/sqrt.approx: within about one
+ * ulp; deterministic, the same bits in every kernel). */
+__device__ __forceinline__ float frcp_approx(float x) {
+	float r;
+	asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+	return r;
+}
+__device__ __forceinline__ float fsqrt_approx(float x) {
+	float r;
+	asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+	return r;
+}
+
 /* Rotation matrix and its sin/cos, one pose. */
 struct PoseRot {
 	float m[9];
@@ -120,24 +133,16 @@ __device__ __forceinline__ float octet_sum(const float p[8]) {
 	return fadd(fadd(fadd(p[0], p[1]), fadd(p[2], p[3])), fadd(fadd(p[4], p[5]), fadd(p[6], p[7])));
 }
 
-/* One channel's trilinear interpolation at a voxel octet (unscaled). */
-__device__ __forceinline__ float4 octet_lerp(const float4* __restrict__ base, uint32_t sx,
-		uint32_t sxy, float pmn_x, float pmn_y, float pmn_z, float pmx_x, float pmx_y,
-		float pmx_z) {
-	float4 d[8];
-	d[0] = __ldg(base);
-	d[1] = __ldg(base + 1);
-	d[2] = __ldg(base + sx);
-	d[3] = __ldg(base + sx + 1);
-	d[4] = __ldg(base + sxy);
-	d[5] = __ldg(base + sxy + 1);
-	d[6] = __ldg(base + sxy + sx);
-	d[7] = __ldg(base + sxy + sx + 1);
+/* One channel's trilinear interpolation at a voxel octet (unscaled), with
+ * the eight corner weights given: corner c at base + (c & 1) + sx * ((c >> 1)
+ * & 1) + sxy * (c >> 2). */
+__device__ __forceinline__ float4 octet_lerp_w(const float4* __restrict__ base, uint32_t sx, uint32_t sxy,
+		const float w[8]) {
 	float px[8], py[8], pz[8], pw[8];
 #pragma unroll
 	for (int c = 0; c < 8; ++c) {
-		const float w = corner_weight(c, pmn_x, pmn_y, pmn_z, pmx_x, pmx_y, pmx_z);
-		px[c] = fmul(d[c].x, w); py[c] = fmul(d[c].y, w); pz[c] = fmul(d[c].z, w); pw[c] = fmul(d[c].w, w);
+		const float4 d = __ldg(base + (c & 1) + sx * ((c >> 1) & 1) + sxy * (c >> 2));
+		px[c] = fmul(d.x, w[c]); py[c] = fmul(d.y, w[c]); pz[c] = fmul(d.z, w[c]); pw[c] = fmul(d.w, w[c]);
 	}
 	return make_float4(octet_sum(px), octet_sum(py), octet_sum(pz), octet_sum(pw));
 }

@@ -126,19 +126,15 @@ __device__ __forceinline__ float eval_pose_modes(const ModesLaunch& L, const flo
 				nlk[h] = stage_grid(L.grid_lig, px, py, pz, mapped, r.w, s, W);
 			}
 		}
-		const uint32_t incl = warp_incl_scan(nlk[0] + nlk[1], lane);
-		const uint32_t n_look = __shfl_sync(GBA_FULL_MASK, incl, 31);
-		uint32_t k = incl - nlk[0] - nlk[1];
-		enqueue_lookups(W, k, lane, nlk[0]);
-		enqueue_lookups(W, k, lane + 32, nlk[1]);
+		const uint32_t n_look = queue_lookups(W, nlk, lane);
 		__syncwarp();
 		for (uint32_t q = lane; q < n_look; q += 32) {
-			const uint32_t e = W.look[q];
-			const float4 v = grid_lookup(L.grid_lig, W, e);
+			const uint32_t s = lookup_slot(W, q);
+			const float4 v = grid_lookup(L.grid_lig, W, q);
 			/* back into the receptor frame, then -(force . mode) */
 			float fx, fy, fz;
 			rot_apply(R.m, v.x, v.y, v.z, fx, fy, fz);
-			project(L.rec_modes + (size_t)W.type[e >> 1] * L.rec_ms, Mr, fx, fy, fz, -1.f, gR);
+			project(L.rec_modes + (size_t)W.type[s] * L.rec_ms, Mr, fx, fy, fz, -1.f, gR);
 		}
 		__syncwarp();
 	}
@@ -171,23 +167,12 @@ __device__ __forceinline__ float eval_pose_modes(const ModesLaunch& L, const flo
 				if (type != 0) nln[h] = stage_nl(L.grid_rec.nl, px, py, pz, s, W, in_nl);
 			}
 		}
-		const uint32_t lk_incl = warp_incl_scan(nlk[0] + nlk[1], lane);
-		const uint32_t n_look = __shfl_sync(GBA_FULL_MASK, lk_incl, 31);
-		uint32_t k = lk_incl - nlk[0] - nlk[1];
-		enqueue_lookups(W, k, lane, nlk[0]);
-		enqueue_lookups(W, k, lane + 32, nlk[1]);
-		const uint32_t a_incl = warp_incl_scan(nln[0], lane);
-		const uint32_t a_tot = __shfl_sync(GBA_FULL_MASK, a_incl, 31);
-		const uint32_t b_incl = warp_incl_scan(nln[1], lane);
-		W.nl_pre[lane] = a_incl - nln[0];
-		W.nl_pre[lane + 32] = a_tot + b_incl - nln[1];
-		const uint32_t n_pair = a_tot + __shfl_sync(GBA_FULL_MASK, b_incl, 31);
-		if (lane == 0) W.nl_pre[kBeadsPerRound] = n_pair;
+		const uint32_t n_look = queue_lookups(W, nlk, lane);
+		const uint32_t n_pair = queue_pairs(W, nln, lane);
 		__syncwarp();
 		for (uint32_t q = lane; q < n_look; q += 32) {
-			const uint32_t e = W.look[q];
-			const uint32_t s = e >> 1;
-			const float4 v = grid_lookup(L.grid_rec, W, e);
+			const uint32_t s = lookup_slot(W, q);
+			const float4 v = grid_lookup(L.grid_rec, W, q);
 			S.add(v.w, v.x, v.y, v.z, W.ux[s], W.uy[s], W.uz[s]);
 			float rx, ry, rz;
 			rot_apply_t(R.m, v.x, v.y, v.z, rx, ry, rz);

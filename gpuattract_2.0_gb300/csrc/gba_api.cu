@@ -155,6 +155,7 @@ DevNL nl_from_desc(const gba_nl_desc& d) {
 	for (int a = 0; a < 3; ++a) g.maxDim[a] = g.pos[a] + (float)(g.dimN[a] - 1) * dVox;
 	g.ratio_size = (uint32_t)int(10000 * g.dPlateau2) + 1;
 	g.ratio_scale = (float)(1.0 / 10000.0 / (double)g.dPlateau2);
+	g.approx_inv = g.dPlateau2 < 2500.0f ? 1 : 0;
 	return g;
 }
 
@@ -372,6 +373,47 @@ int gba_upload_params(gba_ctx* ctx, uint32_t num_types, const gba_ffparam* table
 	GBA_API_END(ctx)
 }
 
+/* The pair-term table for a grid of plateau^2 dPlateau2: per type pair the
+ * parameters and LJPotForce (src/model/forcefield.h:30-83) evaluated at the
+ * plateau distance -- the force factor and energy the NL term subtracts
+ * (src/model/neighborlist.h:122-130) -- in the rounding of the device's
+ * lj_pot_force (unfused FP32, one fused multiply-add), so folding them in
+ * changes no bit of the result. */
+const float4* ParamsItem::pair_table(float dPlateau2) {
+	uint32_t key;
+	std::memcpy(&key, &dPlateau2, 4);
+	auto it = pair_tables.find(key);
+	if (it != pair_tables.end()) return (const float4*)it->second->ptr;
+	const size_t T2 = host_table.size();
+	std::vector<float4> t(2 * T2);
+	const float p2inv = 1.0f / dPlateau2;
+	const bool shape86 = dev.potshape == GBA_POTSHAPE_8_6;
+	for (size_t k = 0; k < T2; ++k) {
+		const gba_ffparam& p = host_table[k];
+		const float ivor = (float)p.ipon;
+		const float rr23 = (p2inv * p2inv) * p2inv;
+		const float rrd = shape86 ? p2inv : rr23;
+		const float sd = shape86 ? 2.0f : 6.0f;
+		const float rep = p.rc * rrd;
+		const float vlj = (rep - p.ac) * rr23;
+		float fb = std::fmaf(6.0f, vlj, sd * (rep * rr23));
+		float e;
+		if (dPlateau2 < p.rmin2) {
+			e = std::fmaf(ivor - 1.0f, p.emin, vlj);
+		} else {
+			e = ivor * vlj;
+			fb = ivor * fb;
+		}
+		t[2 * k] = make_float4(p.rc, p.ac, p.rmin2, p.emin);
+		t[2 * k + 1] = make_float4(ivor, fb, e, 0.0f);
+	}
+	auto buf = std::make_unique<DevBuffer>();
+	buf->upload(t.data(), t.size() * sizeof(float4));
+	const float4* ptr = (const float4*)buf->ptr;
+	pair_tables.emplace(key, std::move(buf));
+	return ptr;
+}
+
 /* Adds the elapsed time of every recorded event pair to the running total. */
 void Context::timing_fold() {
 	for (size_t k = 0; k < timing_used; ++k) {
@@ -538,6 +580,7 @@ RigidLaunch Context::rigid_launch(gba_id rec, gba_id lig, gba_id grid, gba_id pa
 	L.m.lig = Lg->dev;
 	L.m.grid = apply_kernel_options(G->dev);
 	L.m.par = P->dev;
+	L.m.par.pair = P->pair_table(G->dev.nl.dPlateau2);
 	L.bound4 = (kernel_opts & GBA_KOPT_FOUR_BLOCKS) ? 1 : 0;
 	return L;
 }
@@ -581,6 +624,7 @@ ModesLaunch Context::modes_launch(gba_id rec, gba_id lig, gba_id grid_rec, gba_i
 	L.grid_rec = apply_kernel_options(GR->dev);
 	L.grid_lig = apply_kernel_options(GL->dev);
 	L.par = P->dev;
+	L.par.pair = P->pair_table(GR->dev.nl.dPlateau2);
 	L.rec_modes = R->dev.modes;
 	L.rec_ms = 3 * R->dev.n_modes;
 	L.lig_modes = Lg->dev.modes;

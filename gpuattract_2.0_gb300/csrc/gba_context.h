@@ -110,6 +110,10 @@ struct ParamsItem : Item {
 	DevBuffer lj, ivor;
 	DevParams dev{};
 	std::vector<gba_ffparam> host_table;
+	/* per plateau^2 (bit pattern): the pair-term table with the plateau
+	 * terms folded in (plateau_table) */
+	std::map<uint32_t, std::unique_ptr<DevBuffer>> pair_tables;
+	const float4* pair_table(float dPlateau2);
 };
 
 /* Morton visiting order of n poses computed in the given device memory

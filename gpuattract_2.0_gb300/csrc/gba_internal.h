@@ -60,6 +60,8 @@ struct DevNL {
 	 * one ulp of the table entry), instead of being read from ratio[] */
 	float ratio_scale;
 	int ratio_computed;
+	/* plateau below 50 A: the pair term may use the hardware reciprocal */
+	int approx_inv;
 };
 
 struct DevGrid {
@@ -76,6 +78,10 @@ struct DevParams {
 	float ffelec;
 	const float4* lj;         /* T*T {rc, ac, rmin2, emin} */
 	const float* ivor;        /* T*T ipon as float */
+	/* T*T pairs of float4 {rc, ac, rmin2, emin}, {ipon, fb_p, e_p, 0}: fb_p and
+	 * e_p are LJPotForce's force factor and energy at the plateau distance of
+	 * the grid in use, per type pair (set per launch) */
+	const float4* pair;
 };
 
 /* Per-pose census used for the roofline byte count (same meaning as the

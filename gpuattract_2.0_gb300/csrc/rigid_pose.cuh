@@ -40,14 +40,14 @@ struct WarpStage {
 	float ux[kBeadsPerRound], uy[kBeadsPerRound], uz[kBeadsPerRound];   /* unrotated (torque) */
 	float px[kBeadsPerRound], py[kBeadsPerRound], pz[kBeadsPerRound];   /* transformed */
 	float q[kBeadsPerRound];
-	float wnx[kBeadsPerRound], wny[kBeadsPerRound], wnz[kBeadsPerRound]; /* pos - voxel min */
-	float wxx[kBeadsPerRound], wxy[kBeadsPerRound], wxz[kBeadsPerRound]; /* voxel max - pos */
-	uint32_t off[kBeadsPerRound];      /* octet offset inside a channel */
-	uint32_t chan[kBeadsPerRound];     /* mapped channel | outer grid flag << 31 */
+	float cw[8][kBeadsPerRound];       /* trilinear weight of octet corner c */
+	uint32_t gi_t[kBeadsPerRound];     /* type-channel element index | outer grid << 31 */
+	uint32_t gi_q[kBeadsPerRound];     /* charge-channel element index | outer grid << 31 */
 	uint32_t type[kBeadsPerRound];     /* raw type (NL parameters) */
 	uint32_t nl_idx[kBeadsPerRound];   /* list start */
 	uint32_t nl_pre[kBeadsPerRound + 1];  /* exclusive prefix of list lengths */
-	uint8_t look[2 * kBeadsPerRound];  /* lookup queue: bead << 1 | is_charge */
+	uint32_t look_i[2 * kBeadsPerRound];  /* lookup queue: element index | outer << 31 */
+	uint8_t look_s[2 * kBeadsPerRound];   /* lookup queue: bead slot | is_charge << 7 */
 	/* the pose: rotation matrix [0, 9), sin/cos of phi, ssi, rot [9, 15),
 	 * translation [15, 18); kept here rather than in registers */
 	float pose[18];
@@ -91,8 +91,10 @@ __device__ __forceinline__ uint32_t warp_incl_scan(uint32_t v, int lane) {
 /* potForce's grid selection for a staged bead at (px, py, pz),
  * src/model/interpolation.h:66-76, with getIndex / getVoxelByIndex
  * (src/model/IntrplGrid.h:96-104,130-163): picks inner or outer grid, stores
- * the octet offset and trilinear weights in slot s and returns the number of
- * lookups (0, 1, or 2 with the charge channel). */
+ * the eight trilinear corner weights and the element indices of the bead's
+ * type and charge channels in slot s, and returns the number of lookups (0,
+ * 1, or 2 with the charge channel).  An element index addresses a 128-byte
+ * octet record on octet grids and the first corner float4 otherwise. */
 __device__ __forceinline__ uint32_t stage_grid(const DevGrid& G, float px, float py, float pz,
 		uint32_t mapped, float q, int s, WarpStage& W) {
 	if (mapped == 0) return 0;
@@ -106,13 +108,23 @@ __device__ __forceinline__ uint32_t stage_grid(const DevGrid& G, float px, float
 	const float minx = fadd(fmul((float)ix, g.dVox), g.pos[0]);
 	const float miny = fadd(fmul((float)iy, g.dVox), g.pos[1]);
 	const float minz = fadd(fmul((float)iz, g.dVox), g.pos[2]);
-	W.wnx[s] = fsub(px, minx); W.wny[s] = fsub(py, miny); W.wnz[s] = fsub(pz, minz);
-	W.wxx[s] = fsub(fadd(minx, g.dVox), px);
-	W.wxy[s] = fsub(fadd(miny, g.dVox), py);
-	W.wxz[s] = fsub(fadd(minz, g.dVox), pz);
-	W.off[s] = g.oct ? (g.dimN[0] - 1) * (iz * (g.dimN[1] - 1) + iy) + ix
-	                 : g.dimN[0] * (iz * g.dimN[1] + iy) + ix;
-	W.chan[s] = mapped | (outer ? 0x80000000u : 0u);
+	const float pmn_x = fsub(px, minx), pmn_y = fsub(py, miny), pmn_z = fsub(pz, minz);
+	const float pmx_x = fsub(fadd(minx, g.dVox), px);
+	const float pmx_y = fsub(fadd(miny, g.dVox), py);
+	const float pmx_z = fsub(fadd(minz, g.dVox), pz);
+#pragma unroll
+	for (int c = 0; c < 8; ++c) W.cw[c][s] = corner_weight(c, pmn_x, pmn_y, pmn_z, pmx_x, pmx_y, pmx_z);
+	uint32_t off, cells;
+	if (g.oct) {
+		cells = (g.dimN[0] - 1) * (g.dimN[1] - 1) * (g.dimN[2] - 1);
+		off = (g.dimN[0] - 1) * (iz * (g.dimN[1] - 1) + iy) + ix;
+	} else {
+		cells = g.dimN[0] * g.dimN[1] * g.dimN[2];
+		off = g.dimN[0] * (iz * g.dimN[1] + iy) + ix;
+	}
+	const uint32_t og = outer ? 0x80000000u : 0u;
+	W.gi_t[s] = (mapped * cells + off) | og;
+	W.gi_q[s] = off | og;
 	return fabsf(q) > 0.001f ? 2u : 1u;
 }
 
@@ -131,42 +143,68 @@ __device__ __forceinline__ uint32_t stage_nl(const DevNL& nl, float px, float py
 	return d.x;
 }
 
-/* Grid and first corner of queued lookup e (bead << 1 | is_charge). */
-__device__ __forceinline__ const float4* lookup_base(const DevGrid& G, const WarpStage& W, uint32_t e,
-		const DevIntrpl*& gp) {
-	const uint32_t s = e >> 1;
-	const uint32_t ch = W.chan[s];
-	gp = (ch & 0x80000000u) ? &G.outer : &G.inner;
-	const uint32_t c = (e & 1u) ? 0u : (ch & 0x7fffffffu);
-	if (gp->oct) {
-		const size_t nocts = (size_t)(gp->dimN[0] - 1) * (gp->dimN[1] - 1) * (gp->dimN[2] - 1);
-		return gp->oct + 8 * ((size_t)c * nocts + W.off[s]);
-	}
-	const size_t sxy = (size_t)gp->dimN[0] * gp->dimN[1];
-	return gp->data + (size_t)c * (sxy * gp->dimN[2]) + W.off[s];
+/* Bead slot of queued lookup k. */
+__device__ __forceinline__ uint32_t lookup_slot(const WarpStage& W, uint32_t k) { return W.look_s[k] & 0x7fu; }
+
+/* Grid, element and scale of queued lookup k: 1/voxelVol, times the bead
+ * charge for the charge channel. */
+__device__ __forceinline__ const DevIntrpl& lookup_grid(const DevGrid& G, const WarpStage& W, uint32_t k,
+		uint32_t& elem, float& sc) {
+	const uint32_t i = W.look_i[k];
+	const DevIntrpl& g = (i & 0x80000000u) ? G.outer : G.inner;
+	elem = i & 0x7fffffffu;
+	const uint32_t ls = W.look_s[k];
+	sc = (ls & 0x80u) ? fmul(g.voxelVol_inv, W.q[ls & 0x7fu]) : g.voxelVol_inv;
+	return g;
 }
 
 /* One queued lookup by one lane: the channel's interpolated (fx, fy, fz, E),
- * scaled by 1/voxelVol and, for the charge channel, by the bead charge. */
-__device__ __forceinline__ float4 grid_lookup(const DevGrid& G, const WarpStage& W, uint32_t e) {
-	const uint32_t s = e >> 1;
-	const DevIntrpl* gp;
-	const float4* base = lookup_base(G, W, e, gp);
-	float4 v;
-	if (gp->oct)
-		v = octet_lerp(base, 2, 4, W.wnx[s], W.wny[s], W.wnz[s], W.wxx[s], W.wxy[s], W.wxz[s]);
-	else
-		v = octet_lerp(base, gp->dimN[0], gp->dimN[0] * gp->dimN[1], W.wnx[s], W.wny[s], W.wnz[s],
-				W.wxx[s], W.wxy[s], W.wxz[s]);
-	const float sc = (e & 1u) ? fmul(gp->voxelVol_inv, W.q[s]) : gp->voxelVol_inv;
-	v.x = fmul(v.x, sc); v.y = fmul(v.y, sc); v.z = fmul(v.z, sc); v.w = fmul(v.w, sc);
-	return v;
+ * scaled. */
+__device__ __forceinline__ float4 grid_lookup(const DevGrid& G, const WarpStage& W, uint32_t k) {
+	const uint32_t s = lookup_slot(W, k);
+	uint32_t elem;
+	float sc;
+	const DevIntrpl& g = lookup_grid(G, W, k, elem, sc);
+	float w[8];
+#pragma unroll
+	for (int c = 0; c < 8; ++c) w[c] = W.cw[c][s];
+	const float4 v = g.oct ? octet_lerp_w(g.oct + 8 * (size_t)elem, 2, 4, w)
+	                       : octet_lerp_w(g.data + elem, g.dimN[0], g.dimN[0] * g.dimN[1], w);
+	return make_float4(fmul(v.x, sc), fmul(v.y, sc), fmul(v.z, sc), fmul(v.w, sc));
 }
 
 /* Writes the lookup queue entries of slot s (n = 0..2) at position k. */
 __device__ __forceinline__ void enqueue_lookups(WarpStage& W, uint32_t& k, int s, uint32_t n) {
-	if (n > 0) W.look[k++] = (uint8_t)(s << 1);
-	if (n > 1) W.look[k++] = (uint8_t)((s << 1) | 1);
+	if (n > 0) { W.look_i[k] = W.gi_t[s]; W.look_s[k] = (uint8_t)s; ++k; }
+	if (n > 1) { W.look_i[k] = W.gi_q[s]; W.look_s[k] = (uint8_t)(s | 0x80); ++k; }
+}
+
+/* Fills the lookup queue of a round from the per-lane counts (nlk[0] for
+ * bead slot lane, nlk[1] for slot lane + 32): slots 0..31 first, then 32..63,
+ * so that neighbouring queue entries belong to beads in different shared-
+ * memory banks.  Returns the queue length. */
+__device__ __forceinline__ uint32_t queue_lookups(WarpStage& W, const uint32_t nlk[2], int lane) {
+	const uint32_t incl = warp_incl_scan(nlk[0] | (nlk[1] << 16), lane);
+	const uint32_t tot = __shfl_sync(GBA_FULL_MASK, incl, 31);
+	const uint32_t tot_a = tot & 0xffffu;
+	uint32_t ka = (incl & 0xffffu) - nlk[0];
+	uint32_t kb = tot_a + (incl >> 16) - nlk[1];
+	enqueue_lookups(W, ka, lane, nlk[0]);
+	enqueue_lookups(W, kb, lane + 32, nlk[1]);
+	return tot_a + (tot >> 16);
+}
+
+/* Exclusive prefix of the NL list lengths over slots 0..63 (slot lane, then
+ * lane + 32) into W.nl_pre; returns the number of pairs of the round. */
+__device__ __forceinline__ uint32_t queue_pairs(WarpStage& W, const uint32_t nln[2], int lane) {
+	const uint32_t a_incl = warp_incl_scan(nln[0], lane);
+	const uint32_t a_tot = __shfl_sync(GBA_FULL_MASK, a_incl, 31);
+	const uint32_t b_incl = warp_incl_scan(nln[1], lane);
+	W.nl_pre[lane] = a_incl - nln[0];
+	W.nl_pre[lane + 32] = a_tot + b_incl - nln[1];
+	const uint32_t n_pair = a_tot + __shfl_sync(GBA_FULL_MASK, b_incl, 31);
+	if (lane == 0) W.nl_pre[kBeadsPerRound] = n_pair;
+	return n_pair;
 }
 
 /* Owner slot of flattened pair k: the last s with nl_pre[s] <= k. */
@@ -193,83 +231,114 @@ struct PoseSums {
 	}
 };
 
-/* One lane's share of cooperative lookup k: its corner times its trilinear
- * weight, and the lookup's scale. */
-struct CoopPart {
-	float4 v;
-	float sc;
-	uint32_t e;
-	bool valid;
+/* Cooperative accumulators of one lane: the lane always ends a butterfly
+ * holding the same component (x, y, z of the force or E) of one of the two
+ * lookups of its group, so it accumulates that component and, for a force
+ * component, its three torque-matrix entries u (x) f. */
+struct CoopSums {
+	float f = 0.f, t0 = 0.f, t1 = 0.f, t2 = 0.f;
+	/* adds the lane's role into S: comp 0..2 = force x, y, z, 3 = energy
+	 * (static indices only, so S stays in registers) */
+	__device__ __forceinline__ void fold(PoseSums& S, int comp) const {
+		const float z = 0.f;
+		S.E = fadd(S.E, comp == 3 ? f : z);
+		S.Fx = fadd(S.Fx, comp == 0 ? f : z);
+		S.Fy = fadd(S.Fy, comp == 1 ? f : z);
+		S.Fz = fadd(S.Fz, comp == 2 ? f : z);
+#pragma unroll
+		for (int r = 0; r < 3; ++r) {
+			S.T[3 * r] = fadd(S.T[3 * r], comp == r ? t0 : z);
+			S.T[3 * r + 1] = fadd(S.T[3 * r + 1], comp == r ? t1 : z);
+			S.T[3 * r + 2] = fadd(S.T[3 * r + 2], comp == r ? t2 : z);
+		}
+	}
 };
 
-__device__ __forceinline__ CoopPart coop_part(const DevGrid& G, const WarpStage& W, uint32_t k,
-		uint32_t n_look, int cor) {
-	CoopPart r;
-	r.v = make_float4(0.f, 0.f, 0.f, 0.f);
-	r.sc = 0.f;
-	r.e = 0;
-	r.valid = k < n_look;
-	if (r.valid) {
-		r.e = W.look[k];
-		const uint32_t s = r.e >> 1;
-		const DevIntrpl* gp;
-		const float4* p = lookup_base(G, W, r.e, gp) + cor;
-		const float4 d = ldg_no_l1(p);
-		const float w = corner_weight(cor, W.wnx[s], W.wny[s], W.wnz[s], W.wxx[s], W.wxy[s], W.wxz[s]);
-		r.v.x = fmul(d.x, w); r.v.y = fmul(d.y, w); r.v.z = fmul(d.z, w); r.v.w = fmul(d.w, w);
-		r.sc = (r.e & 1u) ? fmul(gp->voxelVol_inv, W.q[s]) : gp->voxelVol_inv;
-	}
-	return r;
-}
-
-/* Drains the lookup queue of a round into S.  Cooperative form: lane group
- * grp = lane / 8 takes lookup k0 + grp and lane cor = lane % 8 loads octet
- * corner cor (x = bit 0, y = bit 1, z = bit 2; the octet record stores d000
- * d100 d010 d110 d001 d101 d011 d111) times its trilinear weight
- * (src/model/trilinIntrpl.h:29-66); a three-step butterfly sums the eight
- * products.  The sum order differs from the reference's left-to-right sum
- * (FP32 rounding only). */
+/* Drains the lookup queue of a round.  Per-lane form: one lookup per lane
+ * into S.  Cooperative form (octet layout): lane group g = lane / 8 takes
+ * lookups k0 + g and k0 + 4 + g, lane c = lane % 8 loads octet corner c of
+ * both (one 128-byte line per lookup, read without L1 allocation) times its
+ * trilinear weight (src/model/trilinIntrpl.h:29-66).  A three-step
+ * reduce-scatter over the group leaves lane c holding one finished component
+ * -- lookup (c & 1), component 2 * ((c >> 1) & 1) + (c >> 2) -- summed in
+ * octet_sum's pairwise order, so both forms give the same value per lookup.
+ * The lane scales it and adds it to its CoopSums role. */
 __device__ __forceinline__ void drain_lookups(const DevGrid& G, const WarpStage& W, uint32_t n_look,
-		int lane, PoseSums& S) {
+		int lane, PoseSums& S, CoopSums& C) {
 	if (!G.coop_lookup) {
 		for (uint32_t k = lane; k < n_look; k += 32) {
-			const uint32_t e = W.look[k];
-			const uint32_t s = e >> 1;
-			const float4 v = grid_lookup(G, W, e);
+			const uint32_t s = lookup_slot(W, k);
+			const float4 v = grid_lookup(G, W, k);
 			S.add(v.w, v.x, v.y, v.z, W.ux[s], W.uy[s], W.uz[s]);
 		}
 		return;
 	}
 	const int grp = lane >> 3, cor = lane & 7;
-	/* two lookups per lane group and iteration: both corner loads are in
-	 * flight before the butterflies */
+	const int mine = cor & 1;                               /* which of the two lookups */
+	const int comp = 2 * ((cor >> 1) & 1) + (cor >> 2);     /* which component */
 	for (uint32_t k0 = 0; k0 < n_look; k0 += 8) {
-		CoopPart a = coop_part(G, W, k0 + grp, n_look, cor);
-		CoopPart b = coop_part(G, W, k0 + 4 + grp, n_look, cor);
+		float c8[8];     /* lookup a (k0 + grp) x y z w, lookup b (k0 + 4 + grp) x y z w */
+		uint32_t sl[2];
+		float sc[2];
+		bool ok[2];
 #pragma unroll
-		for (int o = 1; o < 8; o <<= 1) {
-			a.v.x = fadd(a.v.x, __shfl_xor_sync(GBA_FULL_MASK, a.v.x, o));
-			a.v.y = fadd(a.v.y, __shfl_xor_sync(GBA_FULL_MASK, a.v.y, o));
-			a.v.z = fadd(a.v.z, __shfl_xor_sync(GBA_FULL_MASK, a.v.z, o));
-			a.v.w = fadd(a.v.w, __shfl_xor_sync(GBA_FULL_MASK, a.v.w, o));
-			b.v.x = fadd(b.v.x, __shfl_xor_sync(GBA_FULL_MASK, b.v.x, o));
-			b.v.y = fadd(b.v.y, __shfl_xor_sync(GBA_FULL_MASK, b.v.y, o));
-			b.v.z = fadd(b.v.z, __shfl_xor_sync(GBA_FULL_MASK, b.v.z, o));
-			b.v.w = fadd(b.v.w, __shfl_xor_sync(GBA_FULL_MASK, b.v.w, o));
-		}
-		if (cor == 0) {
-			if (a.valid) {
-				const uint32_t s = a.e >> 1;
-				S.add(fmul(a.v.w, a.sc), fmul(a.v.x, a.sc), fmul(a.v.y, a.sc), fmul(a.v.z, a.sc), W.ux[s],
-						W.uy[s], W.uz[s]);
+		for (int h = 0; h < 2; ++h) {
+			const uint32_t k = k0 + 4 * h + grp;
+			ok[h] = k < n_look;
+			float4 d = make_float4(0.f, 0.f, 0.f, 0.f);
+			float w = 0.f;
+			sl[h] = 0;
+			sc[h] = 0.f;
+			if (ok[h]) {
+				uint32_t elem;
+				const DevIntrpl& g = lookup_grid(G, W, k, elem, sc[h]);
+				sl[h] = lookup_slot(W, k);
+				d = ldg_no_l1(g.oct + 8 * (size_t)elem + cor);
+				w = W.cw[cor][sl[h]];
 			}
-			if (b.valid) {
-				const uint32_t s = b.e >> 1;
-				S.add(fmul(b.v.w, b.sc), fmul(b.v.x, b.sc), fmul(b.v.y, b.sc), fmul(b.v.z, b.sc), W.ux[s],
-						W.uy[s], W.uz[s]);
+			c8[4 * h] = fmul(d.x, w); c8[4 * h + 1] = fmul(d.y, w);
+			c8[4 * h + 2] = fmul(d.z, w); c8[4 * h + 3] = fmul(d.w, w);
+		}
+		/* step 1 (partner c ^ 1): keep lookup (c & 1) */
+		float m4[4];
+#pragma unroll
+		for (int j = 0; j < 4; ++j) {
+			const float keep = mine ? c8[4 + j] : c8[j];
+			const float send = mine ? c8[j] : c8[4 + j];
+			m4[j] = fadd(keep, __shfl_xor_sync(GBA_FULL_MASK, send, 1));
+		}
+		/* step 2 (partner c ^ 2): keep components {0,1} or {2,3} */
+		const int hi2 = (cor >> 1) & 1;
+		float m2[2];
+#pragma unroll
+		for (int j = 0; j < 2; ++j) {
+			const float keep = hi2 ? m4[2 + j] : m4[j];
+			const float send = hi2 ? m4[j] : m4[2 + j];
+			m2[j] = fadd(keep, __shfl_xor_sync(GBA_FULL_MASK, send, 2));
+		}
+		/* step 3 (partner c ^ 4): keep one */
+		const int hi4 = cor >> 2;
+		const float keep = hi4 ? m2[1] : m2[0];
+		const float send = hi4 ? m2[0] : m2[1];
+		const float v = fadd(keep, __shfl_xor_sync(GBA_FULL_MASK, send, 4));
+		/* the lane's lookup, selected without indexing (keeps the arrays in registers) */
+		if (mine ? ok[1] : ok[0]) {
+			const uint32_t s = mine ? sl[1] : sl[0];
+			const float f = fmul(v, mine ? sc[1] : sc[0]);
+			C.f = fadd(C.f, f);
+			if (comp != 3) {
+				C.t0 = ffma(W.ux[s], f, C.t0);
+				C.t1 = ffma(W.uy[s], f, C.t1);
+				C.t2 = ffma(W.uz[s], f, C.t2);
 			}
 		}
 	}
+}
+
+/* Fold of the cooperative accumulators into the pose sums (component of the lane). */
+__device__ __forceinline__ void fold_coop(const CoopSums& C, PoseSums& S, int lane) {
+	const int cor = lane & 7;
+	C.fold(S, 2 * ((cor >> 1) & 1) + (cor >> 2));
 }
 
 /* One NL pair term (plateau-subtracted LJ + Coulomb), the body of the
@@ -281,23 +350,27 @@ __device__ __forceinline__ bool nl_pair(const DevNL& nl, const DevParams& P, uin
 	float dx = fsub(px, rx), dy = fsub(py, ry), dz = fsub(pz, rz);
 	const float dr2 = fadd(fadd(fmul(dx, dx), fmul(dy, dy)), fmul(dz, dz));
 	if (!(dr2 <= nl.dPlateau2) || trec == 0) return false;
-	const float dr2_inv = __frcp_rn(dr2);
+	/* 1/r^2 only scales smooth terms: its one decision, the Coulomb cutoff
+	 * at 1/r^2 = 1/50^2 (src/model/forcefield.h:104-113), lies outside any
+	 * plateau below 50 A, where nl.approx_inv allows the hardware reciprocal */
+	const float dr2_inv = nl.approx_inv ? frcp_approx(dr2) : __frcp_rn(dr2);
 	dx = fmul(dx, dr2_inv); dy = fmul(dy, dr2_inv); dz = fmul(dz, dr2_inv);
 	const bool shape86 = P.potshape == GBA_POTSHAPE_8_6;
 	const size_t k = (size_t)P.num_types * (trec - 1) + (lig_type - 1);
-	const float4 p = __ldg(&P.lj[k]);
-	const float iv = __ldg(&P.ivor[k]);
+	const float4 p = __ldg(&P.pair[2 * k]);
+	const float4 pl = __ldg(&P.pair[2 * k + 1]);   /* ipon, plateau force factor, plateau energy */
 	float f1x, f1y, f1z, e1;
-	lj_pot_force(dr2, dr2_inv, dx, dy, dz, p, iv, shape86, f1x, f1y, f1z, e1);
+	lj_pot_force(dr2, dr2_inv, dx, dy, dz, p, pl.x, shape86, f1x, f1y, f1z, e1);
 	/* getRatio's table bin, src/model/NLGrid.h:141-143 */
 	const int bin = (int)fmul(dr2, 10000.0f);
 	const float ratio = nl.ratio_computed
-			? __fsqrt_rn(fmul(fadd((float)bin, 0.5f), nl.ratio_scale))
+			? fsqrt_approx(fmul(fadd((float)bin, 0.5f), nl.ratio_scale))
 			: __ldg(&nl.ratio[bin]);
 	const float rdx = fmul(ratio, dx), rdy = fmul(ratio, dy), rdz = fmul(ratio, dz);
-	float f2x, f2y, f2z, e2;
-	lj_pot_force(nl.dPlateau2, nl.dPlateau2_inv, rdx, rdy, rdz, p, iv, shape86, f2x, f2y, f2z, e2);
-	fx = fsub(f1x, f2x); fy = fsub(f1y, f2y); fz = fsub(f1z, f2z); e = fsub(e1, e2);
+	/* LJPotForce at the plateau along the same direction: the per-type-pair
+	 * factor and energy come precomputed with the table */
+	fx = fsub(f1x, fmul(pl.y, rdx)); fy = fsub(f1y, fmul(pl.y, rdy)); fz = fsub(f1z, fmul(pl.y, rdz));
+	e = fsub(e1, pl.z);
 	const float qq = fmul(fmul(qlig, rq), P.ffelec);
 	if (fabsf(qq) > 0.001f) {
 		const bool cdiel = P.dielec == GBA_DIELEC_CONSTANT;
@@ -317,6 +390,7 @@ __device__ __forceinline__ void eval_pose_rigid(const RigidModel& M, float tx, f
 		float a0, float a1, float a2, int lane, WarpStage& W, float res[7], PoseCensus* census) {
 	put_pose(W, pose_rotation(a0, a1, a2, lane), tx, ty, tz, lane);
 	PoseSums S;
+	CoopSums C;
 	uint32_t c_grid = 0, c_charged = 0, c_nl = 0, c_ent = 0;
 	for (uint32_t i0 = 0; i0 < M.lig.n; i0 += kBeadsPerRound) {
 		/* 1. stage 64 beads, two per lane: lane, then lane + 32 */
@@ -351,24 +425,12 @@ __device__ __forceinline__ void eval_pose_rigid(const RigidModel& M, float tx, f
 				c_ent += nln[h];
 			}
 		}
-		/* queue positions: lookups of bead lane, then bead lane+32 */
-		const uint32_t lk_incl = warp_incl_scan(nlk[0] + nlk[1], lane);
-		const uint32_t n_look = __shfl_sync(GBA_FULL_MASK, lk_incl, 31);
-		uint32_t lk = lk_incl - nlk[0] - nlk[1];
-		enqueue_lookups(W, lk, lane, nlk[0]);
-		enqueue_lookups(W, lk, lane + 32, nlk[1]);
-		/* NL prefix over slots: slot s < 32 first, then s + 32 */
-		const uint32_t a_incl = warp_incl_scan(nln[0], lane);
-		const uint32_t a_tot = __shfl_sync(GBA_FULL_MASK, a_incl, 31);
-		const uint32_t b_incl = warp_incl_scan(nln[1], lane);
-		W.nl_pre[lane] = a_incl - nln[0];
-		W.nl_pre[lane + 32] = a_tot + b_incl - nln[1];
-		const uint32_t n_pair = a_tot + __shfl_sync(GBA_FULL_MASK, b_incl, 31);
-		if (lane == 0) W.nl_pre[kBeadsPerRound] = n_pair;
+		const uint32_t n_look = queue_lookups(W, nlk, lane);
+		const uint32_t n_pair = queue_pairs(W, nln, lane);
 		__syncwarp();
 
 		/* 2. grid lookups */
-		drain_lookups(M.grid, W, n_look, lane, S);
+		drain_lookups(M.grid, W, n_look, lane, S, C);
 
 		/* 3. neighbour pairs, one per lane; two per lane and iteration so that
 		 * both gather chains (list entry -> receptor bead -> parameters) are
@@ -394,6 +456,7 @@ __device__ __forceinline__ void eval_pose_rigid(const RigidModel& M, float tx, f
 		}
 		__syncwarp();
 	}
+	fold_coop(C, S, lane);
 	float sE = warp_sum(S.E), sFx = warp_sum(S.Fx), sFy = warp_sum(S.Fy), sFz = warp_sum(S.Fz);
 	float T[9];
 #pragma unroll

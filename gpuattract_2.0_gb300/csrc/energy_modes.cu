@@ -168,7 +168,8 @@ __device__ __forceinline__ float eval_pose_modes(const ModesLaunch& L, const flo
 			}
 		}
 		const uint32_t n_look = queue_lookups(W, nlk, lane);
-		const uint32_t n_pair = queue_pairs(W, nln, lane);
+		uint32_t start[2];
+		const uint32_t n_pair = queue_pairs(W, nln, lane, start);
 		__syncwarp();
 		for (uint32_t q = lane; q < n_look; q += 32) {
 			const uint32_t s = lookup_slot(W, q);

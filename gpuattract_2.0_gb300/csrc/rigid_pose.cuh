@@ -48,6 +48,7 @@ struct WarpStage {
 	uint32_t nl_pre[kBeadsPerRound + 1];  /* exclusive prefix of list lengths */
 	uint32_t look_i[2 * kBeadsPerRound];  /* lookup queue: element index | outer << 31 */
 	uint8_t look_s[2 * kBeadsPerRound];   /* lookup queue: bead slot | is_charge << 7 */
+	uint8_t own[64];                   /* PairWindow: slot of the bead starting at window position b */
 	/* the pose: rotation matrix [0, 9), sin/cos of phi, ssi, rot [9, 15),
 	 * translation [15, 18); kept here rather than in registers */
 	float pose[18];
@@ -196,12 +197,15 @@ __device__ __forceinline__ uint32_t queue_lookups(WarpStage& W, const uint32_t n
 
 /* Exclusive prefix of the NL list lengths over slots 0..63 (slot lane, then
  * lane + 32) into W.nl_pre; returns the number of pairs of the round. */
-__device__ __forceinline__ uint32_t queue_pairs(WarpStage& W, const uint32_t nln[2], int lane) {
+__device__ __forceinline__ uint32_t queue_pairs(WarpStage& W, const uint32_t nln[2], int lane,
+		uint32_t start[2]) {
 	const uint32_t a_incl = warp_incl_scan(nln[0], lane);
 	const uint32_t a_tot = __shfl_sync(GBA_FULL_MASK, a_incl, 31);
 	const uint32_t b_incl = warp_incl_scan(nln[1], lane);
-	W.nl_pre[lane] = a_incl - nln[0];
-	W.nl_pre[lane + 32] = a_tot + b_incl - nln[1];
+	start[0] = a_incl - nln[0];
+	start[1] = a_tot + b_incl - nln[1];
+	W.nl_pre[lane] = start[0];
+	W.nl_pre[lane + 32] = start[1];
 	const uint32_t n_pair = a_tot + __shfl_sync(GBA_FULL_MASK, b_incl, 31);
 	if (lane == 0) W.nl_pre[kBeadsPerRound] = n_pair;
 	return n_pair;
@@ -217,6 +221,37 @@ __device__ __forceinline__ uint32_t pair_owner(const WarpStage& W, uint32_t k) {
 	}
 	return lo;
 }
+
+/* Owners of the 64 pairs [w, w + 64) of a round, window by window: every
+ * non-empty bead starting inside the window sets bit (start - w) and records
+ * its slot in W.own; the owner of pair w + b is the bead of the highest set
+ * bit <= b, or, with none, the bead that covered pair w - 1 (carry).  Two
+ * warp OR-reductions per window replace a 6-step search per pair. */
+struct PairWindow {
+	uint32_t carry = 0;
+	/* lane gets the owners of pairs w + lane and w + 32 + lane */
+	__device__ __forceinline__ void owners(WarpStage& W, uint32_t w, const uint32_t start[2],
+			const uint32_t len[2], int lane, uint32_t& sa, uint32_t& sb) {
+		uint32_t lo = 0, hi = 0;
+#pragma unroll
+		for (int h = 0; h < 2; ++h)
+			if (len[h] > 0 && start[h] >= w && start[h] - w < 64u) {
+				const uint32_t b = start[h] - w;
+				W.own[b] = (uint8_t)(lane + 32 * h);
+				if (b < 32) lo |= 1u << b; else hi |= 1u << (b - 32);
+			}
+		lo = __reduce_or_sync(GBA_FULL_MASK, lo);
+		hi = __reduce_or_sync(GBA_FULL_MASK, hi);
+		__syncwarp();
+		const uint32_t upto = 0xffffffffu >> (31 - lane);   /* bits 0..lane */
+		const uint32_t last_lo = lo ? W.own[31 - __clz(lo)] : carry;   /* owner of pair w + 31 */
+		const uint32_t mlo = lo & upto, mhi = hi & upto;
+		sa = mlo ? W.own[31 - __clz(mlo)] : carry;
+		sb = mhi ? W.own[63 - __clz(mhi)] : last_lo;
+		carry = hi ? W.own[63 - __clz(hi)] : last_lo;              /* owner of pair w + 63 */
+		__syncwarp();
+	}
+};
 
 /* Accumulates f into the pose sums with the bead's unrotated coordinates. */
 struct PoseSums {
@@ -426,7 +461,8 @@ __device__ __forceinline__ void eval_pose_rigid(const RigidModel& M, float tx, f
 			}
 		}
 		const uint32_t n_look = queue_lookups(W, nlk, lane);
-		const uint32_t n_pair = queue_pairs(W, nln, lane);
+		uint32_t start[2];
+		const uint32_t n_pair = queue_pairs(W, nln, lane, start);
 		__syncwarp();
 
 		/* 2. grid lookups */
@@ -435,11 +471,13 @@ __device__ __forceinline__ void eval_pose_rigid(const RigidModel& M, float tx, f
 		/* 3. neighbour pairs, one per lane; two per lane and iteration so that
 		 * both gather chains (list entry -> receptor bead -> parameters) are
 		 * in flight together */
-		for (uint32_t k = lane; k < n_pair; k += 64) {
-			const uint32_t k2 = k + 32;
+		PairWindow win;
+		for (uint32_t w = 0; w < n_pair; w += 64) {
+			const uint32_t k = w + lane, k2 = k + 32;
+			uint32_t sa, sb;
+			win.owners(W, w, start, nln, lane, sa, sb);
+			if (k >= n_pair) continue;
 			const bool has2 = k2 < n_pair;
-			const uint32_t sa = pair_owner(W, k);
-			const uint32_t sb = has2 ? pair_owner(W, k2) : sa;
 			const uint32_t ja = __ldg(&M.grid.nl.list[W.nl_idx[sa] + (k - W.nl_pre[sa])]);
 			const uint32_t jb = has2 ? __ldg(&M.grid.nl.list[W.nl_idx[sb] + (k2 - W.nl_pre[sb])]) : ja;
 			const float4 ra = __ldg(&M.rec.xyzq[ja]);

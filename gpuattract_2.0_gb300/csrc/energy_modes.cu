@@ -108,11 +108,13 @@ __device__ __forceinline__ float eval_pose_modes(const ModesLaunch& L, const flo
 	/* ---- receptor beads in the ligand grid ---- */
 	for (uint32_t j0 = 0; j0 < L.rec.n; j0 += kBeadsPerRound) {
 		uint32_t nlk[2];
+		BeadGrid bg[2];
 #pragma unroll
 		for (int h = 0; h < 2; ++h) {
 			const int s = lane + 32 * h;
 			const uint32_t j = j0 + s;
 			nlk[h] = 0;
+			bg[h] = BeadGrid{0u, 0u};
 			if (j < L.rec.n) {
 				const float4 r = __ldg(&L.rec.xyzq[j]);
 				const uint32_t mapped = __ldg(&L.rec.tm[j]) >> 16;
@@ -121,12 +123,12 @@ __device__ __forceinline__ float eval_pose_modes(const ModesLaunch& L, const flo
 				float px, py, pz;
 				rot_apply(Ri, x, y, z, px, py, pz);
 				px = fadd(px, ipx); py = fadd(py, ipy); pz = fadd(pz, ipz);
-				W.q[s] = r.w;
-				W.type[s] = j;      /* receptor bead index of the slot */
-				nlk[h] = stage_grid(L.grid_lig, px, py, pz, mapped, r.w, s, W);
+				/* the type field carries the receptor bead index of the slot */
+				put_bead(W, s, 0.f, 0.f, 0.f, px, py, pz, r.w, j);
+				nlk[h] = stage_grid(L.grid_lig, px, py, pz, mapped, r.w, s, W, bg[h]);
 			}
 		}
-		const uint32_t n_look = queue_lookups(W, nlk, lane);
+		const uint32_t n_look = queue_lookups(W, nlk, bg, lane);
 		__syncwarp();
 		for (uint32_t q = lane; q < n_look; q += 32) {
 			const uint32_t s = lookup_slot(W, q);
@@ -134,7 +136,7 @@ __device__ __forceinline__ float eval_pose_modes(const ModesLaunch& L, const flo
 			/* back into the receptor frame, then -(force . mode) */
 			float fx, fy, fz;
 			rot_apply(R.m, v.x, v.y, v.z, fx, fy, fz);
-			project(L.rec_modes + (size_t)W.type[s] * L.rec_ms, Mr, fx, fy, fz, -1.f, gR);
+			project(L.rec_modes + (size_t)__float_as_uint(W.ut[s].w) * L.rec_ms, Mr, fx, fy, fz, -1.f, gR);
 		}
 		__syncwarp();
 	}
@@ -143,12 +145,14 @@ __device__ __forceinline__ float eval_pose_modes(const ModesLaunch& L, const flo
 	PoseSums S;
 	for (uint32_t i0 = 0; i0 < L.lig.n; i0 += kBeadsPerRound) {
 		uint32_t nlk[2], nln[2];
+		BeadGrid bg[2];
 #pragma unroll
 		for (int h = 0; h < 2; ++h) {
 			const int s = lane + 32 * h;
 			const uint32_t i = i0 + s;
 			nlk[h] = 0;
 			nln[h] = 0;
+			bg[h] = BeadGrid{0u, 0u};
 			if (i < L.lig.n) {
 				const float4 b = __ldg(&L.lig.xyzq[i]);
 				const uint32_t tm = __ldg(&L.lig.tm[i]);
@@ -158,45 +162,53 @@ __device__ __forceinline__ float eval_pose_modes(const ModesLaunch& L, const flo
 				float px, py, pz;
 				rot_apply(R.m, x, y, z, px, py, pz);
 				px = fadd(px, tx); py = fadd(py, ty); pz = fadd(pz, tz);
-				W.ux[s] = b.x; W.uy[s] = b.y; W.uz[s] = b.z;
-				W.px[s] = px; W.py[s] = py; W.pz[s] = pz;
-				W.q[s] = b.w;
-				W.type[s] = type;
-				nlk[h] = stage_grid(L.grid_rec, px, py, pz, mapped, b.w, s, W);
+				put_bead(W, s, b.x, b.y, b.z, px, py, pz, b.w, type);
+				nlk[h] = stage_grid(L.grid_rec, px, py, pz, mapped, b.w, s, W, bg[h]);
 				bool in_nl;
 				if (type != 0) nln[h] = stage_nl(L.grid_rec.nl, px, py, pz, s, W, in_nl);
 			}
 		}
-		const uint32_t n_look = queue_lookups(W, nlk, lane);
+		const uint32_t n_look = queue_lookups(W, nlk, bg, lane);
 		uint32_t start[2];
 		const uint32_t n_pair = queue_pairs(W, nln, lane, start);
 		__syncwarp();
 		for (uint32_t q = lane; q < n_look; q += 32) {
 			const uint32_t s = lookup_slot(W, q);
 			const float4 v = grid_lookup(L.grid_rec, W, q);
-			S.add(v.w, v.x, v.y, v.z, W.ux[s], W.uy[s], W.uz[s]);
+			const float4 u = W.ut[s];
+			S.add(v.w, v.x, v.y, v.z, u.x, u.y, u.z);
 			float rx, ry, rz;
 			rot_apply_t(R.m, v.x, v.y, v.z, rx, ry, rz);
 			project(L.lig_modes + (size_t)(i0 + s) * L.lig_ms, Ml, rx, ry, rz, -1.f, gL);
 		}
-		for (uint32_t q = lane; q < n_pair; q += 32) {
-			const uint32_t s = pair_owner(W, q);
-			const uint32_t j = __ldg(&L.grid_rec.nl.list[W.nl_idx[s] + (q - W.nl_pre[s])]);
-			const float4 r = __ldg(&L.rec.xyzq[j]);
-			float rx = r.x, ry = r.y, rz = r.z;
-			const float* vr = L.rec_modes + (size_t)j * L.rec_ms;
-			deform(vr, Mr, ampR, rx, ry, rz);
-			const uint32_t trec = __ldg(&L.rec.tm[j]) & 0xffffu;
-			float fx, fy, fz, e;
-			if (!nl_pair(L.grid_rec.nl, L.par, W.type[s], W.q[s], W.px[s], W.py[s], W.pz[s], rx, ry, rz,
-					r.w, trec, fx, fy, fz, e))
-				continue;
-			S.add(e, fx, fy, fz, W.ux[s], W.uy[s], W.uz[s]);
-			/* reaction on receptor bead j is -f: its mode gradient gets -(-f . v) */
-			project(vr, Mr, fx, fy, fz, 1.f, gR);
-			float lx, ly, lz;
-			rot_apply_t(R.m, fx, fy, fz, lx, ly, lz);
-			project(L.lig_modes + (size_t)(i0 + s) * L.lig_ms, Ml, lx, ly, lz, -1.f, gL);
+		PairWindow win;
+		for (uint32_t w = 0; w < n_pair; w += 64) {
+			uint32_t so[2];
+			win.owners(W, w, start, nln, lane, so[0], so[1]);
+#pragma unroll
+			for (int h = 0; h < 2; ++h) {
+				const uint32_t q = w + 32 * h + lane;
+				if (q >= n_pair) continue;
+				const uint32_t s = so[h];
+				const uint32_t j = __ldg(&L.grid_rec.nl.list[W.lbase[s] + q]);
+				const float4 r = __ldg(&L.rec.xyzq[j]);
+				float rx = r.x, ry = r.y, rz = r.z;
+				const float* vr = L.rec_modes + (size_t)j * L.rec_ms;
+				deform(vr, Mr, ampR, rx, ry, rz);
+				const uint32_t trec = __ldg(&L.rec.tm[j]) & 0xffffu;
+				const float4 b = W.pq[s];
+				const float4 u = W.ut[s];
+				float fx, fy, fz, e;
+				if (!nl_pair(L.grid_rec.nl, L.par, __float_as_uint(u.w), b.w, b.x, b.y, b.z, rx, ry, rz,
+						r.w, trec, fx, fy, fz, e))
+					continue;
+				S.add(e, fx, fy, fz, u.x, u.y, u.z);
+				/* reaction on receptor bead j is -f: its mode gradient gets -(-f . v) */
+				project(vr, Mr, fx, fy, fz, 1.f, gR);
+				float lx, ly, lz;
+				rot_apply_t(R.m, fx, fy, fz, lx, ly, lz);
+				project(L.lig_modes + (size_t)(i0 + s) * L.lig_ms, Ml, lx, ly, lz, -1.f, gL);
+			}
 		}
 		__syncwarp();
 	}

@@ -378,7 +378,9 @@ int gba_upload_params(gba_ctx* ctx, uint32_t num_types, const gba_ffparam* table
  * plateau distance -- the force factor and energy the NL term subtracts
  * (src/model/neighborlist.h:122-130) -- in the rounding of the device's
  * lj_pot_force (unfused FP32, one fused multiply-add), so folding them in
- * changes no bit of the result. */
+ * changes no bit of the result.  Stored transposed against the host table
+ * (which is indexed receptor type major): the pairs of one ligand bead then
+ * read one contiguous row. */
 const float4* ParamsItem::pair_table(float dPlateau2) {
 	uint32_t key;
 	std::memcpy(&key, &dPlateau2, 4);
@@ -404,8 +406,10 @@ const float4* ParamsItem::pair_table(float dPlateau2) {
 			e = ivor * vlj;
 			fb = ivor * fb;
 		}
-		t[2 * k] = make_float4(p.rc, p.ac, p.rmin2, p.emin);
-		t[2 * k + 1] = make_float4(ivor, fb, e, 0.0f);
+		const size_t nt = (size_t)dev.num_types;
+		const size_t kt = (k % nt) * nt + k / nt;
+		t[2 * kt] = make_float4(p.rc, p.ac, p.rmin2, p.emin);
+		t[2 * kt + 1] = make_float4(ivor, fb, e, 0.0f);
 	}
 	auto buf = std::make_unique<DevBuffer>();
 	buf->upload(t.data(), t.size() * sizeof(float4));

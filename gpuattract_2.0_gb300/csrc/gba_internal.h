@@ -80,7 +80,9 @@ struct DevParams {
 	const float* ivor;        /* T*T ipon as float */
 	/* T*T pairs of float4 {rc, ac, rmin2, emin}, {ipon, fb_p, e_p, 0}: fb_p and
 	 * e_p are LJPotForce's force factor and energy at the plateau distance of
-	 * the grid in use, per type pair (set per launch) */
+	 * the grid in use, per type pair (set per launch); entry
+	 * (ligand type - 1) * T + (receptor type - 1), so the entries one ligand
+	 * bead meets lie in one row */
 	const float4* pair;
 };
 

@@ -34,20 +34,18 @@
 namespace gba {
 
 constexpr int kBeadsPerRound = 64;
+constexpr int kCornerStride = 9;   /* corner weights per slot, padded: 9 is odd, so
+                                      consecutive slots start in different banks */
 
-/* Per-warp staging of one round of beads (SoA, bank-conflict free). */
+/* Per-warp staging of one round of beads.  Consumers read whole records:
+ * one 16-byte load gives a bead's transformed position and charge, another
+ * its unrotated coordinates and type. */
 struct WarpStage {
-	float ux[kBeadsPerRound], uy[kBeadsPerRound], uz[kBeadsPerRound];   /* unrotated (torque) */
-	float px[kBeadsPerRound], py[kBeadsPerRound], pz[kBeadsPerRound];   /* transformed */
-	float q[kBeadsPerRound];
-	float cw[8][kBeadsPerRound];       /* trilinear weight of octet corner c */
-	uint32_t gi_t[kBeadsPerRound];     /* type-channel element index | outer grid << 31 */
-	uint32_t gi_q[kBeadsPerRound];     /* charge-channel element index | outer grid << 31 */
-	uint32_t type[kBeadsPerRound];     /* raw type (NL parameters) */
-	uint32_t nl_idx[kBeadsPerRound];   /* list start */
-	uint32_t nl_pre[kBeadsPerRound + 1];  /* exclusive prefix of list lengths */
-	uint32_t look_i[2 * kBeadsPerRound];  /* lookup queue: element index | outer << 31 */
-	uint8_t look_s[2 * kBeadsPerRound];   /* lookup queue: bead slot | is_charge << 7 */
+	float4 pq[kBeadsPerRound];         /* transformed x, y, z; charge */
+	float4 ut[kBeadsPerRound];         /* unrotated x, y, z (torque); type (bits) */
+	uint32_t lbase[kBeadsPerRound];    /* list start - first flattened pair of the slot */
+	float cw[kBeadsPerRound * kCornerStride];   /* trilinear weight of octet corner c */
+	uint2 look[2 * kBeadsPerRound];    /* lookup queue: {element | outer << 31, slot | is_charge << 7} */
 	uint8_t own[64];                   /* PairWindow: slot of the bead starting at window position b */
 	/* the pose: rotation matrix [0, 9), sin/cos of phi, ssi, rot [9, 15),
 	 * translation [15, 18); kept here rather than in registers */
@@ -79,6 +77,13 @@ __device__ __forceinline__ PoseRot get_pose(const WarpStage& W, float& tx, float
 	return R;
 }
 
+/* Staged bead record of slot s: positions, charge, torque lever, type. */
+__device__ __forceinline__ void put_bead(WarpStage& W, int s, float ux, float uy, float uz, float px,
+		float py, float pz, float q, uint32_t type) {
+	W.pq[s] = make_float4(px, py, pz, q);
+	W.ut[s] = make_float4(ux, uy, uz, __uint_as_float(type));
+}
+
 /* Inclusive warp scan of v. */
 __device__ __forceinline__ uint32_t warp_incl_scan(uint32_t v, int lane) {
 #pragma unroll
@@ -89,15 +94,20 @@ __device__ __forceinline__ uint32_t warp_incl_scan(uint32_t v, int lane) {
 	return v;
 }
 
+/* Element indices of a bead's grid lookups: type channel and charge channel,
+ * each | outer grid << 31.  An element addresses a 128-byte octet record on
+ * octet grids and the first corner float4 otherwise. */
+struct BeadGrid {
+	uint32_t t, q;
+};
+
 /* potForce's grid selection for a staged bead at (px, py, pz),
  * src/model/interpolation.h:66-76, with getIndex / getVoxelByIndex
  * (src/model/IntrplGrid.h:96-104,130-163): picks inner or outer grid, stores
- * the eight trilinear corner weights and the element indices of the bead's
- * type and charge channels in slot s, and returns the number of lookups (0,
- * 1, or 2 with the charge channel).  An element index addresses a 128-byte
- * octet record on octet grids and the first corner float4 otherwise. */
+ * the eight trilinear corner weights of slot s, sets the element indices and
+ * returns the number of lookups (0, 1, or 2 with the charge channel). */
 __device__ __forceinline__ uint32_t stage_grid(const DevGrid& G, float px, float py, float pz,
-		uint32_t mapped, float q, int s, WarpStage& W) {
+		uint32_t mapped, float q, int s, WarpStage& W, BeadGrid& bg) {
 	if (mapped == 0) return 0;
 	const bool inner = !grid_out(G.inner, px, py, pz);
 	const bool outer = !inner && !grid_out(G.outer, px, py, pz);
@@ -113,8 +123,9 @@ __device__ __forceinline__ uint32_t stage_grid(const DevGrid& G, float px, float
 	const float pmx_x = fsub(fadd(minx, g.dVox), px);
 	const float pmx_y = fsub(fadd(miny, g.dVox), py);
 	const float pmx_z = fsub(fadd(minz, g.dVox), pz);
+	float* cw = W.cw + kCornerStride * s;
 #pragma unroll
-	for (int c = 0; c < 8; ++c) W.cw[c][s] = corner_weight(c, pmn_x, pmn_y, pmn_z, pmx_x, pmx_y, pmx_z);
+	for (int c = 0; c < 8; ++c) cw[c] = corner_weight(c, pmn_x, pmn_y, pmn_z, pmx_x, pmx_y, pmx_z);
 	uint32_t off, cells;
 	if (g.oct) {
 		cells = (g.dimN[0] - 1) * (g.dimN[1] - 1) * (g.dimN[2] - 1);
@@ -124,13 +135,14 @@ __device__ __forceinline__ uint32_t stage_grid(const DevGrid& G, float px, float
 		off = g.dimN[0] * (iz * g.dimN[1] + iy) + ix;
 	}
 	const uint32_t og = outer ? 0x80000000u : 0u;
-	W.gi_t[s] = (mapped * cells + off) | og;
-	W.gi_q[s] = off | og;
+	bg.t = (mapped * cells + off) | og;
+	bg.q = off | og;
 	return fabsf(q) > 0.001f ? 2u : 1u;
 }
 
 /* NL voxel lookup of a staged bead (type != 0), NLPotForce's
- * src/model/neighborlist.h:59-66; returns the list length (0 outside). */
+ * src/model/neighborlist.h:59-66: stores the list start (queue_pairs turns it
+ * into the slot's list base) and returns the list length (0 outside). */
 __device__ __forceinline__ uint32_t stage_nl(const DevNL& nl, float px, float py, float pz, int s,
 		WarpStage& W, bool& in_nl) {
 	in_nl = false;
@@ -139,64 +151,65 @@ __device__ __forceinline__ uint32_t stage_nl(const DevNL& nl, float px, float py
 	const int iy = min(max((int)roundf(fmul(fsub(py, nl.pos[1]), nl.dVox_inv)), 0), (int)nl.dimN[1] - 1);
 	const int iz = min(max((int)roundf(fmul(fsub(pz, nl.pos[2]), nl.dVox_inv)), 0), (int)nl.dimN[2] - 1);
 	const uint2 d = __ldg(&nl.grid[nl.dimN[0] * (iz * nl.dimN[1] + iy) + ix]);
-	W.nl_idx[s] = d.y;
+	W.lbase[s] = d.y;
 	in_nl = true;
 	return d.x;
 }
 
 /* Bead slot of queued lookup k. */
-__device__ __forceinline__ uint32_t lookup_slot(const WarpStage& W, uint32_t k) { return W.look_s[k] & 0x7fu; }
+__device__ __forceinline__ uint32_t lookup_slot(const WarpStage& W, uint32_t k) { return W.look[k].y & 0x7fu; }
 
-/* Grid, element and scale of queued lookup k: 1/voxelVol, times the bead
- * charge for the charge channel. */
+/* Grid, element, slot and scale of queued lookup k: 1/voxelVol, times the
+ * bead charge for the charge channel. */
 __device__ __forceinline__ const DevIntrpl& lookup_grid(const DevGrid& G, const WarpStage& W, uint32_t k,
-		uint32_t& elem, float& sc) {
-	const uint32_t i = W.look_i[k];
-	const DevIntrpl& g = (i & 0x80000000u) ? G.outer : G.inner;
-	elem = i & 0x7fffffffu;
-	const uint32_t ls = W.look_s[k];
-	sc = (ls & 0x80u) ? fmul(g.voxelVol_inv, W.q[ls & 0x7fu]) : g.voxelVol_inv;
+		uint32_t& elem, uint32_t& s, float& sc) {
+	const uint2 e = W.look[k];
+	const DevIntrpl& g = (e.x & 0x80000000u) ? G.outer : G.inner;
+	elem = e.x & 0x7fffffffu;
+	s = e.y & 0x7fu;
+	sc = (e.y & 0x80u) ? fmul(g.voxelVol_inv, W.pq[s].w) : g.voxelVol_inv;
 	return g;
 }
 
 /* One queued lookup by one lane: the channel's interpolated (fx, fy, fz, E),
  * scaled. */
 __device__ __forceinline__ float4 grid_lookup(const DevGrid& G, const WarpStage& W, uint32_t k) {
-	const uint32_t s = lookup_slot(W, k);
-	uint32_t elem;
+	uint32_t elem, s;
 	float sc;
-	const DevIntrpl& g = lookup_grid(G, W, k, elem, sc);
+	const DevIntrpl& g = lookup_grid(G, W, k, elem, s, sc);
+	const float* cw = W.cw + kCornerStride * s;
 	float w[8];
 #pragma unroll
-	for (int c = 0; c < 8; ++c) w[c] = W.cw[c][s];
+	for (int c = 0; c < 8; ++c) w[c] = cw[c];
 	const float4 v = g.oct ? octet_lerp_w(g.oct + 8 * (size_t)elem, 2, 4, w)
 	                       : octet_lerp_w(g.data + elem, g.dimN[0], g.dimN[0] * g.dimN[1], w);
 	return make_float4(fmul(v.x, sc), fmul(v.y, sc), fmul(v.z, sc), fmul(v.w, sc));
 }
 
 /* Writes the lookup queue entries of slot s (n = 0..2) at position k. */
-__device__ __forceinline__ void enqueue_lookups(WarpStage& W, uint32_t& k, int s, uint32_t n) {
-	if (n > 0) { W.look_i[k] = W.gi_t[s]; W.look_s[k] = (uint8_t)s; ++k; }
-	if (n > 1) { W.look_i[k] = W.gi_q[s]; W.look_s[k] = (uint8_t)(s | 0x80); ++k; }
+__device__ __forceinline__ void enqueue_lookups(WarpStage& W, uint32_t k, int s, uint32_t n, const BeadGrid& bg) {
+	if (n > 0) W.look[k] = make_uint2(bg.t, (uint32_t)s);
+	if (n > 1) W.look[k + 1] = make_uint2(bg.q, (uint32_t)s | 0x80u);
 }
 
 /* Fills the lookup queue of a round from the per-lane counts (nlk[0] for
  * bead slot lane, nlk[1] for slot lane + 32): slots 0..31 first, then 32..63,
- * so that neighbouring queue entries belong to beads in different shared-
- * memory banks.  Returns the queue length. */
-__device__ __forceinline__ uint32_t queue_lookups(WarpStage& W, const uint32_t nlk[2], int lane) {
+ * so that neighbouring queue entries belong to neighbouring slots.  Returns
+ * the queue length. */
+__device__ __forceinline__ uint32_t queue_lookups(WarpStage& W, const uint32_t nlk[2], const BeadGrid bg[2],
+		int lane) {
 	const uint32_t incl = warp_incl_scan(nlk[0] | (nlk[1] << 16), lane);
 	const uint32_t tot = __shfl_sync(GBA_FULL_MASK, incl, 31);
 	const uint32_t tot_a = tot & 0xffffu;
-	uint32_t ka = (incl & 0xffffu) - nlk[0];
-	uint32_t kb = tot_a + (incl >> 16) - nlk[1];
-	enqueue_lookups(W, ka, lane, nlk[0]);
-	enqueue_lookups(W, kb, lane + 32, nlk[1]);
+	enqueue_lookups(W, (incl & 0xffffu) - nlk[0], lane, nlk[0], bg[0]);
+	enqueue_lookups(W, tot_a + (incl >> 16) - nlk[1], lane + 32, nlk[1], bg[1]);
 	return tot_a + (tot >> 16);
 }
 
 /* Exclusive prefix of the NL list lengths over slots 0..63 (slot lane, then
- * lane + 32) into W.nl_pre; returns the number of pairs of the round. */
+ * lane + 32); turns each slot's list start into its list base (list index of
+ * flattened pair k = lbase + k) and returns the number of pairs of the round
+ * and, per lane, the first flattened pair of its two slots. */
 __device__ __forceinline__ uint32_t queue_pairs(WarpStage& W, const uint32_t nln[2], int lane,
 		uint32_t start[2]) {
 	const uint32_t a_incl = warp_incl_scan(nln[0], lane);
@@ -204,29 +217,16 @@ __device__ __forceinline__ uint32_t queue_pairs(WarpStage& W, const uint32_t nln
 	const uint32_t b_incl = warp_incl_scan(nln[1], lane);
 	start[0] = a_incl - nln[0];
 	start[1] = a_tot + b_incl - nln[1];
-	W.nl_pre[lane] = start[0];
-	W.nl_pre[lane + 32] = start[1];
-	const uint32_t n_pair = a_tot + __shfl_sync(GBA_FULL_MASK, b_incl, 31);
-	if (lane == 0) W.nl_pre[kBeadsPerRound] = n_pair;
-	return n_pair;
-}
-
-/* Owner slot of flattened pair k: the last s with nl_pre[s] <= k. */
-__device__ __forceinline__ uint32_t pair_owner(const WarpStage& W, uint32_t k) {
-	uint32_t lo = 0, hi = kBeadsPerRound;
-#pragma unroll
-	for (int it = 0; it < 6; ++it) {
-		const uint32_t mid = (lo + hi) >> 1;
-		if (W.nl_pre[mid] <= k) lo = mid; else hi = mid;
-	}
-	return lo;
+	if (nln[0]) W.lbase[lane] -= start[0];
+	if (nln[1]) W.lbase[lane + 32] -= start[1];
+	return a_tot + __shfl_sync(GBA_FULL_MASK, b_incl, 31);
 }
 
 /* Owners of the 64 pairs [w, w + 64) of a round, window by window: every
  * non-empty bead starting inside the window sets bit (start - w) and records
  * its slot in W.own; the owner of pair w + b is the bead of the highest set
  * bit <= b, or, with none, the bead that covered pair w - 1 (carry).  Two
- * warp OR-reductions per window replace a 6-step search per pair. */
+ * warp OR-reductions per window replace a search per pair. */
 struct PairWindow {
 	uint32_t carry = 0;
 	/* lane gets the owners of pairs w + lane and w + 32 + lane */
@@ -290,81 +290,88 @@ struct CoopSums {
 };
 
 /* Drains the lookup queue of a round.  Per-lane form: one lookup per lane
- * into S.  Cooperative form (octet layout): lane group g = lane / 8 takes
- * lookups k0 + g and k0 + 4 + g, lane c = lane % 8 loads octet corner c of
- * both (one 128-byte line per lookup, read without L1 allocation) times its
- * trilinear weight (src/model/trilinIntrpl.h:29-66).  A three-step
- * reduce-scatter over the group leaves lane c holding one finished component
- * -- lookup (c & 1), component 2 * ((c >> 1) & 1) + (c >> 2) -- summed in
- * octet_sum's pairwise order, so both forms give the same value per lookup.
- * The lane scales it and adds it to its CoopSums role. */
+ * into S.  Cooperative form (octet layout), sixteen lookups per step in two
+ * blocks of eight: in block b, lane group g = lane / 8 takes lookups
+ * k0 + 8 b + g and k0 + 8 b + 4 + g, lane c = lane % 8 loads octet corner c
+ * of both (one 128-byte line per lookup, read without L1 allocation) times
+ * its trilinear weight (src/model/trilinIntrpl.h:29-66); all four loads of a
+ * lane are issued before the first is used.  A three-step reduce-scatter over
+ * the group leaves lane c holding one finished component -- lookup (c & 1),
+ * component 2 * ((c >> 1) & 1) + (c >> 2) -- summed in octet_sum's pairwise
+ * order, so both forms give the same value per lookup.  Each lane loads its
+ * own lookup first, which makes the first step select-free.  The lane scales
+ * the component and adds it to its CoopSums role. */
 __device__ __forceinline__ void drain_lookups(const DevGrid& G, const WarpStage& W, uint32_t n_look,
 		int lane, PoseSums& S, CoopSums& C) {
 	if (!G.coop_lookup) {
 		for (uint32_t k = lane; k < n_look; k += 32) {
 			const uint32_t s = lookup_slot(W, k);
 			const float4 v = grid_lookup(G, W, k);
-			S.add(v.w, v.x, v.y, v.z, W.ux[s], W.uy[s], W.uz[s]);
+			const float4 u = W.ut[s];
+			S.add(v.w, v.x, v.y, v.z, u.x, u.y, u.z);
 		}
 		return;
 	}
 	const int grp = lane >> 3, cor = lane & 7;
 	const int mine = cor & 1;                               /* which of the two lookups */
 	const int comp = 2 * ((cor >> 1) & 1) + (cor >> 2);     /* which component */
-	for (uint32_t k0 = 0; k0 < n_look; k0 += 8) {
-		float c8[8];     /* lookup a (k0 + grp) x y z w, lookup b (k0 + 4 + grp) x y z w */
+	const int hi2 = (cor >> 1) & 1, hi4 = cor >> 2;
+	for (uint32_t k0 = 0; k0 < n_look; k0 += 16) {
+		/* all loads first: per block b of eight lookups, the lane's own lookup
+		 * (k0 + 8 b + 4 mine + grp) in c[b][0..3], its partner's in c[b][4..7] */
+		float c[2][8];
 		uint32_t sl[2];
 		float sc[2];
 		bool ok[2];
 #pragma unroll
-		for (int h = 0; h < 2; ++h) {
-			const uint32_t k = k0 + 4 * h + grp;
-			ok[h] = k < n_look;
-			float4 d = make_float4(0.f, 0.f, 0.f, 0.f);
-			float w = 0.f;
-			sl[h] = 0;
-			sc[h] = 0.f;
-			if (ok[h]) {
-				uint32_t elem;
-				const DevIntrpl& g = lookup_grid(G, W, k, elem, sc[h]);
-				sl[h] = lookup_slot(W, k);
-				d = ldg_no_l1(g.oct + 8 * (size_t)elem + cor);
-				w = W.cw[cor][sl[h]];
+		for (int b = 0; b < 2; ++b) {
+			sl[b] = 0;
+			sc[b] = 0.f;
+			ok[b] = false;
+#pragma unroll
+			for (int h = 0; h < 2; ++h) {
+				const uint32_t k = k0 + 8 * b + 4 * (h ^ mine) + grp;
+				float4 d = make_float4(0.f, 0.f, 0.f, 0.f);
+				float w = 0.f;
+				if (k < n_look) {
+					uint32_t elem, s;
+					float scale;
+					const DevIntrpl& g = lookup_grid(G, W, k, elem, s, scale);
+					d = ldg_no_l1(g.oct + 8 * (size_t)elem + cor);
+					w = W.cw[kCornerStride * s + cor];
+					if (h == 0) { sl[b] = s; sc[b] = scale; ok[b] = true; }
+				}
+				c[b][4 * h] = fmul(d.x, w); c[b][4 * h + 1] = fmul(d.y, w);
+				c[b][4 * h + 2] = fmul(d.z, w); c[b][4 * h + 3] = fmul(d.w, w);
 			}
-			c8[4 * h] = fmul(d.x, w); c8[4 * h + 1] = fmul(d.y, w);
-			c8[4 * h + 2] = fmul(d.z, w); c8[4 * h + 3] = fmul(d.w, w);
 		}
-		/* step 1 (partner c ^ 1): keep lookup (c & 1) */
-		float m4[4];
 #pragma unroll
-		for (int j = 0; j < 4; ++j) {
-			const float keep = mine ? c8[4 + j] : c8[j];
-			const float send = mine ? c8[j] : c8[4 + j];
-			m4[j] = fadd(keep, __shfl_xor_sync(GBA_FULL_MASK, send, 1));
-		}
-		/* step 2 (partner c ^ 2): keep components {0,1} or {2,3} */
-		const int hi2 = (cor >> 1) & 1;
-		float m2[2];
+		for (int b = 0; b < 2; ++b) {
+			/* step 1 (partner c ^ 1): keep the own lookup */
+			float m4[4];
 #pragma unroll
-		for (int j = 0; j < 2; ++j) {
-			const float keep = hi2 ? m4[2 + j] : m4[j];
-			const float send = hi2 ? m4[j] : m4[2 + j];
-			m2[j] = fadd(keep, __shfl_xor_sync(GBA_FULL_MASK, send, 2));
-		}
-		/* step 3 (partner c ^ 4): keep one */
-		const int hi4 = cor >> 2;
-		const float keep = hi4 ? m2[1] : m2[0];
-		const float send = hi4 ? m2[0] : m2[1];
-		const float v = fadd(keep, __shfl_xor_sync(GBA_FULL_MASK, send, 4));
-		/* the lane's lookup, selected without indexing (keeps the arrays in registers) */
-		if (mine ? ok[1] : ok[0]) {
-			const uint32_t s = mine ? sl[1] : sl[0];
-			const float f = fmul(v, mine ? sc[1] : sc[0]);
-			C.f = fadd(C.f, f);
-			if (comp != 3) {
-				C.t0 = ffma(W.ux[s], f, C.t0);
-				C.t1 = ffma(W.uy[s], f, C.t1);
-				C.t2 = ffma(W.uz[s], f, C.t2);
+			for (int j = 0; j < 4; ++j) m4[j] = fadd(c[b][j], __shfl_xor_sync(GBA_FULL_MASK, c[b][4 + j], 1));
+			/* step 2 (partner c ^ 2): keep components {0,1} or {2,3} */
+			float m2[2];
+#pragma unroll
+			for (int j = 0; j < 2; ++j) {
+				const float keep = hi2 ? m4[2 + j] : m4[j];
+				const float send = hi2 ? m4[j] : m4[2 + j];
+				m2[j] = fadd(keep, __shfl_xor_sync(GBA_FULL_MASK, send, 2));
+			}
+			/* step 3 (partner c ^ 4): keep one */
+			const float keep = hi4 ? m2[1] : m2[0];
+			const float send = hi4 ? m2[0] : m2[1];
+			const float v = fadd(keep, __shfl_xor_sync(GBA_FULL_MASK, send, 4));
+			if (ok[b]) {
+				const float f = fmul(v, sc[b]);
+				C.f = fadd(C.f, f);
+				if (comp != 3) {
+					const float4 u = W.ut[sl[b]];
+					C.t0 = ffma(u.x, f, C.t0);
+					C.t1 = ffma(u.y, f, C.t1);
+					C.t2 = ffma(u.z, f, C.t2);
+				}
 			}
 		}
 	}
@@ -391,7 +398,7 @@ __device__ __forceinline__ bool nl_pair(const DevNL& nl, const DevParams& P, uin
 	const float dr2_inv = nl.approx_inv ? frcp_approx(dr2) : __frcp_rn(dr2);
 	dx = fmul(dx, dr2_inv); dy = fmul(dy, dr2_inv); dz = fmul(dz, dr2_inv);
 	const bool shape86 = P.potshape == GBA_POTSHAPE_8_6;
-	const size_t k = (size_t)P.num_types * (trec - 1) + (lig_type - 1);
+	const size_t k = (size_t)P.num_types * (lig_type - 1) + (trec - 1);
 	const float4 p = __ldg(&P.pair[2 * k]);
 	const float4 pl = __ldg(&P.pair[2 * k + 1]);   /* ipon, plateau force factor, plateau energy */
 	float f1x, f1y, f1z, e1;
@@ -418,6 +425,18 @@ __device__ __forceinline__ bool nl_pair(const DevNL& nl, const DevParams& P, uin
 	return true;
 }
 
+/* Pair term of flattened pair k owned by slot s (list index lbase[s] + k):
+ * adds it to S. */
+__device__ __forceinline__ void pair_term(const RigidModel& M, const WarpStage& W, uint32_t s, uint32_t j,
+		float4 r, uint32_t trec, PoseSums& S) {
+	const float4 b = W.pq[s];
+	const float4 u = W.ut[s];
+	float fx, fy, fz, e;
+	if (nl_pair(M.grid.nl, M.par, __float_as_uint(u.w), b.w, b.x, b.y, b.z, r.x, r.y, r.z, r.w, trec, fx, fy,
+			fz, e))
+		S.add(e, fx, fy, fz, u.x, u.y, u.z);
+}
+
 /* res: E, force xyz, Euler gradient xyz (Result_6D order); identical on all
  * lanes.  W is this warp's shared staging area. */
 template <bool CENSUS>
@@ -432,12 +451,14 @@ __device__ __forceinline__ void eval_pose_rigid(const RigidModel& M, float tx, f
 		float ttx, tty, ttz;
 		const PoseRot R = get_pose(W, ttx, tty, ttz);
 		uint32_t nlk[2], nln[2];
+		BeadGrid bg[2];
 #pragma unroll
 		for (int h = 0; h < 2; ++h) {
 			const int s = lane + 32 * h;
 			const uint32_t i = i0 + s;
 			nlk[h] = 0;
 			nln[h] = 0;
+			bg[h] = BeadGrid{0u, 0u};
 			bool in_nl = false;
 			if (i < M.lig.n) {
 				const float4 b = __ldg(&M.lig.xyzq[i]);
@@ -446,11 +467,8 @@ __device__ __forceinline__ void eval_pose_rigid(const RigidModel& M, float tx, f
 				float px, py, pz;
 				rot_apply(R.m, b.x, b.y, b.z, px, py, pz);
 				px = fadd(px, ttx); py = fadd(py, tty); pz = fadd(pz, ttz);
-				W.ux[s] = b.x; W.uy[s] = b.y; W.uz[s] = b.z;
-				W.px[s] = px; W.py[s] = py; W.pz[s] = pz;
-				W.q[s] = b.w;
-				W.type[s] = type;
-				nlk[h] = stage_grid(M.grid, px, py, pz, mapped, b.w, s, W);
+				put_bead(W, s, b.x, b.y, b.z, px, py, pz, b.w, type);
+				nlk[h] = stage_grid(M.grid, px, py, pz, mapped, b.w, s, W, bg[h]);
 				if (type != 0) nln[h] = stage_nl(M.grid.nl, px, py, pz, s, W, in_nl);
 			}
 			if (CENSUS) {
@@ -460,7 +478,7 @@ __device__ __forceinline__ void eval_pose_rigid(const RigidModel& M, float tx, f
 				c_ent += nln[h];
 			}
 		}
-		const uint32_t n_look = queue_lookups(W, nlk, lane);
+		const uint32_t n_look = queue_lookups(W, nlk, bg, lane);
 		uint32_t start[2];
 		const uint32_t n_pair = queue_pairs(W, nln, lane, start);
 		__syncwarp();
@@ -468,9 +486,9 @@ __device__ __forceinline__ void eval_pose_rigid(const RigidModel& M, float tx, f
 		/* 2. grid lookups */
 		drain_lookups(M.grid, W, n_look, lane, S, C);
 
-		/* 3. neighbour pairs, one per lane; two per lane and iteration so that
-		 * both gather chains (list entry -> receptor bead -> parameters) are
-		 * in flight together */
+		/* 3. neighbour pairs, two per lane and window so that both gather
+		 * chains (list entry -> receptor bead -> parameters) are in flight
+		 * together */
 		PairWindow win;
 		for (uint32_t w = 0; w < n_pair; w += 64) {
 			const uint32_t k = w + lane, k2 = k + 32;
@@ -478,19 +496,14 @@ __device__ __forceinline__ void eval_pose_rigid(const RigidModel& M, float tx, f
 			win.owners(W, w, start, nln, lane, sa, sb);
 			if (k >= n_pair) continue;
 			const bool has2 = k2 < n_pair;
-			const uint32_t ja = __ldg(&M.grid.nl.list[W.nl_idx[sa] + (k - W.nl_pre[sa])]);
-			const uint32_t jb = has2 ? __ldg(&M.grid.nl.list[W.nl_idx[sb] + (k2 - W.nl_pre[sb])]) : ja;
+			const uint32_t ja = __ldg(&M.grid.nl.list[W.lbase[sa] + k]);
+			const uint32_t jb = has2 ? __ldg(&M.grid.nl.list[W.lbase[sb] + k2]) : ja;
 			const float4 ra = __ldg(&M.rec.xyzq[ja]);
 			const float4 rb = __ldg(&M.rec.xyzq[jb]);
 			const uint32_t ta = __ldg(&M.rec.tm[ja]) & 0xffffu;
 			const uint32_t tb = __ldg(&M.rec.tm[jb]) & 0xffffu;
-			float fx, fy, fz, e;
-			if (nl_pair(M.grid.nl, M.par, W.type[sa], W.q[sa], W.px[sa], W.py[sa], W.pz[sa], ra.x, ra.y,
-					ra.z, ra.w, ta, fx, fy, fz, e))
-				S.add(e, fx, fy, fz, W.ux[sa], W.uy[sa], W.uz[sa]);
-			if (has2 && nl_pair(M.grid.nl, M.par, W.type[sb], W.q[sb], W.px[sb], W.py[sb], W.pz[sb], rb.x,
-					rb.y, rb.z, rb.w, tb, fx, fy, fz, e))
-				S.add(e, fx, fy, fz, W.ux[sb], W.uy[sb], W.uz[sb]);
+			pair_term(M, W, sa, ja, ra, ta, S);
+			if (has2) pair_term(M, W, sb, jb, rb, tb, S);
 		}
 		__syncwarp();
 	}

@@ -13,13 +13,14 @@
  *      the bead's geometry goes to per-warp shared memory and each bead
  *      enqueues one grid lookup per channel it reads (type, and charge when
  *      |q| > 0.001) and its NL list length;
- *   2. the warp drains the lookup queue: one lookup per lane (8 gathered
+ *   2. the warp drains the flattened (bead, neighbour) pair list in windows
+ *      of 64 pairs, two per lane (owners from per-window start masks);
+ *   3. the warp drains the lookup queue: one lookup per lane (8 gathered
  *      float4 corners), or with the octet layout and GBA_KOPT_COOP_LOOKUP
  *      eight lanes per lookup, one corner each (one 128-byte line per
- *      lookup, four lookups per warp instruction, loaded without L1
- *      allocation so that L1 keeps the receptor and parameter data);
- *   3. the warp drains the flattened (bead, neighbour) pair list, one pair
- *      per lane (owner found by binary search over the 64 prefix sums).
+ *      lookup, sixteen lookups per step, loaded without L1 allocation so
+ *      that L1 keeps the receptor and parameter data).  Pairs come first:
+ *      measured on GB300, this order is faster.
  * Every lookup and pair contributes straight to the pose sums: energy,
  * force and the torque matrix sum_i x_i (x) f_i are linear in the bead
  * forces, so no per-bead force is kept.  The warp then reduces with
@@ -301,30 +302,22 @@ struct CoopSums {
  * order, so both forms give the same value per lookup.  Each lane loads its
  * own lookup first, which makes the first step select-free.  The lane scales
  * the component and adds it to its CoopSums role. */
-__device__ __forceinline__ void drain_lookups(const DevGrid& G, const WarpStage& W, uint32_t n_look,
-		int lane, PoseSums& S, CoopSums& C) {
-	if (!G.coop_lookup) {
-		for (uint32_t k = lane; k < n_look; k += 32) {
-			const uint32_t s = lookup_slot(W, k);
-			const float4 v = grid_lookup(G, W, k);
-			const float4 u = W.ut[s];
-			S.add(v.w, v.x, v.y, v.z, u.x, u.y, u.z);
-		}
-		return;
-	}
-	const int grp = lane >> 3, cor = lane & 7;
-	const int mine = cor & 1;                               /* which of the two lookups */
-	const int comp = 2 * ((cor >> 1) & 1) + (cor >> 2);     /* which component */
-	const int hi2 = (cor >> 1) & 1, hi4 = cor >> 2;
-	for (uint32_t k0 = 0; k0 < n_look; k0 += 16) {
-		/* all loads first: per block b of eight lookups, the lane's own lookup
-		 * (k0 + 8 b + 4 mine + grp) in c[b][0..3], its partner's in c[b][4..7] */
-		float c[2][8];
-		uint32_t sl[2];
-		float sc[2];
-		bool ok[2];
+/* One cooperative step of drain_lookups: the loads and the reduce-scatter of
+ * lookups k0 .. k0 + 8 NB - 1, kept apart so that other work can run between
+ * them. */
+template <int NB>
+struct CoopStep {
+	float c[NB][8];   /* per block b: own lookup x y z w, partner's x y z w */
+	uint32_t sl[NB];
+	float sc[NB];
+	bool ok[NB];
+
+	/* block b, lane (g, c): own lookup k0 + 8 b + 4 mine + g, then the partner's */
+	__device__ __forceinline__ void load(const DevGrid& G, const WarpStage& W, uint32_t k0, uint32_t n_look,
+			int lane) {
+		const int grp = lane >> 3, cor = lane & 7, mine = cor & 1;
 #pragma unroll
-		for (int b = 0; b < 2; ++b) {
+		for (int b = 0; b < NB; ++b) {
 			sl[b] = 0;
 			sc[b] = 0.f;
 			ok[b] = false;
@@ -345,8 +338,14 @@ __device__ __forceinline__ void drain_lookups(const DevGrid& G, const WarpStage&
 				c[b][4 * h + 2] = fmul(d.z, w); c[b][4 * h + 3] = fmul(d.w, w);
 			}
 		}
+	}
+
+	__device__ __forceinline__ void reduce(const WarpStage& W, int lane, CoopSums& C) const {
+		const int cor = lane & 7;
+		const int comp = 2 * ((cor >> 1) & 1) + (cor >> 2);     /* which component */
+		const int hi2 = (cor >> 1) & 1, hi4 = cor >> 2;
 #pragma unroll
-		for (int b = 0; b < 2; ++b) {
+		for (int b = 0; b < NB; ++b) {
 			/* step 1 (partner c ^ 1): keep the own lookup */
 			float m4[4];
 #pragma unroll
@@ -374,6 +373,24 @@ __device__ __forceinline__ void drain_lookups(const DevGrid& G, const WarpStage&
 				}
 			}
 		}
+	}
+};
+
+__device__ __forceinline__ void drain_lookups(const DevGrid& G, const WarpStage& W, uint32_t n_look,
+		int lane, PoseSums& S, CoopSums& C) {
+	if (!G.coop_lookup) {
+		for (uint32_t k = lane; k < n_look; k += 32) {
+			const uint32_t s = lookup_slot(W, k);
+			const float4 v = grid_lookup(G, W, k);
+			const float4 u = W.ut[s];
+			S.add(v.w, v.x, v.y, v.z, u.x, u.y, u.z);
+		}
+		return;
+	}
+	for (uint32_t k0 = 0; k0 < n_look; k0 += 16) {
+		CoopStep<2> st;
+		st.load(G, W, k0, n_look, lane);
+		st.reduce(W, lane, C);
 	}
 }
 
@@ -483,10 +500,7 @@ __device__ __forceinline__ void eval_pose_rigid(const RigidModel& M, float tx, f
 		const uint32_t n_pair = queue_pairs(W, nln, lane, start);
 		__syncwarp();
 
-		/* 2. grid lookups */
-		drain_lookups(M.grid, W, n_look, lane, S, C);
-
-		/* 3. neighbour pairs, two per lane and window so that both gather
+		/* 2. neighbour pairs, two per lane and window so that both gather
 		 * chains (list entry -> receptor bead -> parameters) are in flight
 		 * together */
 		PairWindow win;
@@ -505,6 +519,9 @@ __device__ __forceinline__ void eval_pose_rigid(const RigidModel& M, float tx, f
 			pair_term(M, W, sa, ja, ra, ta, S);
 			if (has2) pair_term(M, W, sb, jb, rb, tb, S);
 		}
+
+		/* 3. grid lookups */
+		drain_lookups(M.grid, W, n_look, lane, S, C);
 		__syncwarp();
 	}
 	fold_coop(C, S, lane);

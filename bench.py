@@ -388,9 +388,9 @@ def main():
                          "and keep the fastest")
     ap.add_argument("--rec-beads", type=int, default=None,
                     help="smaller receptor with config 1's distributions (profiling captures)")
-    ap.add_argument("--kopts", type=int, default=7,
+    ap.add_argument("--kopts", type=int, default=15,
                     help="kernel options (GBA_KOPT_*: 1 computed ratio, 2 cooperative lookup, "
-                         "4 four blocks per SM)")
+                         "4 four blocks per SM, 8 typed neighbour list)")
     ap.add_argument("--batch-scale", type=float, default=0.05,
                     help="fraction of config 4's pose counts used by --suite full")
     args = ap.parse_args()

@@ -456,7 +456,8 @@ int gba_kernel_time(gba_ctx* ctx, double* ms_total, uint64_t* launches, int32_t 
 int gba_set_kernel_options(gba_ctx* ctx, uint32_t flags) {
 	if (!ctx) return GBA_ERR_INVALID_ARGUMENT;
 	GBA_API_BEGIN
-	if (flags & ~(uint32_t)(GBA_KOPT_RATIO_COMPUTED | GBA_KOPT_COOP_LOOKUP | GBA_KOPT_FOUR_BLOCKS))
+	if (flags & ~(uint32_t)(GBA_KOPT_RATIO_COMPUTED | GBA_KOPT_COOP_LOOKUP | GBA_KOPT_FOUR_BLOCKS |
+			GBA_KOPT_TYPED_LIST))
 		throw ApiError(GBA_ERR_INVALID_ARGUMENT, "gba_set_kernel_options: unknown flag");
 	ctx->bind();
 	Lock g(ctx->stage_mu);
@@ -481,6 +482,10 @@ int gba_release(gba_ctx* ctx, gba_id id) {
 	auto it = ctx->items.find(id);
 	if (it == ctx->items.end())
 		throw ApiError(GBA_ERR_UNKNOWN_ID, "gba_release: unknown id " + std::to_string(id));
+	if (it->second->kind == ItemKind::Protein)
+		for (auto& kv : ctx->items)
+			if (kv.second->kind == ItemKind::Grid)
+				static_cast<GridItem*>(kv.second.get())->typed_lists.erase(id);
 	ctx->items.erase(it);
 	ctx->model_cache.clear();
 	ctx->clear_graphs();
@@ -572,7 +577,7 @@ int gba_census_6d(gba_ctx* ctx, gba_id rec, gba_id lig, gba_id grid, gba_id para
 
 namespace gba {
 
-RigidLaunch Context::rigid_launch(gba_id rec, gba_id lig, gba_id grid, gba_id params) {
+RigidLaunch Context::rigid_launch(gba_id rec, gba_id lig, gba_id grid, gba_id params, bool may_allocate) {
 	Lock g(mu);
 	auto* R = static_cast<ProteinItem*>(find(rec, ItemKind::Protein));
 	auto* Lg = static_cast<ProteinItem*>(find(lig, ItemKind::Protein));
@@ -586,7 +591,44 @@ RigidLaunch Context::rigid_launch(gba_id rec, gba_id lig, gba_id grid, gba_id pa
 	L.m.par = P->dev;
 	L.m.par.pair = P->pair_table(G->dev.nl.dPlateau2);
 	L.bound4 = (kernel_opts & GBA_KOPT_FOUR_BLOCKS) ? 1 : 0;
+	if (kernel_opts & GBA_KOPT_TYPED_LIST)
+		L.m.grid.nl.typed_list = typed_list(*G, rec, *R, may_allocate);
 	return L;
+}
+
+namespace {
+
+/* out[k] = list[k] | type(list[k]) << 24 */
+__global__ void typed_list_kernel(const uint32_t* __restrict__ list, size_t n, const uint32_t* __restrict__ tm,
+		uint32_t* __restrict__ out) {
+	for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x) {
+		const uint32_t j = list[k];
+		out[k] = j | (tm[j] & 0xffu) << 24;
+	}
+}
+
+}  // namespace
+
+const uint32_t* Context::typed_list(GridItem& G, gba_id rec_id, const ProteinItem& R, bool may_allocate) {
+	const size_t n = G.nl_desc.numEl;
+	if (n == 0 || R.max_type > 255 || R.dev.n > (1u << 24)) return nullptr;
+	auto it = G.typed_lists.find(rec_id);
+	if (it != G.typed_lists.end()) return (const uint32_t*)it->second.ptr;
+	if (!may_allocate) return nullptr;
+	it = G.typed_lists.try_emplace(rec_id).first;
+	try {
+		it->second.alloc(n * sizeof(uint32_t));
+		/* list indices were checked against the receptor size (validate_pair) */
+		const int threads = 256;
+		const size_t blocks = std::min<size_t>((n + threads - 1) / threads, (size_t)num_sms * 32);
+		typed_list_kernel<<<(unsigned)blocks, threads>>>(G.dev.nl.list, n, R.dev.tm, (uint32_t*)it->second.ptr);
+		check_cuda(cudaGetLastError(), "typed list launch");
+		check_cuda(cudaDeviceSynchronize(), "typed list");
+	} catch (...) {
+		G.typed_lists.erase(it);
+		throw;
+	}
+	return (const uint32_t*)it->second.ptr;
 }
 
 DevGrid Context::apply_kernel_options(DevGrid g) const {

@@ -103,6 +103,8 @@ struct GridItem : Item {
 	 * builder's nl_cutoff, or for uploaded grids the least radius the
 	 * reference's NL term relies on (plateau + half a voxel diagonal) */
 	double nl_list_radius = 0.0;
+	/* per receptor id: the list with that receptor's bead types in bits 24..31 */
+	std::map<gba_id, DevBuffer> typed_lists;
 };
 
 struct ParamsItem : Item {
@@ -191,7 +193,12 @@ struct Context {
 	void run_minimize(MinLaunch& L, cudaStream_t s, int32_t* status_out);
 	void clear_graphs();
 
-	RigidLaunch rigid_launch(gba_id rec, gba_id lig, gba_id grid, gba_id params);
+	/* may_allocate = false: the typed list is used only if it already exists
+	 * (gba_energy_6d_noalloc) */
+	RigidLaunch rigid_launch(gba_id rec, gba_id lig, gba_id grid, gba_id params, bool may_allocate = true);
+	/* the grid's typed list for receptor `rec_id` (built on first use), or
+	 * nullptr when the receptor's types or indices do not fit */
+	const uint32_t* typed_list(GridItem& g, gba_id rec_id, const ProteinItem& rec, bool may_allocate);
 	void validate_pair(const ProteinItem& rec, const ProteinItem& lig, const GridItem& g,
 			const ParamsItem& p);
 	void run_rigid(RigidLaunch& L, cudaStream_t s);

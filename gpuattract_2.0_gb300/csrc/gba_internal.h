@@ -62,6 +62,9 @@ struct DevNL {
 	int ratio_computed;
 	/* plateau below 50 A: the pair term may use the hardware reciprocal */
 	int approx_inv;
+	/* optional: list[] with the receptor bead's type in bits 24..31 (set per
+	 * launch for one receptor; nullptr: the type is gathered per pair) */
+	const uint32_t* typed_list;
 };
 
 struct DevGrid {

@@ -68,7 +68,7 @@ extern "C" int gba_energy_6d_noalloc(gba_ctx* ctx, gba_id rec, gba_id lig, gba_i
 		if (!is_device_pointer(dofs) || !is_device_pointer(out))
 			throw ApiError(GBA_ERR_INVALID_ARGUMENT, "gba_energy_6d_noalloc: device pointers required");
 		void* scratch = noalloc_scratch(ctx->device);
-		RigidLaunch L = ctx->rigid_launch(rec, lig, grid, params);
+		RigidLaunch L = ctx->rigid_launch(rec, lig, grid, params, false);
 		cudaStream_t s = (cudaStream_t)stream;
 		L.n = n;
 		L.dofs = dofs;

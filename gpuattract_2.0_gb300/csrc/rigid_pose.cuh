@@ -442,10 +442,10 @@ __device__ __forceinline__ bool nl_pair(const DevNL& nl, const DevParams& P, uin
 	return true;
 }
 
-/* Pair term of flattened pair k owned by slot s (list index lbase[s] + k):
- * adds it to S. */
-__device__ __forceinline__ void pair_term(const RigidModel& M, const WarpStage& W, uint32_t s, uint32_t j,
-		float4 r, uint32_t trec, PoseSums& S) {
+/* Pair term of a flattened pair owned by slot s against receptor bead record
+ * r (x, y, z, q) of type trec: adds it to S. */
+__device__ __forceinline__ void pair_term(const RigidModel& M, const WarpStage& W, uint32_t s, float4 r,
+		uint32_t trec, PoseSums& S) {
 	const float4 b = W.pq[s];
 	const float4 u = W.ut[s];
 	float fx, fy, fz, e;
@@ -510,14 +510,28 @@ __device__ __forceinline__ void eval_pose_rigid(const RigidModel& M, float tx, f
 			win.owners(W, w, start, nln, lane, sa, sb);
 			if (k >= n_pair) continue;
 			const bool has2 = k2 < n_pair;
-			const uint32_t ja = __ldg(&M.grid.nl.list[W.lbase[sa] + k]);
-			const uint32_t jb = has2 ? __ldg(&M.grid.nl.list[W.lbase[sb] + k2]) : ja;
-			const float4 ra = __ldg(&M.rec.xyzq[ja]);
-			const float4 rb = __ldg(&M.rec.xyzq[jb]);
-			const uint32_t ta = __ldg(&M.rec.tm[ja]) & 0xffffu;
-			const uint32_t tb = __ldg(&M.rec.tm[jb]) & 0xffffu;
-			pair_term(M, W, sa, ja, ra, ta, S);
-			if (has2) pair_term(M, W, sb, jb, rb, tb, S);
+			const uint32_t ia = W.lbase[sa] + k;
+			const uint32_t ib = has2 ? W.lbase[sb] + k2 : ia;
+			float4 ra, rb;
+			uint32_t ta, tb;
+			if (M.grid.nl.typed_list) {
+				/* entries carry the receptor type: one gather less per pair */
+				const uint32_t ea = __ldg(&M.grid.nl.typed_list[ia]);
+				const uint32_t eb = __ldg(&M.grid.nl.typed_list[ib]);
+				ra = __ldg(&M.rec.xyzq[ea & 0xffffffu]);
+				rb = __ldg(&M.rec.xyzq[eb & 0xffffffu]);
+				ta = ea >> 24;
+				tb = eb >> 24;
+			} else {
+				const uint32_t ja = __ldg(&M.grid.nl.list[ia]);
+				const uint32_t jb = __ldg(&M.grid.nl.list[ib]);
+				ra = __ldg(&M.rec.xyzq[ja]);
+				rb = __ldg(&M.rec.xyzq[jb]);
+				ta = __ldg(&M.rec.tm[ja]) & 0xffffu;
+				tb = __ldg(&M.rec.tm[jb]) & 0xffffu;
+			}
+			pair_term(M, W, sa, ra, ta, S);
+			if (has2) pair_term(M, W, sb, rb, tb, S);
 		}
 
 		/* 3. grid lookups */

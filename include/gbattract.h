@@ -165,13 +165,23 @@ int gba_set_pose_order(gba_ctx* ctx, int enable);
  *                            8 lanes share one grid lookup, one corner each,
  *                            loaded without L1 allocation;
  *   GBA_KOPT_FOUR_BLOCKS     the scoring kernel is compiled for four resident
- *                            256-thread blocks per SM (64 registers a thread).
- * The default is all three.  Changing options drops the cached minimizer
+ *                            256-thread blocks per SM (64 registers a thread);
+ *   GBA_KOPT_TYPED_LIST      the rigid kernels read a copy of the neighbour
+ *                            list whose entries carry the receptor bead's
+ *                            type in their top 8 bits (built on the device at
+ *                            the first use of a grid with a receptor, 4 bytes
+ *                            per list entry, kept with the grid until either
+ *                            is released) instead of gathering the type per
+ *                            pair.  Receptors with types above 255 or 2^24
+ *                            beads or more keep the gather.
+ * The default is all four.  Changing options drops the cached minimizer
  * graphs. */
 #define GBA_KOPT_RATIO_COMPUTED 1u
 #define GBA_KOPT_COOP_LOOKUP    2u
 #define GBA_KOPT_FOUR_BLOCKS    4u
-#define GBA_KOPT_DEFAULT        (GBA_KOPT_RATIO_COMPUTED | GBA_KOPT_COOP_LOOKUP | GBA_KOPT_FOUR_BLOCKS)
+#define GBA_KOPT_TYPED_LIST     8u
+#define GBA_KOPT_DEFAULT        (GBA_KOPT_RATIO_COMPUTED | GBA_KOPT_COOP_LOOKUP | GBA_KOPT_FOUR_BLOCKS | \
+                                 GBA_KOPT_TYPED_LIST)
 int gba_set_kernel_options(gba_ctx* ctx, uint32_t flags);
 
 /* While enabled, CUDA events are recorded on the launching stream around

@@ -132,10 +132,37 @@ def test_octet_layout_does_not_change_results(small_case, ctx):
         ctx.grid_octets(ids[2], False)
         s2, r2, n2 = ctx.minimize_6d(*ids, wl.dofs[:32], max_evals=30)
     finally:
-        ctx.set_kernel_options(7)
+        ctx.set_kernel_options(15)
         ctx.grid_octets(ids[2], False)
     assert np.array_equal(native, octets)
     assert np.array_equal(r1, r2) and np.array_equal(s1, s2)
+
+
+def test_typed_list_is_bitwise_the_gather(small_case, pkg, ctx):
+    """GBA_KOPT_TYPED_LIST reads the receptor type from a per-receptor copy of
+    the neighbour list: results are bit-identical to gathering the type per
+    pair, for scoring and minimization, and the copies are kept per receptor
+    (a second receptor on the same grid gets its own)."""
+    wl, grid = small_case
+    rec, lig, g, p = upload(ctx, wl.rec, wl.lig, grid, wl.params)
+    moved = pkg.Protein(xyz=wl.rec.xyz + np.float32(0.37), type=wl.rec.type,
+                        mapped=wl.rec.mapped, charge=wl.rec.charge[::-1].copy())
+    rec2 = ctx.upload_protein(moved)
+    out = {}
+    try:
+        for flags in (7, 15):
+            ctx.set_kernel_options(flags)
+            out[flags] = (ctx.energy_6d(rec, lig, g, p, wl.dofs),
+                          ctx.energy_6d(rec2, lig, g, p, wl.dofs),
+                          ctx.minimize_6d(rec, lig, g, p, wl.dofs[:16], max_evals=30)[1])
+        ctx.release(rec2)
+        again = ctx.energy_6d(rec, lig, g, p, wl.dofs)
+    finally:
+        ctx.set_kernel_options(15)
+    for a, b in zip(out[7], out[15]):
+        assert np.array_equal(a, b)
+    assert not np.array_equal(out[15][0], out[15][1])
+    assert np.array_equal(again, out[15][0])
 
 
 def test_errors(small_case, pkg, ctx):
@@ -172,7 +199,7 @@ def test_fp64_error_statement(small_case, oracle, ctx):
     assert float(eE.max()) < 1e-3
 
 
-@pytest.mark.parametrize("flags", [0, 1, 2, 4, 7])
+@pytest.mark.parametrize("flags", [0, 1, 2, 4, 7, 8, 15])
 def test_kernel_options_keep_parity(small_case, oracle, ctx, flags):
     """Each GBA_KOPT_* combination stays within the parity bound; grid and NL
     decisions are unaffected (census identical)."""
@@ -188,7 +215,7 @@ def test_kernel_options_keep_parity(small_case, oracle, ctx, flags):
         s, r, n = ctx.minimize_6d(*ids, wl.dofs[:16], max_evals=20)
         assert np.array_equal(ctx.energy_6d(*ids, s), r)
     finally:
-        ctx.set_kernel_options(7)        # GBA_KOPT_DEFAULT
+        ctx.set_kernel_options(15)       # GBA_KOPT_DEFAULT
         ctx.grid_octets(ids[2], False)
     for e in pose_errors(got, ref, st):
         assert float(e.max()) <= RTOL

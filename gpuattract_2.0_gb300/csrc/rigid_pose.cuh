@@ -402,43 +402,74 @@ __device__ __forceinline__ void fold_coop(const CoopSums& C, PoseSums& S, int la
 
 /* One NL pair term (plateau-subtracted LJ + Coulomb), the body of the
  * neighbour loop of src/model/neighborlist.h:70-158.  Returns false when
- * the pair lies outside the plateau. */
+ * the pair lies outside the plateau.
+ *
+ * Every force the reference adds for a pair -- LJPotForce at r, minus
+ * LJPotForce at the plateau along the same direction, ChargePotForce at r,
+ * minus ChargePotForce at the plateau (src/model/neighborlist.h:105-141,
+ * src/model/forcefield.h:30-146) -- is a scalar times d / r^2 (the plateau
+ * terms use ratio * d / r^2).  The scalars are summed first and the
+ * direction is applied once: the same force up to rounding order.  Every
+ * decision (plateau test, rmin2 branch, ratio bin, Coulomb switches) uses
+ * the reference's quantities computed in the reference's order. */
 __device__ __forceinline__ bool nl_pair(const DevNL& nl, const DevParams& P, uint32_t lig_type,
 		float qlig, float px, float py, float pz, float rx, float ry, float rz, float rq,
 		uint32_t trec, float& fx, float& fy, float& fz, float& e) {
-	float dx = fsub(px, rx), dy = fsub(py, ry), dz = fsub(pz, rz);
+	const float dx = fsub(px, rx), dy = fsub(py, ry), dz = fsub(pz, rz);
 	const float dr2 = fadd(fadd(fmul(dx, dx), fmul(dy, dy)), fmul(dz, dz));
 	if (!(dr2 <= nl.dPlateau2) || trec == 0) return false;
 	/* 1/r^2 only scales smooth terms: its one decision, the Coulomb cutoff
 	 * at 1/r^2 = 1/50^2 (src/model/forcefield.h:104-113), lies outside any
 	 * plateau below 50 A, where nl.approx_inv allows the hardware reciprocal */
 	const float dr2_inv = nl.approx_inv ? frcp_approx(dr2) : __frcp_rn(dr2);
-	dx = fmul(dx, dr2_inv); dy = fmul(dy, dr2_inv); dz = fmul(dz, dr2_inv);
 	const bool shape86 = P.potshape == GBA_POTSHAPE_8_6;
 	const size_t k = (size_t)P.num_types * (lig_type - 1) + (trec - 1);
 	const float4 p = __ldg(&P.pair[2 * k]);
 	const float4 pl = __ldg(&P.pair[2 * k + 1]);   /* ipon, plateau force factor, plateau energy */
-	float f1x, f1y, f1z, e1;
-	lj_pot_force(dr2, dr2_inv, dx, dy, dz, p, pl.x, shape86, f1x, f1y, f1z, e1);
+	/* LJPotForce: energy and the radial factor fb (force = fb * d / r^2) */
+	const float rr23 = fmul(fmul(dr2_inv, dr2_inv), dr2_inv);
+	const float rep = fmul(p.x, shape86 ? dr2_inv : rr23);
+	const float vlj = fmul(fsub(rep, p.y), rr23);
+	float fb = ffma(6.0f, vlj, fmul(shape86 ? 2.0f : 6.0f, fmul(rep, rr23)));
+	if (dr2 < p.z) {
+		e = ffma(fsub(pl.x, 1.0f), p.w, vlj);
+	} else {
+		e = fmul(pl.x, vlj);
+		fb = fmul(pl.x, fb);
+	}
 	/* getRatio's table bin, src/model/NLGrid.h:141-143 */
 	const int bin = (int)fmul(dr2, 10000.0f);
 	const float ratio = nl.ratio_computed
 			? fsqrt_approx(fmul(fadd((float)bin, 0.5f), nl.ratio_scale))
 			: __ldg(&nl.ratio[bin]);
-	const float rdx = fmul(ratio, dx), rdy = fmul(ratio, dy), rdz = fmul(ratio, dz);
-	/* LJPotForce at the plateau along the same direction: the per-type-pair
-	 * factor and energy come precomputed with the table */
-	fx = fsub(f1x, fmul(pl.y, rdx)); fy = fsub(f1y, fmul(pl.y, rdy)); fz = fsub(f1z, fmul(pl.y, rdz));
-	e = fsub(e1, pl.z);
+	/* minus LJPotForce at the plateau (per type pair, precomputed) */
+	float s = ffma(-pl.y, ratio, fb);
+	e = fsub(e, pl.z);
 	const float qq = fmul(fmul(qlig, rq), P.ffelec);
 	if (fabsf(qq) > 0.001f) {
-		const bool cdiel = P.dielec == GBA_DIELEC_CONSTANT;
-		float c1x, c1y, c1z, c1e, c2x, c2y, c2z, c2e;
-		charge_pot_force(dr2_inv, dx, dy, dz, qq, cdiel, c1x, c1y, c1z, c1e);
-		charge_pot_force(nl.dPlateau2_inv, rdx, rdy, rdz, qq, cdiel, c2x, c2y, c2z, c2e);
-		fx = fadd(fx, fsub(c1x, c2x)); fy = fadd(fy, fsub(c1y, c2y)); fz = fadd(fz, fsub(c1z, c2z));
-		e = fadd(e, fsub(c1e, c2e));
+		/* ChargePotForce at r minus at the plateau: energy qq * dd when
+		 * dd > 0, radial factor 2 qq / r^2 (distance-dependent dielectric)
+		 * or qq / r (constant dielectric) */
+		float d1, f1, d2, f2;
+		if (P.dielec == GBA_DIELEC_CONSTANT) {
+			const float sr = __fsqrt_rn(dr2_inv), sp = __fsqrt_rn(nl.dPlateau2_inv);
+			d1 = fsub(sr, 0.02f); f1 = sr;
+			d2 = fsub(sp, 0.02f); f2 = sp;
+		} else {
+			d1 = fsub(dr2_inv, 4.0e-4f); f1 = fmul(2.0f, dr2_inv);
+			d2 = fsub(nl.dPlateau2_inv, 4.0e-4f); f2 = fmul(2.0f, nl.dPlateau2_inv);
+		}
+		if (d1 > 0.0f) {
+			e = fadd(e, fmul(qq, d1));
+			s = ffma(qq, f1, s);
+		}
+		if (d2 > 0.0f) {
+			e = fsub(e, fmul(qq, d2));
+			s = ffma(-fmul(qq, f2), ratio, s);
+		}
 	}
+	const float sr2 = fmul(s, dr2_inv);
+	fx = fmul(sr2, dx); fy = fmul(sr2, dy); fz = fmul(sr2, dz);
 	return true;
 }
 

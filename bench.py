@@ -272,11 +272,15 @@ def bench_modes(ctx, pkg, n_poses: int, steps: int):
     t0 = time.perf_counter()
     _, r2, _ = ctx.minimize_6d_modes_plain(*ids, sub, max_evals=steps)
     dt_plain = time.perf_counter() - t0
+    e0 = out[: len(sub), 0].cpu().numpy()
     res = {"workload": f"config 2: receptor {wl.rec.n} / ligand {wl.lig.n} beads, 5+5 modes; "
                        f"{len(wl.dofs)} poses scored, {len(sub)} minimized (maxFunEval {steps})",
            "energy_evals_per_s": evals, "minimize_device_poses_per_s": len(sub) / dt_dev,
            "minimize_plain_poses_per_s": len(sub) / dt_plain, "speedup": dt_plain / dt_dev,
-           "device_equals_plain": bool(np.array_equal(r1, r2)), "evals_per_pose_mean": float(n1.mean())}
+           "device_equals_plain": bool(np.array_equal(r1, r2, equal_nan=True)),
+           "evals_per_pose_mean": float(n1.mean()),
+           "start_E_median": float(np.median(e0)), "minimized_E_median": float(np.median(r1[:, 0])),
+           "lowered_fraction": float(np.mean(r1[:, 0] < e0))}
     for i in (gr, gl, lig, rec, par):
         ctx.release(i)
     return res

@@ -341,8 +341,9 @@ __global__ void __launch_bounds__(256) minimize_modes_kernel(const ModesMinLaunc
 			if (lane == 0) {
 				double g[6 + 2 * GBA_MODES_MAX];
 				for (int k = 0; k < 3; ++k) { g[k] = -(double)res[4 + k]; g[3 + k] = -(double)res[1 + k]; }
-				for (uint32_t m = 0; m < Mr; ++m) g[6 + m] = -(double)res[7 + m];
-				for (uint32_t m = 0; m < Ml; ++m) g[6 + Mr + m] = -(double)res[17 + m];
+				/* mode entries are gradients already (reduceModeForce) */
+				for (uint32_t m = 0; m < Mr; ++m) g[6 + m] = (double)res[7 + m];
+				for (uint32_t m = 0; m < Ml; ++m) g[6 + Mr + m] = (double)res[17 + m];
 				va.provide((double)res[0], g);
 				done = va.done();
 			}

@@ -485,8 +485,9 @@ int gba_minimize_6d_modes_plain(gba_ctx* ctx, gba_id rec, gba_id lig, gba_id gri
 			++nev[p];
 			double g[6 + 2 * GBA_MODES_MAX];
 			for (int a = 0; a < 3; ++a) { g[a] = -(double)r.rigid.ang[a]; g[3 + a] = -(double)r.rigid.pos[a]; }
-			for (int m = 0; m < Mr; ++m) g[6 + m] = -(double)r.modesRec[m];
-			for (int m = 0; m < Ml; ++m) g[6 + Mr + m] = -(double)r.modesLig[m];
+			/* mode entries are gradients already (reduceModeForce) */
+			for (int m = 0; m < Mr; ++m) g[6 + m] = (double)r.modesRec[m];
+			for (int m = 0; m < Ml; ++m) g[6 + Mr + m] = (double)r.modesLig[m];
 			va[p].provide((double)r.rigid.E, g);
 			if (!va[p].done()) next.push_back(p);
 		}

@@ -171,10 +171,13 @@ class Workload:
     modes: bool = False
 
 
+# Shells as the workload descriptions state them (configs 0, 1, 3).  Config 2
+# states none: its globules (radii 28.8 and 21.6 A) touch at about 50 A, so
+# its centres lie on a 45-55 A shell, around contact.
 CONFIGS = {
     0: dict(rec=500, lig=200, poses=1000, shell=(35.0, 45.0), steps=100),
     1: dict(rec=2000, lig=700, poses=100_000, shell=(40.0, 55.0), steps=0),
-    2: dict(rec=1500, lig=600, poses=50_000, shell=(35.0, 45.0), steps=200, modes=5),
+    2: dict(rec=1500, lig=600, poses=50_000, shell=(45.0, 55.0), steps=200, modes=5),
     3: dict(rec=2000, lig=700, poses=10_000, shell=(40.0, 55.0), steps=0),
 }
 

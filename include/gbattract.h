@@ -274,7 +274,12 @@ int gba_minimize_6d_plain(gba_ctx* ctx, gba_id rec, gba_id lig, gba_id grid, gba
 /* Minimization of flexible poses: VA13 over the DOF vector (ang xyz, pos xyz,
  * modesRec[0..Mr), modesLig[0..Ml)) -- minfor.f generalised beyond its fixed
  * 6 DOF (src/apps/em/minfor.f:16,33) -- with the normal-mode energy of
- * gba_energy_6d_modes; persistent device kernel, synchronous. */
+ * gba_energy_6d_modes; persistent device kernel, synchronous.  The gradient
+ * is -ang, -pos (those result entries are forces) and +modesRec, +modesLig:
+ * reduceModeForce stores -sum f . v (src/model/reduction_modes.h:29-90),
+ * which is dE/d(amplitude) plus correctModeForce's term.  The reference's
+ * converter negates the mode entries too (src/apps/em/meta.h:193-201), which
+ * climbs along the modes; this library descends. */
 int gba_minimize_6d_modes(gba_ctx* ctx, gba_id rec, gba_id lig, gba_id grid_rec, gba_id grid_lig,
 		gba_id params, const gba_dof6d_modes* start, size_t n, int max_evals,
 		gba_dof6d_modes* out_state, gba_result6d_modes* out_result, int32_t* out_nevals,

@@ -1118,8 +1118,11 @@ int orc_minimize_6d_modes(const orc_protein* rec, const orc_protein* lig,
 				last_res = r;
 				f = r.rigid.E;
 				for (int k = 0; k < 3; ++k) { g[1 + k] = -(double)r.rigid.ang[k]; g[4 + k] = -(double)r.rigid.pos[k]; }
-				for (int m = 0; m < Mr; ++m) g[7 + m] = -(double)r.modesRec[m];
-				for (int m = 0; m < Ml; ++m) g[7 + Mr + m] = -(double)r.modesLig[m];
+				/* reduceModeForce stores -sum f . v = dE/d(amplitude)
+				 * (src/model/reduction_modes.h:29-90): a gradient already,
+				 * unlike the force-signed ang/pos entries */
+				for (int m = 0; m < Mr; ++m) g[7 + m] = (double)r.modesRec[m];
+				for (int m = 0; m < Ml; ++m) g[7 + Mr + m] = (double)r.modesLig[m];
 				++nev;
 			};
 			minfor(energy, max_fun_eval, x, jn);

@@ -80,9 +80,18 @@ def test_modes_minimizer_device_plain_and_oracle(pkg, oracle, ctx):
            ctx.upload_grid(gl), ctx.upload_params(wl.params))
     s1, r1, n1 = ctx.minimize_6d_modes(*ids, wl.dofs, max_evals=60)
     s2, r2, n2 = ctx.minimize_6d_modes_plain(*ids, wl.dofs, max_evals=60)
-    assert np.array_equal(n1, n2) and np.array_equal(s1, s2) and np.array_equal(r1, r2)
+    # a pose in a deep clash can overflow correctModeForce's 4 k delta^4 to
+    # inf and end in NaN -- identically in both forms
+    assert np.array_equal(n1, n2)
+    assert np.array_equal(s1, s2, equal_nan=True) and np.array_equal(r1, r2, equal_nan=True)
     assert n1.max() <= 61
-    assert np.array_equal(ctx.energy_6d_modes(*ids, s1), r1)
+    fin = np.isfinite(s1).all(axis=1) & np.isfinite(r1).all(axis=1)
+    assert fin.mean() >= 0.9
+    assert np.array_equal(ctx.energy_6d_modes(*ids, s1[fin]), r1[fin])
+    # the minimizer descends (mode entries are gradients, position and angle
+    # entries forces)
+    e0 = ctx.energy_6d_modes(*ids, wl.dofs)[:, 0]
+    assert np.mean(r1[fin, 0] <= e0[fin]) >= 0.9
     _, r3, _ = oracle.minimize_6d_modes(wl.rec, wl.lig, gr, gl, wl.params, wl.dofs, 60)
     d1 = wl.dofs.copy()
     d1[:, 0] = np.nextafter(d1[:, 0], np.float32(np.inf))

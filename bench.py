@@ -264,7 +264,7 @@ def bench_modes(ctx, pkg, n_poses: int, steps: int):
         ctx.energy_6d_modes(*ids, d, out=out)
     torch.cuda.synchronize()
     evals = 3 * len(wl.dofs) / (time.perf_counter() - t0)
-    sub = wl.dofs[: min(len(wl.dofs), 5000)]
+    sub = wl.dofs
     ctx.minimize_6d_modes(*ids, sub[:64], max_evals=10)
     t0 = time.perf_counter()
     _, r1, n1 = ctx.minimize_6d_modes(*ids, sub, max_evals=steps)

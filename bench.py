@@ -255,6 +255,8 @@ def bench_modes(ctx, pkg, n_poses: int, steps: int):
     rec, lig, par = ctx.upload_protein(wl.rec), ctx.upload_protein(wl.lig), ctx.upload_params(wl.params)
     gr = ctx.build_grid(rec, par, pkg.GridOptions())
     gl = ctx.build_grid(lig, par, pkg.GridOptions())
+    for g in (gr, gl):
+        ctx.grid_octets(g, True)      # cooperative 8-lane lookups in both passes
     ids = (rec, lig, gr, gl, par)
     d = torch.from_numpy(wl.dofs).cuda()
     out = ctx.energy_6d_modes(*ids, d)
@@ -273,10 +275,23 @@ def bench_modes(ctx, pkg, n_poses: int, steps: int):
     _, r2, _ = ctx.minimize_6d_modes_plain(*ids, sub, max_evals=steps)
     dt_plain = time.perf_counter() - t0
     e0 = out[: len(sub), 0].cpu().numpy()
+    # the reference's execution model (100-pose work items, one launch each)
+    # on a 5,000-pose subset, against the device form on the same subset
+    few = sub[:5000]
+    t0 = time.perf_counter()
+    _, r4, _ = ctx.minimize_6d_modes(*ids, few, max_evals=steps)
+    dt_dev_few = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    _, r5, _ = ctx.minimize_6d_modes_plain(*ids, few, max_evals=steps, item_size=100)
+    dt_items = time.perf_counter() - t0
     res = {"workload": f"config 2: receptor {wl.rec.n} / ligand {wl.lig.n} beads, 5+5 modes; "
                        f"{len(wl.dofs)} poses scored, {len(sub)} minimized (maxFunEval {steps})",
            "energy_evals_per_s": evals, "minimize_device_poses_per_s": len(sub) / dt_dev,
            "minimize_plain_poses_per_s": len(sub) / dt_plain, "speedup": dt_plain / dt_dev,
+           "subset_5000_device_poses_per_s": len(few) / dt_dev_few,
+           "subset_5000_plain_100_pose_items_poses_per_s": len(few) / dt_items,
+           "speedup_vs_plain_100_pose_items": dt_items / dt_dev_few,
+           "items_equal_device": bool(np.array_equal(r4, r5, equal_nan=True)),
            "device_equals_plain": bool(np.array_equal(r1, r2, equal_nan=True)),
            "evals_per_pose_mean": float(n1.mean()),
            "start_E_median": float(np.median(e0)), "minimized_E_median": float(np.median(r1[:, 0])),

@@ -99,7 +99,7 @@ def load() -> C.CDLL:
         "gba_grid_octets": ([P, U32, I], I),
         "gba_autotune": ([P, U32, U32, U32, U32, P, SZ, I, C.c_char_p, C.POINTER(TuneResultC)], I),
         "gba_minimize_6d_modes": ([P, U32, U32, U32, U32, U32, P, SZ, I, P, P, P, P], I),
-        "gba_minimize_6d_modes_plain": ([P, U32, U32, U32, U32, U32, P, SZ, I, P, P, P, P], I),
+        "gba_minimize_6d_modes_plain": ([P, U32, U32, U32, U32, U32, P, SZ, I, SZ, P, P, P, P], I),
     }
     for name, (args, res) in {**sig, **optional}.items():
         try:

@@ -217,7 +217,8 @@ class GbaContext:
                                                    stream))
         return st, res, nev
 
-    def _modes_min(self, fn, rec, lig, grid_rec, grid_lig, params, dofs, max_evals, stream):
+    def _modes_min(self, fn, rec, lig, grid_rec, grid_lig, params, dofs, max_evals, stream,
+                   item_size=None):
         n = dofs.shape[0]
         if _is_torch(dofs):
             import torch
@@ -228,8 +229,9 @@ class GbaContext:
             st = np.empty((n, DOF_MODES_WIDTH), np.float32)
             res = np.empty((n, RESULT_MODES_WIDTH), np.float32)
             nev = np.empty(n, np.int32)
+        extra = () if item_size is None else (int(item_size),)
         self._check(fn(self.h, rec, lig, grid_rec, grid_lig, params, _lib.ptr(dofs), n, int(max_evals),
-                       _lib.ptr(st), _lib.ptr(res), _lib.ptr(nev), stream))
+                       *extra, _lib.ptr(st), _lib.ptr(res), _lib.ptr(nev), stream))
         return st, res, nev
 
     def minimize_6d_modes(self, rec, lig, grid_rec, grid_lig, params, dofs, max_evals=500,
@@ -240,10 +242,12 @@ class GbaContext:
                                dofs, max_evals, stream)
 
     def minimize_6d_modes_plain(self, rec, lig, grid_rec, grid_lig, params, dofs, max_evals=500,
-                                stream=None):
+                                item_size=0, stream=None):
+        """Host VA13, one round of work items of item_size poses (0: one
+        launch per round) per evaluation; host arrays only."""
         dofs = np.ascontiguousarray(dofs, dtype=np.float32)
         return self._modes_min(self.lib.gba_minimize_6d_modes_plain, rec, lig, grid_rec, grid_lig,
-                               params, dofs, max_evals, stream)
+                               params, dofs, max_evals, stream, item_size=item_size)
 
     def _jobs(self, pairs, with_state: bool):
         """pairs: list of (rec, lig, grid, params, dofs) -> (ctypes array, outputs)."""

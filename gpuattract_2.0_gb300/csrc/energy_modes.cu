@@ -25,6 +25,15 @@
  * The energy holds only the ligand-side terms, as in the reference.
  * Neighbour receptor positions are re-deformed per pair with the same unfused
  * operation sequence as the receptor pass, so no per-pose scratch is needed.
+ *
+ * Every mode projection is linear in the force: f . (R^T v) replaces
+ * (R f) . v and f . (R v) replaces (R^T f) . v, so each staged bead's mode
+ * vectors are rotated once per round into shared memory (ModeStage) and a
+ * projection costs no global load and no rotation.  On octet grids the grid
+ * lookups of both passes take the rigid kernel's 8-lane cooperative form
+ * (CoopStep): the lane holding force component c adds f_c times component
+ * c of the staged vector.  Kernels are compiled for mode capacities 5 and 10
+ * (arrays sized to the capacity, not to GBA_MODES_MAX).
  * The reference's own GPU modes kernels are not followed: they mis-index the
  * deformed receptor and mode buffers (src/model/neighborlist_modes.cu:81-83,
  * src/model/transform_modes.cu:154, src/model/reduction_modes.cu:68-69).
@@ -37,10 +46,11 @@ namespace gba {
 namespace {
 
 /* x + sum_m a_m v_m, unfused in mode order (rotate_translate_deform). */
+template <int MM>
 __device__ __forceinline__ void deform(const float* __restrict__ v, uint32_t M, const float* amp,
 		float& x, float& y, float& z) {
 #pragma unroll
-	for (int m = 0; m < GBA_MODES_MAX; ++m)
+	for (int m = 0; m < MM; ++m)
 		if (m < (int)M) {
 			x = fadd(x, fmul(amp[m], __ldg(v + 3 * m)));
 			y = fadd(y, fmul(amp[m], __ldg(v + 3 * m + 1)));
@@ -49,22 +59,68 @@ __device__ __forceinline__ void deform(const float* __restrict__ v, uint32_t M, 
 }
 
 /* acc[m] += sign * (f . v_m) */
+template <int MM>
 __device__ __forceinline__ void project(const float* __restrict__ v, uint32_t M, float fx, float fy,
 		float fz, float sign, float* acc) {
 #pragma unroll
-	for (int m = 0; m < GBA_MODES_MAX; ++m)
+	for (int m = 0; m < MM; ++m)
 		if (m < (int)M)
 			acc[m] = ffma(sign, ffma(fz, __ldg(v + 3 * m + 2), ffma(fy, __ldg(v + 3 * m + 1),
 					fmul(fx, __ldg(v + 3 * m)))), acc[m]);
+}
+
+/* Per warp and round: each staged bead's mode vectors, rotated into the frame
+ * of the forces they are projected on, component-major. */
+template <int MM>
+struct ModeStage {
+	float w[kBeadsPerRound][3][MM];
+};
+
+/* Rotated mode vectors of slot s: w_m = R v_m (transpose = false) or R^T v_m. */
+template <int MM>
+__device__ __forceinline__ void stage_modes(ModeStage<MM>& S, int s, const float* __restrict__ v, uint32_t M,
+		const float m9[9], bool transpose) {
+#pragma unroll
+	for (int m = 0; m < MM; ++m)
+		if (m < (int)M) {
+			const float vx = __ldg(v + 3 * m), vy = __ldg(v + 3 * m + 1), vz = __ldg(v + 3 * m + 2);
+			float a, b, c;
+			if (transpose) rot_apply_t(m9, vx, vy, vz, a, b, c);
+			else rot_apply(m9, vx, vy, vz, a, b, c);
+			S.w[s][0][m] = a;
+			S.w[s][1][m] = b;
+			S.w[s][2][m] = c;
+		}
+}
+
+/* acc[m] += sign * (f . w_m) with the staged vectors of slot s */
+template <int MM>
+__device__ __forceinline__ void project_staged(const ModeStage<MM>& S, uint32_t s, uint32_t M, float fx,
+		float fy, float fz, float sign, float* acc) {
+#pragma unroll
+	for (int m = 0; m < MM; ++m)
+		if (m < (int)M)
+			acc[m] = ffma(sign, ffma(fz, S.w[s][2][m], ffma(fy, S.w[s][1][m], fmul(fx, S.w[s][0][m]))), acc[m]);
+}
+
+/* acc[m] -= f_c * w_m[c]: the cooperative lane holding force component c */
+template <int MM>
+__device__ __forceinline__ void project_component(const ModeStage<MM>& S, uint32_t s, int c, uint32_t M,
+		float f, float* acc) {
+#pragma unroll
+	for (int m = 0; m < MM; ++m)
+		if (m < (int)M) acc[m] = ffma(-f, S.w[s][c][m], acc[m]);
 }
 
 }  // namespace
 
 /* One pose of the modes energy.  Lane k (k < 26) brings the k-th float of the
  * DOF_6D_Modes record; returns on lane k (k < 27) the k-th float of the
- * Result_6D_Modes record.  Only the model fields of L are read. */
+ * Result_6D_Modes record.  Only the model fields of L are read.  MM >= the
+ * receptor's and the ligand's mode counts. */
+template <int MM>
 __device__ __forceinline__ float eval_pose_modes(const ModesLaunch& L, const float dv, const int lane,
-		WarpStage& W) {
+		WarpStage& W, ModeStage<MM>& MS) {
 	const uint32_t Mr = L.rec.n_modes, Ml = L.lig.n_modes;
 	const float tx = __shfl_sync(GBA_FULL_MASK, dv, 0);
 	const float ty = __shfl_sync(GBA_FULL_MASK, dv, 1);
@@ -72,9 +128,9 @@ __device__ __forceinline__ float eval_pose_modes(const ModesLaunch& L, const flo
 	const float a0 = __shfl_sync(GBA_FULL_MASK, dv, 3);
 	const float a1 = __shfl_sync(GBA_FULL_MASK, dv, 4);
 	const float a2 = __shfl_sync(GBA_FULL_MASK, dv, 5);
-	float ampR[GBA_MODES_MAX], ampL[GBA_MODES_MAX];
+	float ampR[MM], ampL[MM];
 #pragma unroll
-	for (int m = 0; m < GBA_MODES_MAX; ++m) {
+	for (int m = 0; m < MM; ++m) {
 		ampR[m] = __shfl_sync(GBA_FULL_MASK, dv, 6 + m);
 		ampL[m] = __shfl_sync(GBA_FULL_MASK, dv, 16 + m);
 	}
@@ -100,10 +156,11 @@ __device__ __forceinline__ float eval_pose_modes(const ModesLaunch& L, const flo
 	const float ipx = fadd(fadd(fmul(R.m[0], -tx), fmul(R.m[3], -ty)), fmul(R.m[6], -tz));
 	const float ipy = fadd(fadd(fmul(R.m[1], -tx), fmul(R.m[4], -ty)), fmul(R.m[7], -tz));
 	const float ipz = fadd(fadd(fmul(R.m[2], -tx), fmul(R.m[5], -ty)), fmul(R.m[8], -tz));
+	const int comp = coop_component(lane);
 
-	float gR[GBA_MODES_MAX], gL[GBA_MODES_MAX];
+	float gR[MM], gL[MM];
 #pragma unroll
-	for (int m = 0; m < GBA_MODES_MAX; ++m) { gR[m] = 0.f; gL[m] = 0.f; }
+	for (int m = 0; m < MM; ++m) { gR[m] = 0.f; gL[m] = 0.f; }
 
 	/* ---- receptor beads in the ligand grid ---- */
 	for (uint32_t j0 = 0; j0 < L.rec.n; j0 += kBeadsPerRound) {
@@ -118,31 +175,49 @@ __device__ __forceinline__ float eval_pose_modes(const ModesLaunch& L, const flo
 			if (j < L.rec.n) {
 				const float4 r = __ldg(&L.rec.xyzq[j]);
 				const uint32_t mapped = __ldg(&L.rec.tm[j]) >> 16;
+				const float* vr = L.rec_modes + (size_t)j * L.rec_ms;
 				float x = r.x, y = r.y, z = r.z;
-				deform(L.rec_modes + (size_t)j * L.rec_ms, Mr, ampR, x, y, z);
+				deform<MM>(vr, Mr, ampR, x, y, z);
 				float px, py, pz;
 				rot_apply(Ri, x, y, z, px, py, pz);
 				px = fadd(px, ipx); py = fadd(py, ipy); pz = fadd(pz, ipz);
-				/* the type field carries the receptor bead index of the slot */
 				put_bead(W, s, 0.f, 0.f, 0.f, px, py, pz, r.w, j);
 				nlk[h] = stage_grid(L.grid_lig, px, py, pz, mapped, r.w, s, W, bg[h]);
+				/* the ligand-frame force f is rotated back by R before the
+				 * projection: (R f) . v = f . (R^T v); staged for the
+				 * cooperative lookups only (one lookup per bead or two: the
+				 * per-lane form rotates f instead) */
+				if (nlk[h] && L.grid_lig.coop_lookup) stage_modes<MM>(MS, s, vr, Mr, R.m, true);
 			}
 		}
 		const uint32_t n_look = queue_lookups(W, nlk, bg, lane);
 		__syncwarp();
-		for (uint32_t q = lane; q < n_look; q += 32) {
-			const uint32_t s = lookup_slot(W, q);
-			const float4 v = grid_lookup(L.grid_lig, W, q);
-			/* back into the receptor frame, then -(force . mode) */
-			float fx, fy, fz;
-			rot_apply(R.m, v.x, v.y, v.z, fx, fy, fz);
-			project(L.rec_modes + (size_t)__float_as_uint(W.ut[s].w) * L.rec_ms, Mr, fx, fy, fz, -1.f, gR);
+		if (L.grid_lig.coop_lookup) {
+			for (uint32_t k0 = 0; k0 < n_look; k0 += 16) {
+				CoopStep<2> st;
+				st.load(L.grid_lig, W, k0, n_look, lane);
+#pragma unroll
+				for (int b = 0; b < 2; ++b) {
+					const float v = st.component(b, lane);
+					if (st.ok[b] && comp < 3) project_component<MM>(MS, st.sl[b], comp, Mr, fmul(v, st.sc[b]), gR);
+				}
+			}
+		} else {
+			for (uint32_t q = lane; q < n_look; q += 32) {
+				const uint32_t s = lookup_slot(W, q);
+				const float4 v = grid_lookup(L.grid_lig, W, q);
+				/* back into the receptor frame, then -(force . mode) */
+				float fx, fy, fz;
+				rot_apply(R.m, v.x, v.y, v.z, fx, fy, fz);
+				project<MM>(L.rec_modes + (size_t)__float_as_uint(W.ut[s].w) * L.rec_ms, Mr, fx, fy, fz, -1.f, gR);
+			}
 		}
 		__syncwarp();
 	}
 
 	/* ---- ligand beads in the receptor grid + NL against the deformed receptor ---- */
 	PoseSums S;
+	CoopSums C;
 	for (uint32_t i0 = 0; i0 < L.lig.n; i0 += kBeadsPerRound) {
 		uint32_t nlk[2], nln[2];
 		BeadGrid bg[2];
@@ -157,8 +232,9 @@ __device__ __forceinline__ float eval_pose_modes(const ModesLaunch& L, const flo
 				const float4 b = __ldg(&L.lig.xyzq[i]);
 				const uint32_t tm = __ldg(&L.lig.tm[i]);
 				const uint32_t type = tm & 0xffffu, mapped = tm >> 16;
+				const float* vl = L.lig_modes + (size_t)i * L.lig_ms;
 				float x = b.x, y = b.y, z = b.z;
-				deform(L.lig_modes + (size_t)i * L.lig_ms, Ml, ampL, x, y, z);
+				deform<MM>(vl, Ml, ampL, x, y, z);
 				float px, py, pz;
 				rot_apply(R.m, x, y, z, px, py, pz);
 				px = fadd(px, tx); py = fadd(py, ty); pz = fadd(pz, tz);
@@ -166,21 +242,46 @@ __device__ __forceinline__ float eval_pose_modes(const ModesLaunch& L, const flo
 				nlk[h] = stage_grid(L.grid_rec, px, py, pz, mapped, b.w, s, W, bg[h]);
 				bool in_nl;
 				if (type != 0) nln[h] = stage_nl(L.grid_rec.nl, px, py, pz, s, W, in_nl);
+				/* the global-frame force f is projected in the ligand frame:
+				 * (R^T f) . v = f . (R v) */
+				if (nlk[h] | nln[h]) stage_modes<MM>(MS, s, vl, Ml, R.m, false);
 			}
 		}
 		const uint32_t n_look = queue_lookups(W, nlk, bg, lane);
 		uint32_t start[2];
 		const uint32_t n_pair = queue_pairs(W, nln, lane, start);
 		__syncwarp();
-		for (uint32_t q = lane; q < n_look; q += 32) {
-			const uint32_t s = lookup_slot(W, q);
-			const float4 v = grid_lookup(L.grid_rec, W, q);
-			const float4 u = W.ut[s];
-			S.add(v.w, v.x, v.y, v.z, u.x, u.y, u.z);
-			float rx, ry, rz;
-			rot_apply_t(R.m, v.x, v.y, v.z, rx, ry, rz);
-			project(L.lig_modes + (size_t)(i0 + s) * L.lig_ms, Ml, rx, ry, rz, -1.f, gL);
+		if (L.grid_rec.coop_lookup) {
+			for (uint32_t k0 = 0; k0 < n_look; k0 += 16) {
+				CoopStep<2> st;
+				st.load(L.grid_rec, W, k0, n_look, lane);
+#pragma unroll
+				for (int b = 0; b < 2; ++b) {
+					const float v = st.component(b, lane);
+					if (st.ok[b]) {
+						const float f = fmul(v, st.sc[b]);
+						C.f = fadd(C.f, f);
+						if (comp != 3) {
+							const float4 u = W.ut[st.sl[b]];
+							C.t0 = ffma(u.x, f, C.t0);
+							C.t1 = ffma(u.y, f, C.t1);
+							C.t2 = ffma(u.z, f, C.t2);
+							project_component<MM>(MS, st.sl[b], comp, Ml, f, gL);
+						}
+					}
+				}
+			}
+		} else {
+			for (uint32_t q = lane; q < n_look; q += 32) {
+				const uint32_t s = lookup_slot(W, q);
+				const float4 v = grid_lookup(L.grid_rec, W, q);
+				const float4 u = W.ut[s];
+				S.add(v.w, v.x, v.y, v.z, u.x, u.y, u.z);
+				project_staged<MM>(MS, s, Ml, v.x, v.y, v.z, -1.f, gL);
+			}
 		}
+		/* neighbour pairs after the lookups: measured faster here (the rigid
+		 * kernel measured the opposite) */
 		PairWindow win;
 		for (uint32_t w = 0; w < n_pair; w += 64) {
 			uint32_t so[2];
@@ -194,7 +295,7 @@ __device__ __forceinline__ float eval_pose_modes(const ModesLaunch& L, const flo
 				const float4 r = __ldg(&L.rec.xyzq[j]);
 				float rx = r.x, ry = r.y, rz = r.z;
 				const float* vr = L.rec_modes + (size_t)j * L.rec_ms;
-				deform(vr, Mr, ampR, rx, ry, rz);
+				deform<MM>(vr, Mr, ampR, rx, ry, rz);
 				const uint32_t trec = __ldg(&L.rec.tm[j]) & 0xffffu;
 				const float4 b = W.pq[s];
 				const float4 u = W.ut[s];
@@ -204,21 +305,20 @@ __device__ __forceinline__ float eval_pose_modes(const ModesLaunch& L, const flo
 					continue;
 				S.add(e, fx, fy, fz, u.x, u.y, u.z);
 				/* reaction on receptor bead j is -f: its mode gradient gets -(-f . v) */
-				project(vr, Mr, fx, fy, fz, 1.f, gR);
-				float lx, ly, lz;
-				rot_apply_t(R.m, fx, fy, fz, lx, ly, lz);
-				project(L.lig_modes + (size_t)(i0 + s) * L.lig_ms, Ml, lx, ly, lz, -1.f, gL);
+				project<MM>(vr, Mr, fx, fy, fz, 1.f, gR);
+				project_staged<MM>(MS, s, Ml, fx, fy, fz, -1.f, gL);
 			}
 		}
 		__syncwarp();
 	}
+	fold_coop(C, S, lane);
 
 	float sE = warp_sum(S.E), sFx = warp_sum(S.Fx), sFy = warp_sum(S.Fy), sFz = warp_sum(S.Fz);
 	float T[9];
 #pragma unroll
 	for (int k = 0; k < 9; ++k) T[k] = warp_sum(S.T[k]);
 #pragma unroll
-	for (int m = 0; m < GBA_MODES_MAX; ++m) {
+	for (int m = 0; m < MM; ++m) {
 		if (m < (int)Mr) gR[m] = warp_sum(gR[m]);
 		if (m < (int)Ml) gL[m] = warp_sum(gL[m]);
 	}
@@ -227,7 +327,7 @@ __device__ __forceinline__ float eval_pose_modes(const ModesLaunch& L, const flo
 	torque_reduce(R, T, ang);
 	/* correctModeForce: delta += (float)(4 k * delta^4) */
 #pragma unroll
-	for (int m = 0; m < GBA_MODES_MAX; ++m) {
+	for (int m = 0; m < MM; ++m) {
 		if (m < (int)Mr) {
 			const double dl = gR[m];
 			gR[m] = fadd(gR[m], (float)__dmul_rn(__dmul_rn((double)fmul(4.0f, L.rec.mode_force[m]),
@@ -249,22 +349,39 @@ __device__ __forceinline__ float eval_pose_modes(const ModesLaunch& L, const flo
 	else if (lane == 5) v = ang[1];
 	else if (lane == 6) v = ang[2];
 #pragma unroll
-	for (int m = 0; m < GBA_MODES_MAX; ++m) {
+	for (int m = 0; m < MM; ++m) {
 		if (lane == 7 + m) v = m < (int)Mr ? gR[m] : 0.f;
 		if (lane == 17 + m) v = m < (int)Ml ? gL[m] : 0.f;
 	}
 	return v;
 }
 
-__global__ void __launch_bounds__(256) modes_energy_kernel(const ModesLaunch L) {
-	__shared__ WarpStage stage[8];
+namespace {
+
+constexpr int kModesThreads = 256;       /* scoring kernel block */
+constexpr int kModesMinThreads = 128;    /* minimizer kernel block */
+
+/* mode capacity compiled for a launch: 5 or GBA_MODES_MAX */
+int mode_capacity(const ModesLaunch& L) {
+	return (L.rec.n_modes <= 5 && L.lig.n_modes <= 5) ? 5 : GBA_MODES_MAX;
+}
+
+}  // namespace
+
+extern __shared__ float4 modes_dyn_smem[];
+
+template <int MM>
+__global__ void __launch_bounds__(kModesThreads) modes_energy_kernel(const ModesLaunch L) {
+	__shared__ WarpStage stage[kModesThreads / 32];
+	ModeStage<MM>* ms = reinterpret_cast<ModeStage<MM>*>(modes_dyn_smem);
 	const int lane = threadIdx.x & 31;
+	const int wib = threadIdx.x >> 5;
 	const size_t warp = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
 	const size_t nwarps = ((size_t)gridDim.x * blockDim.x) >> 5;
 	for (size_t p = warp; p < L.n; p += nwarps) {
 		const float* d = reinterpret_cast<const float*>(L.dofs + p);
 		const float dv = lane < 26 ? __ldg(d + lane) : 0.f;
-		const float v = eval_pose_modes(L, dv, lane, stage[threadIdx.x >> 5]);
+		const float v = eval_pose_modes<MM>(L, dv, lane, stage[wib], ms[wib]);
 		if (lane < 27) reinterpret_cast<float*>(L.out + p)[lane] = v;
 	}
 }
@@ -278,9 +395,12 @@ __device__ __forceinline__ unsigned long long modes_global_ns() {
 	return t;
 }
 
-__global__ void __launch_bounds__(256) minimize_modes_kernel(const ModesMinLaunch M) {
-	__shared__ WarpStage stage[8];
+template <int MM>
+__global__ void __launch_bounds__(kModesMinThreads) minimize_modes_kernel(const ModesMinLaunch M) {
+	__shared__ WarpStage stage[kModesMinThreads / 32];
+	ModeStage<MM>* ms = reinterpret_cast<ModeStage<MM>*>(modes_dyn_smem);
 	const int lane = threadIdx.x & 31;
+	const int wib = threadIdx.x >> 5;
 	const ModesLaunch& L = M.m;
 	const uint32_t Mr = L.rec.n_modes, Ml = L.lig.n_modes;
 	const int jn = 6 + (int)Mr + (int)Ml;
@@ -303,11 +423,11 @@ __global__ void __launch_bounds__(256) minimize_modes_kernel(const ModesMinLaunc
 			break;
 		}
 		const size_t p = (size_t)slot;
-		VA13<6 + 2 * GBA_MODES_MAX> va;
+		VA13<6 + 2 * MM> va;
 		/* lane k holds DOF float k (pos, ang, modesRec[10], modesLig[10]) */
 		float dv = lane < 26 ? __ldg(reinterpret_cast<const float*>(M.start + p) + lane) : 0.f;
 		if (lane == 0) {
-			double x0[6 + 2 * GBA_MODES_MAX];
+			double x0[6 + 2 * MM];
 			const float* s = reinterpret_cast<const float*>(M.start + p);
 			for (int k = 0; k < 3; ++k) { x0[k] = s[3 + k]; x0[3 + k] = s[k]; }
 			for (uint32_t m = 0; m < Mr; ++m) x0[6 + m] = s[6 + m];
@@ -331,7 +451,7 @@ __global__ void __launch_bounds__(256) minimize_modes_kernel(const ModesMinLaunc
 				const float t = __shfl_sync(GBA_FULL_MASK, lane == 0 ? rec[k] : 0.f, 0);
 				if (lane == k) dv = t;
 			}
-			v = eval_pose_modes(L, dv, lane, stage[threadIdx.x >> 5]);
+			v = eval_pose_modes<MM>(L, dv, lane, stage[wib], ms[wib]);
 			++nev;
 			/* gather the result record on lane 0 */
 			float res[27];
@@ -339,7 +459,7 @@ __global__ void __launch_bounds__(256) minimize_modes_kernel(const ModesMinLaunc
 			for (int k = 0; k < 27; ++k) res[k] = __shfl_sync(GBA_FULL_MASK, v, k);
 			int done = 0;
 			if (lane == 0) {
-				double g[6 + 2 * GBA_MODES_MAX];
+				double g[6 + 2 * MM];
 				for (int k = 0; k < 3; ++k) { g[k] = -(double)res[4 + k]; g[3 + k] = -(double)res[1 + k]; }
 				/* mode entries are gradients already (reduceModeForce) */
 				for (uint32_t m = 0; m < Mr; ++m) g[6 + m] = (double)res[7 + m];
@@ -363,26 +483,75 @@ __global__ void __launch_bounds__(256) minimize_modes_kernel(const ModesMinLaunc
 	}
 }
 
-cudaError_t launch_modes_energy(const ModesLaunch& L, int blocks, int threads, cudaStream_t s) {
-	modes_energy_kernel<<<blocks, threads, 0, s>>>(L);
+namespace {
+
+template <int MM>
+size_t mode_stage_bytes(int threads) {
+	return (size_t)(threads / 32) * sizeof(ModeStage<MM>);
+}
+
+/* dynamic shared memory beyond the 48 KB default needs the opt-in */
+template <class K>
+cudaError_t allow_smem(K kernel, size_t dyn) {
+	return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
+}
+
+template <int MM>
+cudaError_t launch_modes_mm(const ModesLaunch& L, int blocks, int threads, cudaStream_t s) {
+	const size_t dyn = mode_stage_bytes<MM>(threads);
+	cudaError_t e = allow_smem(modes_energy_kernel<MM>, dyn);
+	if (e != cudaSuccess) return e;
+	modes_energy_kernel<MM><<<blocks, threads, dyn, s>>>(L);
 	return cudaGetLastError();
 }
 
-int modes_blocks_per_sm(int threads) {
+template <int MM>
+int modes_bps_mm(int threads) {
+	const size_t dyn = mode_stage_bytes<MM>(threads);
+	if (allow_smem(modes_energy_kernel<MM>, dyn) != cudaSuccess) return 1;
 	int nb = 0;
-	cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, modes_energy_kernel, threads, 0);
+	cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, modes_energy_kernel<MM>, threads, dyn);
 	return nb > 0 ? nb : 1;
+}
+
+template <int MM>
+cudaError_t launch_min_mm(const ModesMinLaunch& M, int blocks, int threads, cudaStream_t s) {
+	const size_t dyn = mode_stage_bytes<MM>(threads);
+	cudaError_t e = allow_smem(minimize_modes_kernel<MM>, dyn);
+	if (e != cudaSuccess) return e;
+	minimize_modes_kernel<MM><<<blocks, threads, dyn, s>>>(M);
+	return cudaGetLastError();
+}
+
+template <int MM>
+int min_bps_mm(int threads) {
+	const size_t dyn = mode_stage_bytes<MM>(threads);
+	if (allow_smem(minimize_modes_kernel<MM>, dyn) != cudaSuccess) return 1;
+	int nb = 0;
+	cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, minimize_modes_kernel<MM>, threads, dyn);
+	return nb > 0 ? nb : 1;
+}
+
+}  // namespace
+
+cudaError_t launch_modes_energy(const ModesLaunch& L, int blocks, int threads, cudaStream_t s) {
+	if (threads != kModesThreads) return cudaErrorInvalidValue;
+	return mode_capacity(L) == 5 ? launch_modes_mm<5>(L, blocks, threads, s)
+	                             : launch_modes_mm<GBA_MODES_MAX>(L, blocks, threads, s);
+}
+
+int modes_blocks_per_sm(int threads, const ModesLaunch& L) {
+	return mode_capacity(L) == 5 ? modes_bps_mm<5>(threads) : modes_bps_mm<GBA_MODES_MAX>(threads);
 }
 
 cudaError_t launch_minimize_modes(const ModesMinLaunch& M, int blocks, int threads, cudaStream_t s) {
-	minimize_modes_kernel<<<blocks, threads, 0, s>>>(M);
-	return cudaGetLastError();
+	if (threads != kModesMinThreads) return cudaErrorInvalidValue;
+	return mode_capacity(M.m) == 5 ? launch_min_mm<5>(M, blocks, threads, s)
+	                               : launch_min_mm<GBA_MODES_MAX>(M, blocks, threads, s);
 }
 
-int minimize_modes_blocks_per_sm(int threads) {
-	int nb = 0;
-	cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, minimize_modes_kernel, threads, 0);
-	return nb > 0 ? nb : 1;
+int minimize_modes_blocks_per_sm(int threads, const ModesLaunch& L) {
+	return mode_capacity(L) == 5 ? min_bps_mm<5>(threads) : min_bps_mm<GBA_MODES_MAX>(threads);
 }
 
 }  // namespace gba

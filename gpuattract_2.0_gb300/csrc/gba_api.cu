@@ -680,7 +680,7 @@ ModesLaunch Context::modes_launch(gba_id rec, gba_id lig, gba_id grid_rec, gba_i
 
 void Context::run_modes(ModesLaunch& L, cudaStream_t s) {
 	const int threads = 256;
-	int bps = modes_blocks_per_sm(threads);
+	int bps = modes_blocks_per_sm(threads, L);
 	size_t want = (L.n + threads / 32 - 1) / (threads / 32);
 	size_t blocks = std::max<size_t>(1, std::min<size_t>(want, (size_t)num_sms * bps));
 	check_cuda(launch_modes_energy(L, (int)blocks, threads, s), "modes energy launch");

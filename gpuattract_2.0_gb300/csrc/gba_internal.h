@@ -171,7 +171,8 @@ struct ModesLaunch {
 };
 
 cudaError_t launch_modes_energy(const ModesLaunch& L, int blocks, int threads, cudaStream_t s);
-int modes_blocks_per_sm(int threads);
+/* resident blocks of the scoring kernel compiled for L's mode counts */
+int modes_blocks_per_sm(int threads, const ModesLaunch& L);
 
 struct ModesMinLaunch {
 	ModesLaunch m;                  /* model fields; dofs/out/n unused */
@@ -186,7 +187,7 @@ struct ModesMinLaunch {
 };
 
 cudaError_t launch_minimize_modes(const ModesMinLaunch& M, int blocks, int threads, cudaStream_t s);
-int minimize_modes_blocks_per_sm(int threads);
+int minimize_modes_blocks_per_sm(int threads, const ModesLaunch& L);
 
 /* Number of resident blocks per SM of the rigid kernel for `threads`. */
 int rigid_blocks_per_sm(int threads, bool census, bool bound4 = false);

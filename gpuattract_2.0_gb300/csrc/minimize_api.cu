@@ -405,7 +405,7 @@ int gba_minimize_6d_modes(gba_ctx* ctx, gba_id rec, gba_id lig, gba_id grid_rec,
 	M.counter = (unsigned long long*)((char*)ctx->aux.ptr + 16);
 	check_cuda(cudaMemsetAsync((char*)ctx->aux.ptr + 12, 0, 12, s), "modes minimize: cursor");
 	const int threads = 128;
-	const int bps = minimize_modes_blocks_per_sm(threads);
+	const int bps = minimize_modes_blocks_per_sm(threads, M.m);
 	size_t blocks = std::max<size_t>(1, std::min<size_t>((n * 32 + threads - 1) / threads,
 			(size_t)ctx->num_sms * bps));
 	check_cuda(launch_minimize_modes(M, (int)blocks, threads, s), "modes minimize launch");
@@ -426,8 +426,8 @@ int gba_minimize_6d_modes(gba_ctx* ctx, gba_id rec, gba_id lig, gba_id grid_rec,
 
 int gba_minimize_6d_modes_plain(gba_ctx* ctx, gba_id rec, gba_id lig, gba_id grid_rec,
 		gba_id grid_lig, gba_id params, const gba_dof6d_modes* start, size_t n, int max_evals,
-		gba_dof6d_modes* out_state, gba_result6d_modes* out_result, int32_t* out_nevals,
-		void* stream) {
+		size_t item_size, gba_dof6d_modes* out_state, gba_result6d_modes* out_result,
+		int32_t* out_nevals, void* stream) {
 	if (!ctx) return GBA_ERR_INVALID_ARGUMENT;
 	GBA_TRY
 	if (n == 0) return GBA_OK;
@@ -469,12 +469,20 @@ int gba_minimize_6d_modes_plain(gba_ctx* ctx, gba_id rec, gba_id lig, gba_id gri
 			for (int m = 0; m < Mr; ++m) d.modesRec[m] = (float)pt[6 + m];
 			for (int m = 0; m < Ml; ++m) d.modesLig[m] = (float)pt[6 + Mr + m];
 		}
-		check_cuda(cudaMemcpyAsync(din, hin, na * sizeof(gba_dof6d_modes), cudaMemcpyHostToDevice, s), "H2D");
-		L.dofs = din;
-		L.out = dout;
-		L.n = na;
-		ctx->run_modes(L, s);
-		check_cuda(cudaMemcpyAsync(hout, dout, na * sizeof(gba_result6d_modes), cudaMemcpyDeviceToHost, s), "D2H");
+		/* one round = the active poses cut into work items, each copied in,
+		 * evaluated by one launch and copied out */
+		const size_t item = item_size ? item_size : na;
+		for (size_t b = 0; b < na; b += item) {
+			const size_t m = std::min(item, na - b);
+			check_cuda(cudaMemcpyAsync(din + b, hin + b, m * sizeof(gba_dof6d_modes), cudaMemcpyHostToDevice, s),
+					"H2D");
+			L.dofs = din + b;
+			L.out = dout + b;
+			L.n = m;
+			ctx->run_modes(L, s);
+			check_cuda(cudaMemcpyAsync(hout + b, dout + b, m * sizeof(gba_result6d_modes), cudaMemcpyDeviceToHost,
+					s), "D2H");
+		}
 		check_cuda(cudaStreamSynchronize(s), "plain modes: sync");
 		next.clear();
 		for (size_t k = 0; k < na; ++k) {

@@ -340,28 +340,35 @@ struct CoopStep {
 		}
 	}
 
+	/* the reduce-scatter of block b: the lane's finished, unscaled component
+	 * (lane c: lookup c & 1, component 2 * ((c >> 1) & 1) + (c >> 2)) */
+	__device__ __forceinline__ float component(int b, int lane) const {
+		const int cor = lane & 7;
+		const int hi2 = (cor >> 1) & 1, hi4 = cor >> 2;
+		/* step 1 (partner c ^ 1): keep the own lookup */
+		float m4[4];
+#pragma unroll
+		for (int j = 0; j < 4; ++j) m4[j] = fadd(c[b][j], __shfl_xor_sync(GBA_FULL_MASK, c[b][4 + j], 1));
+		/* step 2 (partner c ^ 2): keep components {0,1} or {2,3} */
+		float m2[2];
+#pragma unroll
+		for (int j = 0; j < 2; ++j) {
+			const float keep = hi2 ? m4[2 + j] : m4[j];
+			const float send = hi2 ? m4[j] : m4[2 + j];
+			m2[j] = fadd(keep, __shfl_xor_sync(GBA_FULL_MASK, send, 2));
+		}
+		/* step 3 (partner c ^ 4): keep one */
+		const float keep = hi4 ? m2[1] : m2[0];
+		const float send = hi4 ? m2[0] : m2[1];
+		return fadd(keep, __shfl_xor_sync(GBA_FULL_MASK, send, 4));
+	}
+
 	__device__ __forceinline__ void reduce(const WarpStage& W, int lane, CoopSums& C) const {
 		const int cor = lane & 7;
 		const int comp = 2 * ((cor >> 1) & 1) + (cor >> 2);     /* which component */
-		const int hi2 = (cor >> 1) & 1, hi4 = cor >> 2;
 #pragma unroll
 		for (int b = 0; b < NB; ++b) {
-			/* step 1 (partner c ^ 1): keep the own lookup */
-			float m4[4];
-#pragma unroll
-			for (int j = 0; j < 4; ++j) m4[j] = fadd(c[b][j], __shfl_xor_sync(GBA_FULL_MASK, c[b][4 + j], 1));
-			/* step 2 (partner c ^ 2): keep components {0,1} or {2,3} */
-			float m2[2];
-#pragma unroll
-			for (int j = 0; j < 2; ++j) {
-				const float keep = hi2 ? m4[2 + j] : m4[j];
-				const float send = hi2 ? m4[j] : m4[2 + j];
-				m2[j] = fadd(keep, __shfl_xor_sync(GBA_FULL_MASK, send, 2));
-			}
-			/* step 3 (partner c ^ 4): keep one */
-			const float keep = hi4 ? m2[1] : m2[0];
-			const float send = hi4 ? m2[0] : m2[1];
-			const float v = fadd(keep, __shfl_xor_sync(GBA_FULL_MASK, send, 4));
+			const float v = component(b, lane);
 			if (ok[b]) {
 				const float f = fmul(v, sc[b]);
 				C.f = fadd(C.f, f);
@@ -375,6 +382,13 @@ struct CoopStep {
 		}
 	}
 };
+
+/* Component (0..3 = force x, y, z, energy) that lane holds after
+ * CoopStep::component. */
+__device__ __forceinline__ int coop_component(int lane) {
+	const int cor = lane & 7;
+	return 2 * ((cor >> 1) & 1) + (cor >> 2);
+}
 
 __device__ __forceinline__ void drain_lookups(const DevGrid& G, const WarpStage& W, uint32_t n_look,
 		int lane, PoseSums& S, CoopSums& C) {

@@ -285,12 +285,16 @@ int gba_minimize_6d_modes(gba_ctx* ctx, gba_id rec, gba_id lig, gba_id grid_rec,
 		gba_dof6d_modes* out_state, gba_result6d_modes* out_result, int32_t* out_nevals,
 		void* stream);
 
-/* Plain per-step form of gba_minimize_6d_modes (host VA13, one launch per
- * evaluation round); host pointers only. */
+/* Plain per-step form of gba_minimize_6d_modes: host VA13 and, per
+ * evaluation round, the active poses cut into work items of item_size poses
+ * (0 = all active poses in one item; 100 is the reference server's default),
+ * each copied in, evaluated by one launch and copied out, as
+ * gba_minimize_6d_plain does.  Host pointers only; results bit-identical to
+ * gba_minimize_6d_modes. */
 int gba_minimize_6d_modes_plain(gba_ctx* ctx, gba_id rec, gba_id lig, gba_id grid_rec,
 		gba_id grid_lig, gba_id params, const gba_dof6d_modes* start, size_t n, int max_evals,
-		gba_dof6d_modes* out_state, gba_result6d_modes* out_result, int32_t* out_nevals,
-		void* stream);
+		size_t item_size, gba_dof6d_modes* out_state, gba_result6d_modes* out_result,
+		int32_t* out_nevals, void* stream);
 
 /* Wall-time budget for device minimization (0 = none): warps stop claiming
  * poses once it is spent and the call returns GBA_ERR_TIMEOUT; the

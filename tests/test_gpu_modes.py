@@ -38,11 +38,14 @@ def mode_errors(got, ref, Mr, Ml):
     return np.concatenate(errs) if errs else np.zeros(1)
 
 
-def run_modes(ctx, oracle, rec, lig, params, opts, dofs):
+def run_modes(ctx, oracle, rec, lig, params, opts, dofs, octets=False):
     gr = oracle.build_grid(rec, params, opts)
     gl = oracle.build_grid(lig, params, opts)
     ids = (ctx.upload_protein(rec), ctx.upload_protein(lig), ctx.upload_grid(gr),
            ctx.upload_grid(gl), ctx.upload_params(params))
+    if octets:               # cooperative 8-lane lookups in both passes
+        ctx.grid_octets(ids[2], True)
+        ctx.grid_octets(ids[3], True)
     return ctx.energy_6d_modes(*ids, dofs), gr, gl
 
 
@@ -59,10 +62,11 @@ def test_golden_modes_reference_outputs(golden_cases, oracle, ctx):
     assert np.all(got[:, 7 + rec.n_modes:17] == 0) and np.all(got[:, 17 + lig.n_modes:] == 0)
 
 
-def test_modes_fresh_case_vs_oracle(pkg, oracle, ctx):
+@pytest.mark.parametrize("octets", [False, True])
+def test_modes_fresh_case_vs_oracle(pkg, oracle, ctx, octets):
     wl = pkg.synth.make_pair(2, 130, 70, 96, (16.0, 24.0), n_modes=5, seed=515)
     opts = pkg.GridOptions()
-    got, gr, gl = run_modes(ctx, oracle, wl.rec, wl.lig, wl.params, opts, wl.dofs)
+    got, gr, gl = run_modes(ctx, oracle, wl.rec, wl.lig, wl.params, opts, wl.dofs, octets)
     ref, st = oracle.energy_6d_modes(wl.rec, wl.lig, gr, gl, wl.params, wl.dofs, stats=True)
     for e in pose_errors(got[:, :7], ref[:, :7], st):
         assert float(e.max()) <= 1e-4
@@ -85,6 +89,9 @@ def test_modes_minimizer_device_plain_and_oracle(pkg, oracle, ctx):
     assert np.array_equal(n1, n2)
     assert np.array_equal(s1, s2, equal_nan=True) and np.array_equal(r1, r2, equal_nan=True)
     assert n1.max() <= 61
+    s3, r3i, n3 = ctx.minimize_6d_modes_plain(*ids, wl.dofs, max_evals=60, item_size=100)
+    assert np.array_equal(n1, n3)
+    assert np.array_equal(s1, s3, equal_nan=True) and np.array_equal(r1, r3i, equal_nan=True)
     fin = np.isfinite(s1).all(axis=1) & np.isfinite(r1).all(axis=1)
     assert fin.mean() >= 0.9
     assert np.array_equal(ctx.energy_6d_modes(*ids, s1[fin]), r1[fin])
@@ -100,6 +107,13 @@ def test_modes_minimizer_device_plain_and_oracle(pkg, oracle, ctx):
     print(f"modes minimization within 1e-3 of the oracle: GPU {100 * frac:.1f}%, oracle with a "
           f"one-ulp start perturbation {100 * floor:.1f}%")
     assert frac >= floor - 0.05
+    # octet grids (cooperative lookups): device and plain forms still agree bit for bit
+    ctx.grid_octets(ids[2], True)
+    ctx.grid_octets(ids[3], True)
+    s5, r5, n5 = ctx.minimize_6d_modes(*ids, wl.dofs[:32], max_evals=30)
+    s6, r6, n6 = ctx.minimize_6d_modes_plain(*ids, wl.dofs[:32], max_evals=30)
+    assert np.array_equal(n5, n6)
+    assert np.array_equal(s5, s6, equal_nan=True) and np.array_equal(r5, r6, equal_nan=True)
 
 
 def test_zero_amplitudes_match_rigid(small_case, pkg, oracle, ctx):

@@ -129,6 +129,25 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
+def shard(dofs, world: int, rank: int):
+    """Rank `rank`'s share of a job of `world` equal contiguous pose slices
+    (weak scaling: each rank scores its own poses, no collective on the data
+    path)."""
+    n = len(dofs) // world
+    return dofs[rank * n:(rank + 1) * n]
+
+
+def max_over_ranks(values, world: int, device: str = "cuda"):
+    """Element-wise maximum of a list of floats over all ranks (the slowest
+    rank sets a step's time); identity for one rank."""
+    if world <= 1:
+        return [float(v) for v in values]
+    import torch
+    t = torch.tensor([float(v) for v in values], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return [float(v) for v in t.tolist()]
+
+
 def make_workload(n_poses: int | None, rec_beads: int | None = None):
     """Config 1 (or, for small profiling captures, config 1's distributions with
     a smaller receptor)."""
@@ -425,7 +444,9 @@ def main():
         dist.init_process_group("nccl")
     torch.cuda.set_device(local)
     import __graft_entry__
-    pkg, wl = make_workload(args.poses, args.rec_beads)
+    pkg, wl = make_workload(args.poses * world if args.poses else (100_000 * world if world > 1 else None),
+                            args.rec_beads)
+    wl.dofs = np.ascontiguousarray(shard(wl.dofs, world, rank))
     from gbattract.context import GbaContext
     ctx = GbaContext(local)
     ctx.set_kernel_options(args.kopts)
@@ -510,11 +531,7 @@ def main():
     kernel_ms, kernel_launches = ctx.kernel_time(reset=True)
     ctx.kernel_timing(False)
     ks = [a.elapsed_time(b) / 1000.0 for a, b in times]
-    ktot = sum(ks)
-    if world > 1:
-        t = torch.tensor([ktot], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ktot = float(t.item())
+    ktot, = max_over_ranks([sum(ks)], world)
     value = world * n * args.steps / ktot
     kavg = ktot / args.steps
     kernel_avg_s = kernel_ms / 1000.0 / max(1, kernel_launches)
@@ -533,7 +550,7 @@ def main():
     t0 = time.perf_counter()
     for _ in range(e_steps):
         ctx.energy_6d(rec, lig, grid, par, hd, out=ho)
-    e2e_dt = (time.perf_counter() - t0) / e_steps
+    e2e_dt, = max_over_ranks([(time.perf_counter() - t0) / e_steps], world)
     e2e = world * n / e2e_dt
 
     # parity spot check of the timed result (device path) against the host path

@@ -506,7 +506,6 @@ __device__ __forceinline__ void eval_pose_rigid(const RigidModel& M, float tx, f
 		float a0, float a1, float a2, int lane, WarpStage& W, float res[7], PoseCensus* census) {
 	put_pose(W, pose_rotation(a0, a1, a2, lane), tx, ty, tz, lane);
 	PoseSums S;
-	CoopSums C;
 	uint32_t c_grid = 0, c_charged = 0, c_nl = 0, c_ent = 0;
 	for (uint32_t i0 = 0; i0 < M.lig.n; i0 += kBeadsPerRound) {
 		/* 1. stage 64 beads, two per lane: lane, then lane + 32 */
@@ -547,43 +546,47 @@ __device__ __forceinline__ void eval_pose_rigid(const RigidModel& M, float tx, f
 
 		/* 2. neighbour pairs, two per lane and window so that both gather
 		 * chains (list entry -> receptor bead -> parameters) are in flight
-		 * together */
+		 * together, the next window's list entries already on their way */
 		PairWindow win;
+		/* list entries of the next window are loaded while this one is
+		 * computed; typed entries carry the receptor type in bits 24..31 */
+		const uint32_t* lst = M.grid.nl.typed_list ? M.grid.nl.typed_list : M.grid.nl.list;
+		const bool typed = M.grid.nl.typed_list != nullptr;
+		uint32_t sa = 0, sb = 0, ea = 0, eb = 0;
+		if (n_pair > 0) {
+			win.owners(W, 0, start, nln, lane, sa, sb);
+			if ((uint32_t)lane < n_pair) ea = __ldg(&lst[W.lbase[sa] + lane]);
+			if ((uint32_t)lane + 32 < n_pair) eb = __ldg(&lst[W.lbase[sb] + lane + 32]);
+		}
 		for (uint32_t w = 0; w < n_pair; w += 64) {
 			const uint32_t k = w + lane, k2 = k + 32;
-			uint32_t sa, sb;
-			win.owners(W, w, start, nln, lane, sa, sb);
+			const uint32_t csa = sa, csb = sb, cea = ea, ceb = eb;
+			if (w + 64 < n_pair) {
+				win.owners(W, w + 64, start, nln, lane, sa, sb);
+				if (k + 64 < n_pair) ea = __ldg(&lst[W.lbase[sa] + k + 64]);
+				if (k2 + 64 < n_pair) eb = __ldg(&lst[W.lbase[sb] + k2 + 64]);
+			}
 			if (k >= n_pair) continue;
 			const bool has2 = k2 < n_pair;
-			const uint32_t ia = W.lbase[sa] + k;
-			const uint32_t ib = has2 ? W.lbase[sb] + k2 : ia;
-			float4 ra, rb;
-			uint32_t ta, tb;
-			if (M.grid.nl.typed_list) {
-				/* entries carry the receptor type: one gather less per pair */
-				const uint32_t ea = __ldg(&M.grid.nl.typed_list[ia]);
-				const uint32_t eb = __ldg(&M.grid.nl.typed_list[ib]);
-				ra = __ldg(&M.rec.xyzq[ea & 0xffffffu]);
-				rb = __ldg(&M.rec.xyzq[eb & 0xffffffu]);
-				ta = ea >> 24;
-				tb = eb >> 24;
-			} else {
-				const uint32_t ja = __ldg(&M.grid.nl.list[ia]);
-				const uint32_t jb = __ldg(&M.grid.nl.list[ib]);
-				ra = __ldg(&M.rec.xyzq[ja]);
-				rb = __ldg(&M.rec.xyzq[jb]);
-				ta = __ldg(&M.rec.tm[ja]) & 0xffffu;
-				tb = __ldg(&M.rec.tm[jb]) & 0xffffu;
-			}
-			pair_term(M, W, sa, ra, ta, S);
-			if (has2) pair_term(M, W, sb, rb, tb, S);
+			const uint32_t eb2 = has2 ? ceb : cea;
+			const uint32_t ja = typed ? cea & 0xffffffu : cea;
+			const uint32_t jb = typed ? eb2 & 0xffffffu : eb2;
+			const float4 ra = __ldg(&M.rec.xyzq[ja]);
+			const float4 rb = __ldg(&M.rec.xyzq[jb]);
+			const uint32_t ta = typed ? cea >> 24 : __ldg(&M.rec.tm[ja]) & 0xffffu;
+			const uint32_t tb = typed ? eb2 >> 24 : __ldg(&M.rec.tm[jb]) & 0xffffu;
+			pair_term(M, W, csa, ra, ta, S);
+			if (has2) pair_term(M, W, csb, rb, tb, S);
 		}
 
-		/* 3. grid lookups */
-		drain_lookups(M.grid, W, n_look, lane, S, C);
+		/* 3. grid lookups (cooperative sums folded per round) */
+		{
+			CoopSums Cr;
+			drain_lookups(M.grid, W, n_look, lane, S, Cr);
+			fold_coop(Cr, S, lane);
+		}
 		__syncwarp();
 	}
-	fold_coop(C, S, lane);
 	float sE = warp_sum(S.E), sFx = warp_sum(S.Fx), sFy = warp_sum(S.Fy), sFz = warp_sum(S.Fz);
 	float T[9];
 #pragma unroll

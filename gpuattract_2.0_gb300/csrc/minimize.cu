@@ -43,7 +43,9 @@ __device__ __forceinline__ bool warp_over_budget(unsigned long long t_start, uns
 	return __shfl_sync(GBA_FULL_MASK, over, 0) != 0;
 }
 
-__global__ void __launch_bounds__(256) minimize_rigid_kernel(const MinLaunch L) {
+/* compiled for four resident 256-thread blocks per SM (64 registers, like
+ * the scoring kernel's four-block instantiation) */
+__global__ void __launch_bounds__(256, 4) minimize_rigid_kernel(const MinLaunch L) {
 	__shared__ WarpStage stage[8];   /* one per warp of a <=256-thread block */
 	const int lane = threadIdx.x & 31;
 	unsigned long long t_start = 0;

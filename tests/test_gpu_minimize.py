@@ -52,30 +52,35 @@ def test_device_equals_plain_form(min_case, ctx):
     assert np.array_equal(ctx.energy_6d(*ids, s1), r1)
 
 
-def test_against_cpu_oracle_va13(min_case, oracle, ctx):
+def test_against_cpu_oracle_va13(pkg, oracle, ctx):
     """Minimized energies against the CPU oracle's VA13 (FP32 CPU energies).
 
     The reference's minimizer is chaotic at the FP32 noise level: moving one
     start coordinate by one ulp changes the minimized energy by more than 1e-3
     for about a fifth of these poses on the oracle itself (the floor measured
-    below), and glibc's sinf/cosf differ from correctly rounded values in about
+    below: the lowest of three such perturbations, over 1,024 poses so that
+    the fractions are known to about a point), and glibc's sinf/cosf differ from correctly rounded values in about
     1% of calls, so no GPU path can follow the CPU trajectories bit for bit.
     The GPU must agree with the oracle as well as the oracle agrees with
     itself under that one-ulp perturbation (5 points of slack), and the oracle
     re-evaluated at the GPU's minimized states must reproduce the GPU's
     reported energies and gradients (the energy parity bound, 1e-4 scaled)."""
     from test_gpu_rigid import pose_errors
-    wl, grid = min_case
+    wl = pkg.synth.make_pair(0, 160, 70, 1024, (20.0, 30.0), seed=909)
+    grid = oracle.build_grid(wl.rec, wl.params, pkg.GridOptions())
     ids = upload(ctx, wl.rec, wl.lig, grid, wl.params)
     s_dev, r_dev, n_dev = ctx.minimize_6d(*ids, wl.dofs, max_evals=100)
     _, r_cpu, n_cpu = oracle.minimize_6d(wl.rec, wl.lig, grid, wl.params, wl.dofs, 100)
-    d1 = wl.dofs.copy()
-    d1[:, 0] = np.nextafter(d1[:, 0], np.float32(np.inf))
-    _, r_ulp, _ = oracle.minimize_6d(wl.rec, wl.lig, grid, wl.params, d1, 100)
+    floors = []
+    for col, direction in ((0, np.inf), (3, -np.inf), (5, np.inf)):
+        d1 = wl.dofs.copy()
+        d1[:, col] = np.nextafter(d1[:, col], np.float32(direction))
+        _, r_ulp, _ = oracle.minimize_6d(wl.rec, wl.lig, grid, wl.params, d1, 100)
+        floors.append(minimized_agreement(r_ulp, r_cpu))
     frac = minimized_agreement(r_dev, r_cpu)
-    floor = minimized_agreement(r_ulp, r_cpu)
-    print(f"minimized energies within 1e-3 of the oracle: GPU {100 * frac:.1f}%, oracle with a "
-          f"one-ulp start perturbation {100 * floor:.1f}% of {len(r_dev)} poses")
+    floor = min(floors)
+    print(f"minimized energies within 1e-3 of the oracle: GPU {100 * frac:.1f}%, oracle with one-ulp "
+          f"start perturbations {', '.join(f'{100 * f:.1f}%' for f in floors)} of {len(r_dev)} poses")
     assert frac >= floor - 0.05
     ref, st = oracle.energy_6d(wl.rec, wl.lig, grid, wl.params, s_dev, stats=True)
     for e in pose_errors(r_dev, ref, st):

@@ -394,6 +394,18 @@ def bench_batched_uneven(ctx, pkg, pose_scale: float, steps: int):
         plain_done.append(1e3 * (time.perf_counter() - t0))
     dt_plain = time.perf_counter() - t0
     same = all(np.array_equal(a[1], b[1]) for a, b in zip(got, plain))
+    # the reference's execution model (100-pose work items, pair after pair)
+    # on the first 8 pairs, against the batched device form on the same pairs
+    few = jobs[:8]
+    n_few = sum(len(j[4]) for j in few)
+    t0 = time.perf_counter()
+    got_few = ctx.batch_minimize_6d(few, max_evals=steps)
+    dt_dev_few = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    items = [ctx.minimize_6d_plain(rec, lig, grid, par, dofs, max_evals=steps, item_size=100)
+             for (rec, lig, grid, par, dofs) in few]
+    dt_items = time.perf_counter() - t0
+    same_items = all(np.array_equal(a[1], b[1]) for a, b in zip(got_few, items))
     for i in handles:
         ctx.release(i)
     pd = np.array(plain_done)
@@ -401,6 +413,9 @@ def bench_batched_uneven(ctx, pkg, pose_scale: float, steps: int):
                         f"(pose counts x{pose_scale}), maxFunEval {steps}",
             "batched_device_poses_per_s": total / dt_dev, "plain_per_step_poses_per_s": total / dt_plain,
             "speedup": dt_plain / dt_dev, "device_equals_plain": bool(same),
+            "first_8_pairs_poses": n_few, "first_8_pairs_device_poses_per_s": n_few / dt_dev_few,
+            "first_8_pairs_plain_100_pose_items_poses_per_s": n_few / dt_items,
+            "speedup_vs_plain_100_pose_items": dt_items / dt_dev_few, "items_equal_device": bool(same_items),
             "batched_pair_completion_ms_p50": float(np.percentile(pair_done_ms, 50)),
             "batched_pair_completion_ms_p99": float(np.percentile(pair_done_ms, 99)),
             "plain_pair_completion_ms_p50": float(np.percentile(pd, 50)),

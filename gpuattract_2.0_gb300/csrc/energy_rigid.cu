@@ -12,6 +12,8 @@
  * by one kernel in which a warp owns a pose (grid-stride over poses) and
  * nothing per bead leaves the SM; lanes 0..6 store the 28-byte Result_6D.
  */
+#include <atomic>
+
 #include "rigid_pose.cuh"
 
 namespace gba {
@@ -75,7 +77,18 @@ cudaError_t launch_rigid_energy(const RigidLaunch& L, int blocks, int threads, c
 	return cudaGetLastError();
 }
 
+/* resident blocks per SM, queried once per device, instantiation and block
+ * size (the query costs host time on every launch otherwise) */
 int rigid_blocks_per_sm(int threads, bool census, bool bound4) {
+	static std::atomic<int> cache[64][3][33];
+	int dev = 0;
+	cudaGetDevice(&dev);
+	const int v = census ? 0 : (bound4 ? 1 : 2), t = threads / 32;
+	const bool cacheable = dev >= 0 && dev < 64 && threads % 32 == 0 && t >= 1 && t <= 32;
+	if (cacheable) {
+		const int c = cache[dev][v][t].load(std::memory_order_relaxed);
+		if (c > 0) return c;
+	}
 	int nb = 0;
 	if (census)
 		cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, rigid_energy_kernel<true, false>, threads, 0);
@@ -83,7 +96,9 @@ int rigid_blocks_per_sm(int threads, bool census, bool bound4) {
 		cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, rigid_energy_kernel<false, true>, threads, 0);
 	else
 		cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, rigid_energy_kernel<false, false>, threads, 0);
-	return nb > 0 ? nb : 1;
+	nb = nb > 0 ? nb : 1;
+	if (cacheable) cache[dev][v][t].store(nb, std::memory_order_relaxed);
+	return nb;
 }
 
 }  // namespace gba

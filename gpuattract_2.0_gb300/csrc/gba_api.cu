@@ -119,6 +119,8 @@ Context::~Context() {
 	if (pinned_status) cudaFreeHost(pinned_status);
 	for (void* p : pinned_buf)
 		if (p) cudaFreeHost(p);
+	/* frees still in flight complete before the pool's memory is released */
+	if (scratch_pool) cudaMemPoolDestroy(scratch_pool);
 }
 
 const char* kind_name(ItemKind k) {
@@ -224,6 +226,22 @@ int gba_create(int device, gba_ctx** out) {
 	}
 	c->device = device;
 	cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device);
+	/* a private stream-ordered pool for per-call scratch that keeps its
+	 * memory reserved (without it the calls fall back to the default pool) */
+	cudaMemPoolProps props{};
+	props.allocType = cudaMemAllocationTypePinned;
+	props.location.type = cudaMemLocationTypeDevice;
+	props.location.id = device;
+	if (cudaMemPoolCreate(&c->scratch_pool, &props) == cudaSuccess) {
+		uint64_t keep = UINT64_MAX;
+		if (cudaMemPoolSetAttribute(c->scratch_pool, cudaMemPoolAttrReleaseThreshold, &keep) != cudaSuccess) {
+			cudaMemPoolDestroy(c->scratch_pool);
+			c->scratch_pool = nullptr;
+		}
+	} else {
+		c->scratch_pool = nullptr;
+	}
+	cudaGetLastError();
 	*out = c;
 	return GBA_OK;
 }
@@ -687,7 +705,7 @@ void Context::run_modes(ModesLaunch& L, cudaStream_t s) {
 }
 
 void Context::run_rigid(RigidLaunch& L, cudaStream_t s) {
-	StreamScratch scratch;
+	StreamScratch scratch(scratch_pool);
 	L.order = pose_order(L.dofs, 6, L.n, L.m.grid.outer, s, scratch);
 	const TuneParams tp = tuned("energy", L.n);
 	const int threads = tp.threads;

@@ -266,9 +266,9 @@ def bench_minimization(ctx, pkg, nthreads: int, with_cpu: bool):
     return out
 
 
-def bench_modes(ctx, pkg, n_poses: int, steps: int):
+def bench_modes(ctx, pkg, n_poses: int, steps: int, minimize: bool = True):
     """Config 2: receptor 1500 / ligand 600 beads with 5 modes each: modes
-    energy+gradient evals/s, and device vs plain minimization."""
+    energy+gradient evals/s, and (minimize) device vs plain minimization."""
     import torch
     wl = pkg.synth.make_config(2, n_poses=n_poses)
     rec, lig, par = ctx.upload_protein(wl.rec), ctx.upload_protein(wl.lig), ctx.upload_params(wl.params)
@@ -285,6 +285,11 @@ def bench_modes(ctx, pkg, n_poses: int, steps: int):
         ctx.energy_6d_modes(*ids, d, out=out)
     torch.cuda.synchronize()
     evals = 3 * len(wl.dofs) / (time.perf_counter() - t0)
+    if not minimize:
+        for i in (gr, gl, lig, rec, par):
+            ctx.release(i)
+        return {"workload": f"config 2: receptor {wl.rec.n} / ligand {wl.lig.n} beads, 5+5 modes; "
+                            f"{len(wl.dofs)} poses scored", "energy_evals_per_s": evals}
     sub = wl.dofs
     ctx.minimize_6d_modes(*ids, sub[:64], max_evals=10)
     t0 = time.perf_counter()
@@ -422,6 +427,21 @@ def bench_batched_uneven(ctx, pkg, pose_scale: float, steps: int):
             "plain_pair_completion_ms_p99": float(np.percentile(pd, 99))}
 
 
+def run_modes_only(args):
+    """`--suite modes`: the config-2 section alone (profiling captures of the
+    modes kernel); --no-min skips the minimizers."""
+    import torch
+    torch.cuda.set_device(0)
+    import __graft_entry__
+    pkg = __graft_entry__.load_package()
+    from gbattract.context import GbaContext
+    ctx = GbaContext(0)
+    res = bench_modes(ctx, pkg, n_poses=args.modes_poses, steps=200, minimize=not args.no_min)
+    ctx.close()
+    print(json.dumps({"suite": {"modes": res}}))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -433,8 +453,9 @@ def main():
     ap.add_argument("--ref-sample", type=int, default=2000)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-min", action="store_true", help="skip the minimization report")
-    ap.add_argument("--suite", default="default", choices=["default", "full"],
-                    help="full: also configs 2 (modes), 3 (adjoint), 4 (batched uneven pairs)")
+    ap.add_argument("--suite", default="default", choices=["default", "full", "modes"],
+                    help="full: also configs 2 (modes), 3 (adjoint), 4 (batched uneven pairs); "
+                         "modes: config 2 alone")
     ap.add_argument("--modes-poses", type=int, default=50000)
     ap.add_argument("--variant", default="order=1,octets=1",
                     help="layout / visiting-order variant timed, or 'search' to time all four "
@@ -451,6 +472,8 @@ def main():
         args.warmup = 3
     if args.impl == "reference":
         return run_reference(args)
+    if args.suite == "modes":
+        return run_modes_only(args)
 
     import torch
     rank, world, local = dist_env()

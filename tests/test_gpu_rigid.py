@@ -101,6 +101,47 @@ def test_edge_sizes(small_case, oracle, ctx):
         assert np.array_equal(out[: len(wl.dofs)], ctx.energy_6d(*ids, dofs[: len(wl.dofs)]))
 
 
+@pytest.mark.parametrize("n_lig", [1, 63, 64, 65, 129])
+def test_ligand_round_boundaries(pkg, oracle, ctx, n_lig):
+    """Ligands of 1, 63, 64, 65 and 129 beads: one, exactly full and
+    partially filled rounds of 64 staged beads, against the oracle."""
+    wl = pkg.synth.make_pair(0, 140, n_lig, 64, (12.0, 22.0), seed=300 + n_lig)
+    grid = oracle.build_grid(wl.rec, wl.params, pkg.GridOptions())
+    ids = upload(ctx, wl.rec, wl.lig, grid, wl.params)
+    got = ctx.energy_6d(*ids, wl.dofs)
+    ref, st = oracle.energy_6d(wl.rec, wl.lig, grid, wl.params, wl.dofs, stats=True)
+    for e in pose_errors(got, ref, st):
+        assert float(e.max()) <= RTOL
+    cen, _ = ctx.census_6d(*ids, wl.dofs)
+    for col, key in enumerate(("n_grid", "n_grid_charged", "n_nl", "n_nl_entries")):
+        assert np.array_equal(cen[:, col], st[key])
+
+
+def test_non_finite_poses_leave_the_others_alone(small_case, ctx):
+    """Poses with NaN or infinite translations or angles fail every grid and
+    neighbour-list bounds test, so they touch no grid memory and score zero
+    energy and force; the finite poses of the same batch keep their results
+    bit for bit (also through the visiting-order pass, which sends NaN keys
+    to cell 0)."""
+    wl, grid = small_case
+    ids = upload(ctx, wl.rec, wl.lig, grid, wl.params)
+    clean = ctx.energy_6d(*ids, wl.dofs)
+    bad = wl.dofs.copy()
+    rows = np.arange(0, len(bad), 3)
+    bad[rows[0::4], 0] = np.nan
+    bad[rows[1::4], 1] = np.inf
+    bad[rows[2::4], 3] = np.nan
+    bad[rows[3::4], 2] = -np.inf
+    keep = np.setdiff1d(np.arange(len(bad)), rows)
+    for n_rep in (1, 80):          # the second batch is large enough to be visiting-ordered
+        d = np.tile(bad, (n_rep, 1))
+        out = ctx.energy_6d(*ids, d)
+        for r in range(n_rep):
+            o = out[r * len(bad):(r + 1) * len(bad)]
+            assert np.array_equal(o[keep], clean[keep])
+            assert np.all(o[rows, :4] == 0.0)
+
+
 def test_pose_order_does_not_change_results(small_case, ctx):
     """Large batches are visited in Morton order; every pose keeps its slot."""
     wl, grid = small_case

@@ -631,9 +631,9 @@ def main():
                          "bytes_per_launch": bytes_launch, "kernel_ms_avg": 1000.0 * kernel_avg_s,
                          "kernel_launches_timed": kernel_launches},
             "cpu_baseline": cpu, "clocks": clk.summary(),
-            # per step: the fused energy kernel (+ the Morton-key kernel when the visiting
-            # order is on; the CUB radix-sort passes it feeds are library kernels)
-            "gpu_launches": args.steps * (2 if best.startswith("order=1") else 1),
+            # per step: the fused energy kernel (+ the three visiting-order kernels --
+            # cell counts, their prefix sum, the scatter -- when the order is on)
+            "gpu_launches": args.steps * (4 if best.startswith("order=1") else 1),
             "minimization": minim,
             "variants_ms": variants, "variant_timed": best, "kernel_options": args.kopts,
             "suite": suite or None,

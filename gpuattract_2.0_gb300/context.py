@@ -295,7 +295,7 @@ class GbaContext:
         self._check(self.lib.gba_grid_octets(self.h, grid, int(bool(enable))))
 
     def set_pose_order(self, enable: bool):
-        """Visit large batches in Morton order of the pose translation (default on)."""
+        """Visit large batches grouped by pose translation (default on)."""
         self._check(self.lib.gba_set_pose_order(self.h, int(bool(enable))))
 
     def set_kernel_options(self, flags: int):

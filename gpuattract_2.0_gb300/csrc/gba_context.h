@@ -122,8 +122,9 @@ struct ParamsItem : Item {
 	const float4* pair_table(float dPlateau2);
 };
 
-/* Morton visiting order of n poses computed in the given device memory
- * (pose_order.cu); throws ApiError if [buf, buf + cap) is too small. */
+/* Visiting order of n poses (grouped by translation cell) computed in the
+ * given device memory (pose_order.cu); throws ApiError if [buf, buf + cap)
+ * is too small. */
 const uint32_t* pose_order_in(const void* dofs, size_t stride_floats, size_t n, const DevIntrpl& box,
 		void* buf, size_t cap, cudaStream_t s);
 

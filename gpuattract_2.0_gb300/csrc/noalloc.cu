@@ -1,10 +1,11 @@
 /*
  * noalloc.cu -- gba_energy_6d_noalloc: the fused rigid energy launch of
- * gba_energy_6d for device-resident poses, with the Morton visiting-order
- * scratch taken from a fixed, statically allocated device array instead of
- * the stream-ordered allocator.  The call performs no device or host memory
- * allocation: no cudaMalloc / cudaMallocAsync / cudaFree, no allocating
- * library routine; CUB's radix sort runs on caller-supplied temporary storage.
+ * gba_energy_6d for device-resident poses, with the visiting-order scratch
+ * (translation-cell counts, each pose's cell and rank, the order) taken from a
+ * fixed, statically allocated device array instead of the stream-ordered
+ * allocator.  The call performs no device or host memory allocation: no
+ * cudaMalloc / cudaMallocAsync / cudaFree, no allocating library routine; the
+ * cell counts are cleared with cudaMemsetAsync on every call.
  *
  * Scratch: one file-scope __device__ array of kNoAllocScratchBytes per device
  * (2 MiB), addressed through cudaGetSymbolAddress on the first call made on

@@ -147,10 +147,12 @@ int gba_upload_params(gba_ctx* ctx, uint32_t num_types, const gba_ffparam* table
 /* Drops a data item (DataManager::remove). */
 int gba_release(gba_ctx* ctx, gba_id id);
 
-/* Batches of >= 4096 poses are visited in Morton order of their translation
- * (results unchanged, each pose keeps its slot) so that the poses resident on
- * the GPU at a time share grid regions in L2.  Enabled by default; 0 turns it
- * off.  No reference counterpart (a scheduling choice of this library). */
+/* Batches of >= 4096 poses are visited grouped by translation cell (32^3
+ * cells over the outer grid; multi-pair minimizer batches by pair and Morton
+ * order) -- results unchanged, each pose keeps its slot -- so that the poses
+ * resident on the GPU at a time share grid regions in L2.  Enabled by
+ * default; 0 turns it off.  No reference counterpart (a scheduling choice of
+ * this library). */
 int gba_set_pose_order(gba_ctx* ctx, int enable);
 
 /* Kernel implementation options (no reference counterpart; every option

@@ -143,7 +143,7 @@ def test_non_finite_poses_leave_the_others_alone(small_case, ctx):
 
 
 def test_pose_order_does_not_change_results(small_case, ctx):
-    """Large batches are visited in Morton order; every pose keeps its slot."""
+    """Large batches are visited grouped by translation; every pose keeps its slot."""
     wl, grid = small_case
     ids = upload(ctx, wl.rec, wl.lig, grid, wl.params)
     rng = np.random.default_rng(8)

@@ -192,9 +192,12 @@ struct Context {
 	const uint32_t* pose_order(const void* dofs, size_t stride_floats, size_t n, const DevIntrpl& box,
 			cudaStream_t s, StreamScratch& scratch);
 	DevBuffer order_buf;      /* visiting-order keys, indices and sort scratch */
+	DevBuffer rank_buf;       /* per pair of a batch: its place in the visiting order */
+	/* pair_rank (optional, device): the rank of each pair's poses in the
+	 * visiting order, else the pair index */
 	const uint32_t* pose_order_persistent(const void* dofs, size_t stride_floats, size_t n,
-			const DevIntrpl& box, const RigidModel* models, const uint32_t* pair_of, size_t npairs,
-			cudaStream_t s);
+			const DevIntrpl& box, const RigidModel* models, const uint32_t* pair_of, const uint32_t* pair_rank,
+			size_t npairs, cudaStream_t s);
 	TuneParams tuned(const std::string& kind, size_t n) const;
 	void run_minimize(MinLaunch& L, cudaStream_t s, int32_t* status_out);
 	void clear_graphs();

@@ -225,9 +225,22 @@ int gba_batch_minimize_6d(gba_ctx* ctx, const gba_pair_job* jobs, size_t njobs, 
 		for (size_t j = 0; j < njobs; ++j)
 			if (jobs[j].n) copy_in((void*)(L.start + G.offset[j]), jobs[j].start, jobs[j].n * sizeof(gba_dof6d), s);
 	}
-	/* visit poses grouped by pair, in Morton order of the start translation */
+	/* visit poses grouped by pair, in Morton order of the start translation;
+	 * pairs with larger ligands (more work per evaluation) first, so that the
+	 * poses still running when the queue empties are cheap ones */
+	const uint32_t* pair_rank = nullptr;
+	if (njobs > 1) {
+		std::vector<uint32_t> by_cost(njobs), rank(njobs);
+		for (size_t j = 0; j < njobs; ++j) by_cost[j] = (uint32_t)j;
+		std::stable_sort(by_cost.begin(), by_cost.end(), [&](uint32_t a, uint32_t b) {
+			return G.models[a].lig.n > G.models[b].lig.n;
+		});
+		for (size_t r = 0; r < njobs; ++r) rank[by_cost[r]] = (uint32_t)r;
+		ctx->rank_buf.upload(rank.data(), njobs * sizeof(uint32_t));
+		pair_rank = (const uint32_t*)ctx->rank_buf.ptr;
+	}
 	L.order = ctx->pose_order_persistent(L.start, 6, n, G.models[0].grid.outer, L.models, L.pair_of,
-			njobs, s);
+			pair_rank, njobs, s);
 	int32_t status = GBA_OK;
 	ctx->run_minimize(L, s, &status);
 	if (!single_dev) {

@@ -32,11 +32,12 @@ __device__ __forceinline__ uint32_t spread10(uint32_t v) {
 
 constexpr int kMortonBits = 8;   /* per axis: 256 cells across the outer-grid box */
 
-/* key = pair << 24 | Morton(translation in the pair's outer-grid box) */
+/* key = rank(pair) << 24 | Morton(translation in the pair's outer-grid box);
+ * rank = pair_rank[pair] when given, else the pair index */
 template <typename K>
 __global__ void order_keys_kernel(const float* __restrict__ dofs, size_t stride_floats, size_t n,
 		DevIntrpl box, const RigidModel* __restrict__ models, const uint32_t* __restrict__ pair_of,
-		K* __restrict__ keys, uint32_t* __restrict__ idx) {
+		const uint32_t* __restrict__ pair_rank, K* __restrict__ keys, uint32_t* __restrict__ idx) {
 	const size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
 	if (p >= n) return;
 	uint32_t pair = 0;
@@ -45,6 +46,7 @@ __global__ void order_keys_kernel(const float* __restrict__ dofs, size_t stride_
 		pair = __ldg(&pair_of[p]);
 		b = &models[pair].grid.outer;
 	}
+	const uint32_t rank = pair_rank ? __ldg(&pair_rank[pair]) : pair;
 	const float* d = dofs + p * stride_floats;
 	constexpr float cells = (float)(1 << kMortonBits);
 	uint32_t q[3];
@@ -56,7 +58,7 @@ __global__ void order_keys_kernel(const float* __restrict__ dofs, size_t stride_
 		q[a] = (uint32_t)t;
 	}
 	const uint32_t m = spread10(q[0]) | (spread10(q[1]) << 1) | (spread10(q[2]) << 2);
-	keys[p] = ((K)pair << (3 * kMortonBits)) | m;
+	keys[p] = ((K)rank << (3 * kMortonBits)) | m;
 	idx[p] = (uint32_t)p;
 }
 
@@ -72,7 +74,8 @@ size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
  * from `get(bytes)`; returns the ordered indices. */
 template <typename K, typename Get>
 const uint32_t* sort_keys(const void* dofs, size_t stride_floats, size_t n, const DevIntrpl& box,
-		const RigidModel* models, const uint32_t* pair_of, int end_bit, cudaStream_t s, Get get) {
+		const RigidModel* models, const uint32_t* pair_of, const uint32_t* pair_rank, int end_bit,
+		cudaStream_t s, Get get) {
 	cub::DoubleBuffer<K> kb(nullptr, nullptr);
 	cub::DoubleBuffer<uint32_t> ib(nullptr, nullptr);
 	size_t tmp = 0;
@@ -86,7 +89,7 @@ const uint32_t* sort_keys(const void* dofs, size_t stride_floats, size_t n, cons
 	uint32_t* i1 = (uint32_t*)(base + 2 * kbytes + ibytes);
 	void* t = base + 2 * kbytes + 2 * ibytes;
 	order_keys_kernel<K><<<(unsigned)((n + 255) / 256), 256, 0, s>>>((const float*)dofs, stride_floats,
-			n, box, models, pair_of, k0, i0);
+			n, box, models, pair_of, pair_rank, k0, i0);
 	check_cuda(cudaGetLastError(), "pose order: keys");
 	kb = cub::DoubleBuffer<K>(k0, k1);
 	ib = cub::DoubleBuffer<uint32_t>(i0, i1);
@@ -181,11 +184,13 @@ const uint32_t* bucket_order(const void* dofs, size_t stride_floats, size_t n, c
 /* 32-bit keys while they fit (up to 256 pairs), else 64-bit. */
 template <typename Get>
 const uint32_t* sort_order(const void* dofs, size_t stride_floats, size_t n, const DevIntrpl& box,
-		const RigidModel* models, const uint32_t* pair_of, size_t npairs, cudaStream_t s, Get get) {
+		const RigidModel* models, const uint32_t* pair_of, const uint32_t* pair_rank, size_t npairs,
+		cudaStream_t s, Get get) {
 	const int end_bit = key_bits(npairs);
 	if (end_bit <= 32)
-		return sort_keys<uint32_t>(dofs, stride_floats, n, box, models, pair_of, end_bit, s, get);
-	return sort_keys<unsigned long long>(dofs, stride_floats, n, box, models, pair_of, end_bit, s, get);
+		return sort_keys<uint32_t>(dofs, stride_floats, n, box, models, pair_of, pair_rank, end_bit, s, get);
+	return sort_keys<unsigned long long>(dofs, stride_floats, n, box, models, pair_of, pair_rank, end_bit, s,
+			get);
 }
 
 }  // namespace
@@ -201,10 +206,10 @@ const uint32_t* Context::pose_order(const void* dofs, size_t stride_floats, size
 /* Order kept in context buffers (stable addresses for the cached minimizer
  * graph); the caller holds stage_mu. */
 const uint32_t* Context::pose_order_persistent(const void* dofs, size_t stride_floats, size_t n,
-		const DevIntrpl& box, const RigidModel* models, const uint32_t* pair_of, size_t npairs,
-		cudaStream_t s) {
+		const DevIntrpl& box, const RigidModel* models, const uint32_t* pair_of, const uint32_t* pair_rank,
+		size_t npairs, cudaStream_t s) {
 	if (!order_enabled || n < kOrderMinPoses || n > 0x7fffffffull) return nullptr;
-	return sort_order(dofs, stride_floats, n, box, models, pair_of, npairs, s,
+	return sort_order(dofs, stride_floats, n, box, models, pair_of, pair_rank, npairs, s,
 			[&](size_t bytes) {
 				DevBuffer& b = order_buf;
 				if (b.bytes < bytes) b.alloc(bytes + bytes / 4 + 256);

@@ -10,7 +10,9 @@
  *   term of ChargePotForce (src/model/forcefield.h:87-146),
  * with per-bead charges and per-type-pair (r0, eps) as free parameters.
  * Candidate receptor beads come from the receptor's neighbour-list grid
- * (voxel lists cover every bead within cutoff of a ligand bead).
+ * (voxel lists cover every bead within cutoff of a ligand bead).  Like the
+ * rigid kernel, a warp takes one pose and walks the flattened
+ * (bead, neighbour) pairs of 64 staged ligand beads at a time.
  *
  * The backward kernel recomputes the transformed coordinates and pair terms
  * (nothing is stored by the forward) and produces, scaled by the upstream
@@ -22,8 +24,8 @@
  * Parameter gradients accumulate in FP64 shared-memory partials per block and
  * are flushed with FP64 global atomics.
  */
-#include "energy_dev.cuh"
 #include "gba_context.h"
+#include "rigid_pose.cuh"
 
 namespace gba {
 
@@ -48,40 +50,84 @@ struct PairwiseLaunch {
 	double* g_qrec;        /* rec.n */
 	double* g_r0;          /* T*T */
 	double* g_eps;         /* T*T */
+	const float4* tab;     /* 3*T*T: per type pair the constants of lj86 (lj_table_kernel) */
 };
 
 namespace {
 
-/* LJ energy, radial force factor and d/d(r0, eps) of one 8-6 pair. */
-__device__ __forceinline__ void lj86(float r2, float ir2, float r0, float eps, int ipon, float& e,
-		float& fb, float& de_dr0, float& de_deps) {
+/* Per type pair (r0, eps, ipon), the constants of the 8-6 term and of its
+ * derivatives, computed once per call: {rc, ac, emin, rmin2},
+ * {-3 emin / rc, 4 emin / ac, 8 r0^7, 6 r0^5}, {r0^8, r0^6, eps, ipon}, with
+ * rc = eps r0^8, ac = eps r0^6, emin = -27 ac^4 / (256 rc^3),
+ * rmin2 = 4 rc / (3 ac) as readParamTableFromFile derives them
+ * (src/fileIO/readFile.cpp:484-497).  The pair loop then divides nothing but
+ * 1/r^2. */
+__global__ void lj_table_kernel(uint32_t T2, const float* __restrict__ r0v, const float* __restrict__ epsv,
+		const int32_t* __restrict__ ipon, float4* __restrict__ tab) {
+	const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+	if (k >= T2) return;
+	const float r0 = r0v[k], eps = epsv[k];
 	const float r0_2 = r0 * r0, r0_6 = r0_2 * r0_2 * r0_2, r0_8 = r0_6 * r0_2;
 	const float rc = eps * r0_8, ac = eps * r0_6;
+	const bool ok = ac > 0.f && rc > 0.f;
+	const float emin = ok ? -27.f * (ac * ac) * (ac * ac) / (256.f * rc * rc * rc) : 0.f;
+	const float rmin2 = ok ? 4.f * rc / (3.f * ac) : 0.f;
+	tab[3 * k] = make_float4(rc, ac, emin, rmin2);
+	tab[3 * k + 1] = make_float4(ok ? -3.f * emin / rc : 0.f, ok ? 4.f * emin / ac : 0.f, 8.f * (r0_6 * r0),
+			6.f * (r0_2 * r0_2 * r0));
+	tab[3 * k + 2] = make_float4(r0_8, r0_6, eps, (float)ipon[k]);
+}
+
+/* LJ energy, radial force factor and d/d(r0, eps) of one 8-6 pair from the
+ * type pair's table entry t. */
+template <bool DERIV>
+__device__ __forceinline__ void lj86(float r2, float ir2, const float4* __restrict__ t, float& e, float& fb,
+		float& de_dr0, float& de_deps) {
+	const float4 c = __ldg(t);
+	const float4 k = DERIV ? __ldg(t + 1) : make_float4(0.f, 0.f, 0.f, 0.f);
+	const float4 m = __ldg(t + 2);
+	const float rc = c.x, ac = c.y, emin = c.z, rmin2 = c.w, iv = m.w;
 	const float ir6 = ir2 * ir2 * ir2, ir8 = ir6 * ir2;
 	const float vlj = rc * ir8 - ac * ir6;
-	const float emin = (ac > 0.f && rc > 0.f) ? -27.f * (ac * ac) * (ac * ac) / (256.f * rc * rc * rc) : 0.f;
-	const float rmin2 = (ac > 0.f && rc > 0.f) ? 4.f * rc / (3.f * ac) : 0.f;
-	const float iv = (float)ipon;
-	float de_drc, de_dac;
+	float de_drc = 0.f, de_dac = 0.f;
 	fb = 6.f * vlj + 2.f * rc * ir8;     /* force factor: f = fb * d / r^2 */
 	if (r2 < rmin2) {
 		e = vlj + (iv - 1.f) * emin;
-		de_drc = ir8 + (iv - 1.f) * (-3.f * emin / rc);
-		de_dac = -ir6 + (iv - 1.f) * (4.f * emin / ac);
+		if (DERIV) {
+			de_drc = ir8 + (iv - 1.f) * k.x;
+			de_dac = -ir6 + (iv - 1.f) * k.y;
+		}
 	} else {
 		e = iv * vlj;
 		fb *= iv;
-		de_drc = iv * ir8;
-		de_dac = -iv * ir6;
+		if (DERIV) {
+			de_drc = iv * ir8;
+			de_dac = -iv * ir6;
+		}
 	}
 	/* rc = eps r0^8, ac = eps r0^6 */
-	de_dr0 = eps * (8.f * (r0_6 * r0) * de_drc + 6.f * (r0_2 * r0_2 * r0) * de_dac);
-	de_deps = r0_8 * de_drc + r0_6 * de_dac;
+	de_dr0 = DERIV ? m.z * (k.z * de_drc + k.w * de_dac) : 0.f;
+	de_deps = DERIV ? m.x * de_drc + m.y * de_dac : 0.f;
 }
 
+/* Per-warp staging of the pairwise kernels: one round of 64 ligand beads. */
+struct PairStage {
+	float4 pq[kBeadsPerRound];       /* transformed x, y, z; charge */
+	float4 ut[kBeadsPerRound];       /* unrotated x, y, z (torque lever); type (bits) */
+	uint32_t lbase[kBeadsPerRound];  /* list start - first flattened pair of the slot */
+	float gq[kBeadsPerRound];        /* backward: dE/dq of the slot's bead over this round */
+	uint8_t own[64];                 /* PairWindow: slot of the bead starting at window position b */
+};
+constexpr int kPairwiseThreads = 256;
+
+/* One warp per pose, the ligand in rounds of 64 beads like the rigid kernel:
+ * lane-per-bead staging (transform, neighbour-list voxel), then the round's
+ * flattened (bead, neighbour) pairs in windows of 64, two per lane, so that
+ * uneven list lengths do not idle lanes. */
 template <bool BACKWARD>
-__global__ void __launch_bounds__(256) pairwise_kernel(const PairwiseLaunch L) {
+__global__ void __launch_bounds__(kPairwiseThreads) pairwise_kernel(const PairwiseLaunch L) {
 	extern __shared__ double sm[];
+	__shared__ PairStage stage[kPairwiseThreads / 32];
 	const uint32_t T2 = L.T * L.T;
 	double* s_r0 = sm;
 	double* s_eps = sm + T2;
@@ -93,6 +139,7 @@ __global__ void __launch_bounds__(256) pairwise_kernel(const PairwiseLaunch L) {
 		__syncthreads();
 	}
 	const int lane = threadIdx.x & 31;
+	PairStage& W = stage[threadIdx.x >> 5];
 	const size_t warp = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
 	const size_t nwarps = ((size_t)gridDim.x * blockDim.x) >> 5;
 	const bool cdiel = L.dielec == GBA_DIELEC_CONSTANT;
@@ -106,60 +153,91 @@ __global__ void __launch_bounds__(256) pairwise_kernel(const PairwiseLaunch L) {
 		const float w = BACKWARD ? __ldg(&L.gE[p]) : 0.f;
 		float sE = 0.f, sFx = 0.f, sFy = 0.f, sFz = 0.f;
 		float Tq[9] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-		for (uint32_t i = lane; i < L.lig.n; i += 32) {
-			const float4 b = __ldg(&L.lig.xyzq[i]);
-			const uint32_t tl = __ldg(&L.lig.tm[i]) & 0xffffu;
-			if (tl == 0) continue;
-			float px, py, pz;
-			rot_apply(R.m, b.x, b.y, b.z, px, py, pz);
-			px = fadd(px, c[0]); py = fadd(py, c[1]); pz = fadd(pz, c[2]);
-			if (nl_out(L.nl, px, py, pz)) continue;
-			const int ix = min(max((int)roundf(fmul(fsub(px, L.nl.pos[0]), L.nl.dVox_inv)), 0), (int)L.nl.dimN[0] - 1);
-			const int iy = min(max((int)roundf(fmul(fsub(py, L.nl.pos[1]), L.nl.dVox_inv)), 0), (int)L.nl.dimN[1] - 1);
-			const int iz = min(max((int)roundf(fmul(fsub(pz, L.nl.pos[2]), L.nl.dVox_inv)), 0), (int)L.nl.dimN[2] - 1);
-			const uint2 d = __ldg(&L.nl.grid[L.nl.dimN[0] * (iz * L.nl.dimN[1] + iy) + ix]);
-			const float qi = __ldg(&L.q_lig[i]);
-			float fx = 0.f, fy = 0.f, fz = 0.f, e = 0.f, gqi = 0.f;
-			for (uint32_t k = 0; k < d.x; ++k) {
-				const uint32_t j = __ldg(&L.nl.list[d.y + k]);
-				const uint32_t tr = __ldg(&L.rec.tm[j]) & 0xffffu;
-				if (tr == 0) continue;
-				const float4 r = __ldg(&L.rec.xyzq[j]);
-				const float dx = px - r.x, dy = py - r.y, dz = pz - r.z;
-				const float r2 = dx * dx + dy * dy + dz * dz;
-				if (!(r2 < L.cut2)) continue;
-				const float ir2 = 1.0f / r2;
-				const uint32_t tp = L.T * (tr - 1) + (tl - 1);
-				float el, fb, dr0, deps;
-				lj86(r2, ir2, __ldg(&L.r0[tp]), __ldg(&L.eps[tp]), __ldg(&L.ipon[tp]), el, fb, dr0, deps);
-				/* Coulomb, no |q q| switch: smooth in the charges */
-				const float qj = __ldg(&L.q_rec[j]);
-				float dd, fcf;
-				if (cdiel) {
-					const float ir = sqrtf(ir2);
-					dd = ir - 0.02f;
-					fcf = dd > 0.f ? ir : 0.f;      /* f = ffelec qq (1/r) d / r^2 */
-				} else {
-					dd = ir2 - 4.0e-4f;
-					fcf = dd > 0.f ? 2.f * ir2 : 0.f;  /* f = ffelec qq 2/r^2 d / r^2 */
-				}
-				dd = fmaxf(dd, 0.f);
-				const float qq = L.ffelec * qi * qj;
-				e += el + qq * dd;
-				const float ff = (fb + qq * fcf) * ir2;
-				fx += ff * dx; fy += ff * dy; fz += ff * dz;
-				if (BACKWARD) {
-					gqi += L.ffelec * qj * dd;
-					atomicAdd(&s_qr[j], (double)(w * (L.ffelec * qi * dd)));
-					atomicAdd(&s_r0[tp], (double)(w * dr0));
-					atomicAdd(&s_eps[tp], (double)(w * deps));
+		for (uint32_t i0 = 0; i0 < L.lig.n; i0 += kBeadsPerRound) {
+			uint32_t nln[2];
+#pragma unroll
+			for (int h = 0; h < 2; ++h) {
+				const int s = lane + 32 * h;
+				const uint32_t i = i0 + s;
+				nln[h] = 0;
+				if (i < L.lig.n) {
+					const float4 b = __ldg(&L.lig.xyzq[i]);
+					const uint32_t tl = __ldg(&L.lig.tm[i]) & 0xffffu;
+					if (tl != 0) {
+						float px, py, pz;
+						rot_apply(R.m, b.x, b.y, b.z, px, py, pz);
+						px = fadd(px, c[0]); py = fadd(py, c[1]); pz = fadd(pz, c[2]);
+						W.pq[s] = make_float4(px, py, pz, __ldg(&L.q_lig[i]));
+						W.ut[s] = make_float4(b.x, b.y, b.z, __uint_as_float(tl));
+						if (BACKWARD) W.gq[s] = 0.f;
+						bool in_nl;
+						nln[h] = stage_nl(L.nl, px, py, pz, s, W, in_nl);
+					}
 				}
 			}
-			if (BACKWARD && gqi != 0.f) atomicAdd(&s_ql[i], (double)(w * gqi));
-			sE += e; sFx += fx; sFy += fy; sFz += fz;
-			Tq[0] += b.x * fx; Tq[1] += b.y * fx; Tq[2] += b.z * fx;
-			Tq[3] += b.x * fy; Tq[4] += b.y * fy; Tq[5] += b.z * fy;
-			Tq[6] += b.x * fz; Tq[7] += b.y * fz; Tq[8] += b.z * fz;
+			uint32_t start[2];
+			const uint32_t n_pair = queue_pairs(W, nln, lane, start);
+			__syncwarp();
+			PairWindow win;
+			for (uint32_t w0 = 0; w0 < n_pair; w0 += 64) {
+				uint32_t so[2];
+				win.owners(W, w0, start, nln, lane, so[0], so[1]);
+#pragma unroll
+				for (int h = 0; h < 2; ++h) {
+					const uint32_t q = w0 + 32 * h + lane;
+					if (q >= n_pair) continue;
+					const uint32_t s = so[h];
+					const uint32_t j = __ldg(&L.nl.list[W.lbase[s] + q]);
+					const uint32_t tr = __ldg(&L.rec.tm[j]) & 0xffffu;
+					if (tr == 0) continue;
+					const float4 r = __ldg(&L.rec.xyzq[j]);
+					const float4 b = W.pq[s];
+					const float dx = b.x - r.x, dy = b.y - r.y, dz = b.z - r.z;
+					const float r2 = dx * dx + dy * dy + dz * dz;
+					if (!(r2 < L.cut2)) continue;
+					const float4 u = W.ut[s];
+					const uint32_t tl = __float_as_uint(u.w);
+					const float ir2 = __frcp_rn(r2);      /* = 1.0f / r2, correctly rounded */
+					const uint32_t tp = L.T * (tr - 1) + (tl - 1);
+					float el, fb, dr0, deps;
+					lj86<BACKWARD>(r2, ir2, L.tab + 3 * (size_t)tp, el, fb, dr0, deps);
+					/* Coulomb, no |q q| switch: smooth in the charges */
+					const float qi = b.w, qj = __ldg(&L.q_rec[j]);
+					float dd, fcf;
+					if (cdiel) {
+						const float ir = sqrtf(ir2);
+						dd = ir - 0.02f;
+						fcf = dd > 0.f ? ir : 0.f;      /* f = ffelec qq (1/r) d / r^2 */
+					} else {
+						dd = ir2 - 4.0e-4f;
+						fcf = dd > 0.f ? 2.f * ir2 : 0.f;  /* f = ffelec qq 2/r^2 d / r^2 */
+					}
+					dd = fmaxf(dd, 0.f);
+					const float qq = L.ffelec * qi * qj;
+					sE += el + qq * dd;
+					if (BACKWARD) {
+						const float ff = (fb + qq * fcf) * ir2;
+						const float fx = ff * dx, fy = ff * dy, fz = ff * dz;
+						sFx += fx; sFy += fy; sFz += fz;
+						Tq[0] += u.x * fx; Tq[1] += u.y * fx; Tq[2] += u.z * fx;
+						Tq[3] += u.x * fy; Tq[4] += u.y * fy; Tq[5] += u.z * fy;
+						Tq[6] += u.x * fz; Tq[7] += u.y * fz; Tq[8] += u.z * fz;
+						atomicAdd(&W.gq[s], L.ffelec * qj * dd);
+						atomicAdd(&s_qr[j], (double)(w * (L.ffelec * qi * dd)));
+						atomicAdd(&s_r0[tp], (double)(w * dr0));
+						atomicAdd(&s_eps[tp], (double)(w * deps));
+					}
+				}
+			}
+			if (BACKWARD) {
+				__syncwarp();
+#pragma unroll
+				for (int h = 0; h < 2; ++h) {
+					const int s = lane + 32 * h;
+					if (nln[h] && W.gq[s] != 0.f) atomicAdd(&s_ql[i0 + s], (double)(w * W.gq[s]));
+				}
+			}
+			__syncwarp();
 		}
 		if (!BACKWARD) {
 			sE = warp_sum(sE);
@@ -254,9 +332,18 @@ extern "C" int gba_pairwise_6d(gba_ctx* ctx, gba_id rec, gba_id lig, gba_id grid
 		L.g_r0 = g_r0;
 		L.g_eps = g_eps;
 		cudaStream_t s = (cudaStream_t)stream;
-		const int threads = 256;
+		/* per-call constants of the 8-6 term per type pair (r0, eps change per call) */
+		const uint32_t T2 = L.T * L.T;
+		StreamScratch scratch(ctx->scratch_pool);
+		float4* tab = (float4*)scratch.get(3 * (size_t)std::max<uint32_t>(T2, 1) * sizeof(float4), s);
+		if (T2 > 0) {
+			lj_table_kernel<<<(T2 + 255) / 256, 256, 0, s>>>(T2, L.r0, L.eps, L.ipon, tab);
+			check_cuda(cudaGetLastError(), "pairwise: parameter table");
+		}
+		L.tab = tab;
+		const int threads = kPairwiseThreads;
 		const size_t smem = backward ? sizeof(double) * (2 * (size_t)L.T * L.T + L.lig.n + L.rec.n) : 0;
-		if (smem > 200 * 1024)
+		if (smem + sizeof(PairStage) * (kPairwiseThreads / 32) > 200 * 1024)
 			throw ApiError(GBA_ERR_INVALID_ARGUMENT, "gba_pairwise_6d: proteins/types too large for the adjoint's shared partials");
 		size_t blocks;
 		if (backward) {

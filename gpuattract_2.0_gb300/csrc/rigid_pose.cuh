@@ -144,8 +144,9 @@ __device__ __forceinline__ uint32_t stage_grid(const DevGrid& G, float px, float
 /* NL voxel lookup of a staged bead (type != 0), NLPotForce's
  * src/model/neighborlist.h:59-66: stores the list start (queue_pairs turns it
  * into the slot's list base) and returns the list length (0 outside). */
+template <class Stage>
 __device__ __forceinline__ uint32_t stage_nl(const DevNL& nl, float px, float py, float pz, int s,
-		WarpStage& W, bool& in_nl) {
+		Stage& W, bool& in_nl) {
 	in_nl = false;
 	if (nl_out(nl, px, py, pz)) return 0;
 	const int ix = min(max((int)roundf(fmul(fsub(px, nl.pos[0]), nl.dVox_inv)), 0), (int)nl.dimN[0] - 1);
@@ -211,7 +212,8 @@ __device__ __forceinline__ uint32_t queue_lookups(WarpStage& W, const uint32_t n
  * lane + 32); turns each slot's list start into its list base (list index of
  * flattened pair k = lbase + k) and returns the number of pairs of the round
  * and, per lane, the first flattened pair of its two slots. */
-__device__ __forceinline__ uint32_t queue_pairs(WarpStage& W, const uint32_t nln[2], int lane,
+template <class Stage>
+__device__ __forceinline__ uint32_t queue_pairs(Stage& W, const uint32_t nln[2], int lane,
 		uint32_t start[2]) {
 	const uint32_t a_incl = warp_incl_scan(nln[0], lane);
 	const uint32_t a_tot = __shfl_sync(GBA_FULL_MASK, a_incl, 31);
@@ -231,7 +233,8 @@ __device__ __forceinline__ uint32_t queue_pairs(WarpStage& W, const uint32_t nln
 struct PairWindow {
 	uint32_t carry = 0;
 	/* lane gets the owners of pairs w + lane and w + 32 + lane */
-	__device__ __forceinline__ void owners(WarpStage& W, uint32_t w, const uint32_t start[2],
+	template <class Stage>
+	__device__ __forceinline__ void owners(Stage& W, uint32_t w, const uint32_t start[2],
 			const uint32_t len[2], int lane, uint32_t& sa, uint32_t& sb) {
 		uint32_t lo = 0, hi = 0;
 #pragma unroll

@@ -347,17 +347,24 @@ def bench_adjoint(ctx, pkg, n_poses: int):
         E = PairwiseEnergy.apply(d, ql, qr, r0, eps, sysm)
         E.sum().backward()
 
-    fb()
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for _ in range(3):
-        fb()
-    torch.cuda.synchronize()
-    rate = 3 * len(wl.dofs) / (time.perf_counter() - t0)
+    def fwd():
+        with torch.no_grad():
+            PairwiseEnergy.apply(d, ql, qr, r0, eps, sysm)
+
+    rates = {}
+    for name, f in (("fwd_bwd_evals_per_s", fb), ("fwd_evals_per_s", fwd)):
+        f()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(3):
+            f()
+        torch.cuda.synchronize()
+        rates[name] = 3 * len(wl.dofs) / (time.perf_counter() - t0)
     for i in (grid, lig, rec, par):
         ctx.release(i)
     return {"workload": f"config 3: receptor {wl.rec.n} / ligand {wl.lig.n} beads, {len(wl.dofs)} poses, "
-                        "10 A pairwise cutoff", "fwd_bwd_evals_per_s": rate}
+                        "10 A pairwise cutoff", **rates,
+            "timing": "wall clock of 3 synchronised torch.autograd calls"}
 
 
 def bench_batched_uneven(ctx, pkg, pose_scale: float, steps: int):
@@ -451,6 +458,25 @@ def run_modes_only(args):
     return 0
 
 
+def run_section_only(args):
+    """`--suite adjoint` / `--suite minimize`: the config-3 or the config-0
+    section alone (profiling captures of the pairwise kernels or of the
+    device minimizer)."""
+    import torch
+    torch.cuda.set_device(0)
+    import __graft_entry__
+    pkg = __graft_entry__.load_package()
+    from gbattract.context import GbaContext
+    ctx = GbaContext(0)
+    if args.suite == "adjoint":
+        res = bench_adjoint(ctx, pkg, n_poses=args.poses or 10_000)
+    else:
+        res = bench_minimization(ctx, pkg, nthreads=os.cpu_count() or 1, with_cpu=not args.no_cpu)
+    ctx.close()
+    print(json.dumps({"suite": {args.suite: res}}))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -462,9 +488,10 @@ def main():
     ap.add_argument("--ref-sample", type=int, default=2000)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-min", action="store_true", help="skip the minimization report")
-    ap.add_argument("--suite", default="default", choices=["default", "full", "modes"],
+    ap.add_argument("--suite", default="default", choices=["default", "full", "modes", "adjoint", "minimize"],
                     help="full: also configs 2 (modes), 3 (adjoint), 4 (batched uneven pairs); "
-                         "modes: config 2 alone")
+                         "modes: config 2 alone; adjoint: config 3 alone; minimize: config 0's "
+                         "minimization alone")
     ap.add_argument("--modes-poses", type=int, default=50000)
     ap.add_argument("--variant", default="order=1,octets=1",
                     help="layout / visiting-order variant timed, or 'search' to time all four "
@@ -483,6 +510,8 @@ def main():
         return run_reference(args)
     if args.suite == "modes":
         return run_modes_only(args)
+    if args.suite in ("adjoint", "minimize"):
+        return run_section_only(args)
 
     import torch
     rank, world, local = dist_env()

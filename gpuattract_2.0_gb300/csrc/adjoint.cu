@@ -51,6 +51,7 @@ struct PairwiseLaunch {
 	double* g_r0;          /* T*T */
 	double* g_eps;         /* T*T */
 	const float4* tab;     /* 3*T*T: per type pair the constants of lj86 (lj_table_kernel) */
+	unsigned long long* next;   /* pose counter, zero at launch (PoseFeed) */
 };
 
 namespace {
@@ -123,7 +124,8 @@ constexpr int kPairwiseThreads = 256;
 /* One warp per pose, the ligand in rounds of 64 beads like the rigid kernel:
  * lane-per-bead staging (transform, neighbour-list voxel), then the round's
  * flattened (bead, neighbour) pairs in windows of 64, two per lane, so that
- * uneven list lengths do not idle lanes. */
+ * uneven list lengths do not idle lanes.  A warp takes its next pose from a
+ * global counter when it finishes one (PoseFeed). */
 template <bool BACKWARD>
 __global__ void __launch_bounds__(kPairwiseThreads) pairwise_kernel(const PairwiseLaunch L) {
 	extern __shared__ double sm[];
@@ -140,10 +142,9 @@ __global__ void __launch_bounds__(kPairwiseThreads) pairwise_kernel(const Pairwi
 	}
 	const int lane = threadIdx.x & 31;
 	PairStage& W = stage[threadIdx.x >> 5];
-	const size_t warp = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-	const size_t nwarps = ((size_t)gridDim.x * blockDim.x) >> 5;
 	const bool cdiel = L.dielec == GBA_DIELEC_CONSTANT;
-	for (size_t p = warp; p < L.n; p += nwarps) {
+	PoseFeed feed(L.next);
+	for (size_t p = feed.take(lane); p < L.n; p = feed.take(lane)) {
 		const float* dofp = reinterpret_cast<const float*>(L.dofs + p);
 		const float dv = lane < 6 ? __ldg(dofp + lane) : 0.f;
 		float c[6];
@@ -336,6 +337,8 @@ extern "C" int gba_pairwise_6d(gba_ctx* ctx, gba_id rec, gba_id lig, gba_id grid
 		const uint32_t T2 = L.T * L.T;
 		StreamScratch scratch(ctx->scratch_pool);
 		float4* tab = (float4*)scratch.get(3 * (size_t)std::max<uint32_t>(T2, 1) * sizeof(float4), s);
+		L.next = (unsigned long long*)scratch.get(sizeof(unsigned long long), s);
+		check_cuda(cudaMemsetAsync(L.next, 0, sizeof(unsigned long long), s), "pairwise: pose counter");
 		if (T2 > 0) {
 			lj_table_kernel<<<(T2 + 255) / 256, 256, 0, s>>>(T2, L.r0, L.eps, L.ipon, tab);
 			check_cuda(cudaGetLastError(), "pairwise: parameter table");

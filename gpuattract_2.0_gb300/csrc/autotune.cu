@@ -113,6 +113,8 @@ extern "C" int gba_autotune(gba_ctx* ctx, gba_id rec, gba_id lig, gba_id grid, g
 			check_cuda(cudaMemcpy(d, sample, n * sizeof(gba_dof6d), cudaMemcpyDefault), "sample");
 			gba_result6d* r = (gba_result6d*)ctx->staging(1, n * sizeof(gba_result6d));
 			EventTimer T;
+			StreamScratch scratch(ctx->scratch_pool);
+			unsigned long long* next = (unsigned long long*)scratch.get(sizeof(unsigned long long), s);
 			if (!have_e) {
 				best_e = 1e30f;
 				for (int threads : {128, 256}) {
@@ -122,9 +124,11 @@ extern "C" int gba_autotune(gba_ctx* ctx, gba_id rec, gba_id lig, gba_id grid, g
 						L.dofs = d;
 						L.out = r;
 						L.n = n;
+						L.next = next;
 						const size_t blocks = std::max<size_t>(1, std::min<size_t>(
 								(n + threads / 32 - 1) / (threads / 32), (size_t)ctx->num_sms * bps));
 						const float ms = T.best_ms([&] {
+							check_cuda(cudaMemsetAsync(next, 0, sizeof(unsigned long long), s), "tune: pose counter");
 							check_cuda(launch_rigid_energy(L, (int)blocks, threads, s), "tune launch");
 						}, s);
 						if (ms < best_e) {

@@ -187,6 +187,31 @@ __device__ __forceinline__ void charge_pot_force(float dr2_inv, float dx, float 
 	}
 }
 
+/* Pose indices of one warp, identical on all lanes.  With a counter (zero
+ * at launch) the warp takes the next unclaimed index whenever it finishes a
+ * pose: per-pose cost varies by orders of magnitude (contact poses walk
+ * thousands of neighbour pairs, distant ones none), and a fixed stride left
+ * warps idle while others finished their share.  Without one, the fixed
+ * stride warp, warp + nwarps, ... */
+struct PoseFeed {
+	unsigned long long* next;
+	size_t k, stride;
+	__device__ __forceinline__ PoseFeed(unsigned long long* counter)
+		: next(counter),
+		  k(((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5),
+		  stride(((size_t)gridDim.x * blockDim.x) >> 5) {}
+	__device__ __forceinline__ size_t take(int lane) {
+		if (next) {
+			unsigned long long t = 0;
+			if (lane == 0) t = atomicAdd(next, 1ull);
+			return (size_t)__shfl_sync(GBA_FULL_MASK, t, 0);
+		}
+		const size_t r = k;
+		k += stride;
+		return r;
+	}
+};
+
 /* Butterfly sum across the warp. */
 __device__ __forceinline__ float warp_sum(float v) {
 #pragma unroll

@@ -376,9 +376,8 @@ __global__ void __launch_bounds__(kModesThreads) modes_energy_kernel(const Modes
 	ModeStage<MM>* ms = reinterpret_cast<ModeStage<MM>*>(modes_dyn_smem);
 	const int lane = threadIdx.x & 31;
 	const int wib = threadIdx.x >> 5;
-	const size_t warp = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-	const size_t nwarps = ((size_t)gridDim.x * blockDim.x) >> 5;
-	for (size_t p = warp; p < L.n; p += nwarps) {
+	PoseFeed feed(L.next);
+	for (size_t p = feed.take(lane); p < L.n; p = feed.take(lane)) {
 		const float* d = reinterpret_cast<const float*>(L.dofs + p);
 		const float dv = lane < 26 ? __ldg(d + lane) : 0.f;
 		const float v = eval_pose_modes<MM>(L, dv, lane, stage[wib], ms[wib]);

@@ -24,9 +24,8 @@ template <bool CENSUS, bool BOUND4>
 __global__ void __launch_bounds__(256, BOUND4 ? 4 : 1) rigid_energy_kernel(const RigidLaunch L) {
 	__shared__ WarpStage stage[8];   /* one per warp of a <=256-thread block */
 	const int lane = threadIdx.x & 31;
-	const size_t warp = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-	const size_t nwarps = ((size_t)gridDim.x * blockDim.x) >> 5;
-	for (size_t k = warp; k < L.n; k += nwarps) {
+	PoseFeed feed(L.next);
+	for (size_t k = feed.take(lane); k < L.n; k = feed.take(lane)) {
 		const size_t p = L.order ? (size_t)__ldg(&L.order[k]) : k;
 		const float* dofp = reinterpret_cast<const float*>(L.dofs + p);
 		const float dv = lane < 6 ? __ldg(dofp + lane) : 0.f;
@@ -47,9 +46,8 @@ __global__ void __launch_bounds__(256, BOUND4 ? 4 : 1) rigid_energy_kernel(const
 __global__ void __launch_bounds__(256) batch_energy_kernel(const BatchEnergyLaunch L) {
 	__shared__ WarpStage stage[8];   /* one per warp of a <=256-thread block */
 	const int lane = threadIdx.x & 31;
-	const size_t warp = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-	const size_t nwarps = ((size_t)gridDim.x * blockDim.x) >> 5;
-	for (size_t p = warp; p < L.n; p += nwarps) {
+	PoseFeed feed(L.next);
+	for (size_t p = feed.take(lane); p < L.n; p = feed.take(lane)) {
 		const RigidModel& M = L.models[__ldg(&L.pair_of[p])];
 		const float* dofp = reinterpret_cast<const float*>(L.dofs + p);
 		const float dv = lane < 6 ? __ldg(dofp + lane) : 0.f;

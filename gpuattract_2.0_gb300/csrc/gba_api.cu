@@ -697,6 +697,9 @@ ModesLaunch Context::modes_launch(gba_id rec, gba_id lig, gba_id grid_rec, gba_i
 }
 
 void Context::run_modes(ModesLaunch& L, cudaStream_t s) {
+	StreamScratch scratch(scratch_pool);
+	L.next = (unsigned long long*)scratch.get(sizeof(unsigned long long), s);
+	check_cuda(cudaMemsetAsync(L.next, 0, sizeof(unsigned long long), s), "modes energy: pose counter");
 	const int threads = 256;
 	int bps = modes_blocks_per_sm(threads, L);
 	size_t want = (L.n + threads / 32 - 1) / (threads / 32);
@@ -707,6 +710,8 @@ void Context::run_modes(ModesLaunch& L, cudaStream_t s) {
 void Context::run_rigid(RigidLaunch& L, cudaStream_t s) {
 	StreamScratch scratch(scratch_pool);
 	L.order = pose_order(L.dofs, 6, L.n, L.m.grid.outer, s, scratch);
+	L.next = (unsigned long long*)scratch.get(sizeof(unsigned long long), s);
+	check_cuda(cudaMemsetAsync(L.next, 0, sizeof(unsigned long long), s), "rigid energy: pose counter");
 	const TuneParams tp = tuned("energy", L.n);
 	const int threads = tp.threads;
 	const int warps_per_block = threads / 32;

@@ -112,6 +112,7 @@ struct RigidLaunch {
 	const uint32_t* order;    /* visiting order (nullptr: submission order) */
 	size_t n;
 	int bound4;               /* launch the four-blocks-per-SM instantiation */
+	unsigned long long* next; /* pose counter, zero at launch (PoseFeed); nullptr: fixed stride */
 };
 
 cudaError_t launch_rigid_energy(const RigidLaunch& L, int blocks, int threads, cudaStream_t s);
@@ -150,6 +151,7 @@ struct BatchEnergyLaunch {
 	const gba_dof6d* dofs;
 	gba_result6d* out;
 	size_t n;
+	unsigned long long* next; /* pose counter, zero at launch (PoseFeed); nullptr: fixed stride */
 };
 
 cudaError_t launch_batch_energy(const BatchEnergyLaunch& L, int blocks, int threads, cudaStream_t s);
@@ -168,6 +170,7 @@ struct ModesLaunch {
 	const gba_dof6d_modes* dofs;
 	gba_result6d_modes* out;
 	size_t n;
+	unsigned long long* next; /* pose counter, zero at launch (PoseFeed); nullptr: fixed stride */
 };
 
 cudaError_t launch_modes_energy(const ModesLaunch& L, int blocks, int threads, cudaStream_t s);

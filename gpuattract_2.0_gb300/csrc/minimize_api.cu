@@ -294,6 +294,9 @@ int gba_batch_energy_6d(gba_ctx* ctx, const gba_pair_job* jobs, size_t njobs, vo
 	L.out = (gba_result6d*)ctx->staging(2, n * sizeof(gba_result6d));
 	for (size_t j = 0; j < njobs; ++j)
 		if (jobs[j].n) copy_in((void*)(L.dofs + G.offset[j]), jobs[j].start, jobs[j].n * sizeof(gba_dof6d), s);
+	StreamScratch scratch(ctx->scratch_pool);
+	L.next = (unsigned long long*)scratch.get(sizeof(unsigned long long), s);
+	check_cuda(cudaMemsetAsync(L.next, 0, sizeof(unsigned long long), s), "batch energy: pose counter");
 	const int threads = 256;
 	size_t blocks = std::max<size_t>(1, std::min<size_t>((n + 7) / 8, (size_t)ctx->num_sms * 3));
 	check_cuda(launch_batch_energy(L, (int)blocks, threads, s), "batch energy launch");

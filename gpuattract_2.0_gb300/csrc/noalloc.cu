@@ -1,19 +1,21 @@
 /*
  * noalloc.cu -- gba_energy_6d_noalloc: the fused rigid energy launch of
  * gba_energy_6d for device-resident poses, with the visiting-order scratch
- * (translation-cell counts, each pose's cell and rank, the order) taken from a
- * fixed, statically allocated device array instead of the stream-ordered
- * allocator.  The call performs no device or host memory allocation: no
- * cudaMalloc / cudaMallocAsync / cudaFree, no allocating library routine; the
- * cell counts are cleared with cudaMemsetAsync on every call.
+ * (the pose counter, translation-cell counts, each pose's cell and rank, the
+ * order) taken from a fixed, statically allocated device array instead of the
+ * stream-ordered allocator.  The call performs no device or host memory
+ * allocation: no cudaMalloc / cudaMallocAsync / cudaFree, no allocating
+ * library routine; the pose counter and the cell counts are cleared with
+ * cudaMemsetAsync on every call.
  *
  * Scratch: one file-scope __device__ array of kNoAllocScratchBytes per device
  * (2 MiB), addressed through cudaGetSymbolAddress on the first call made on
  * each device (with that device current); that first call may load the
  * module, so make it before any stream capture.  Batches of more than
- * kNoAllocMaxPoses poses are rejected with GBA_ERR_INVALID_ARGUMENT.  Nothing
- * in the scratch has to start at zero: the order kernel writes every key and
- * index it sorts, the sort writes its own temporary state.  The array is
+ * kNoAllocMaxPoses poses are rejected with GBA_ERR_INVALID_ARGUMENT.  The
+ * first 256 bytes hold the pose counter; nothing else in the scratch has to
+ * start at zero: the order kernel writes every key and index it sorts, the
+ * sort writes its own temporary state.  The array is
  * shared by every call on a device: overlapping calls (other streams, threads
  * or contexts on the same device) race on it and must be serialized by the
  * caller.
@@ -28,6 +30,7 @@ namespace gba {
 
 constexpr size_t kNoAllocScratchBytes = (size_t)2 << 20;
 constexpr size_t kNoAllocMaxPoses = 65536;
+constexpr size_t kCounterBytes = 256;   /* the pose counter, keeping the order scratch 256-byte aligned */
 
 __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
@@ -75,8 +78,11 @@ extern "C" int gba_energy_6d_noalloc(gba_ctx* ctx, gba_id rec, gba_id lig, gba_i
 		L.dofs = dofs;
 		L.out = out;
 		L.census = nullptr;
+		L.next = (unsigned long long*)scratch;
+		check_cuda(cudaMemsetAsync(L.next, 0, sizeof(unsigned long long), s), "gba_energy_6d_noalloc: pose counter");
 		L.order = (ctx->order_enabled && n >= Context::kOrderMinPoses)
-				? pose_order_in(dofs, 6, n, L.m.grid.outer, scratch, kNoAllocScratchBytes, s)
+				? pose_order_in(dofs, 6, n, L.m.grid.outer, (char*)scratch + kCounterBytes,
+						kNoAllocScratchBytes - kCounterBytes, s)
 				: nullptr;
 		/* launch shape as gba_energy_6d chooses it */
 		const TuneParams tp = ctx->tuned("energy", n);

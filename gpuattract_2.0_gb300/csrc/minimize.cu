@@ -44,9 +44,14 @@ __device__ __forceinline__ bool warp_over_budget(unsigned long long t_start, uns
 }
 
 /* compiled for four resident 256-thread blocks per SM (64 registers, like
- * the scoring kernel's four-block instantiation) */
+ * the scoring kernel's four-block instantiation); the staging areas, one per
+ * warp, are dynamic shared memory sized to the block, so that smaller blocks
+ * are not held back by shared memory they do not use (128 threads: eight
+ * blocks per SM instead of four) */
+extern __shared__ __align__(16) unsigned char min_stage_smem[];
+
 __global__ void __launch_bounds__(256, 4) minimize_rigid_kernel(const MinLaunch L) {
-	__shared__ WarpStage stage[8];   /* one per warp of a <=256-thread block */
+	WarpStage* stage = reinterpret_cast<WarpStage*>(min_stage_smem);
 	const int lane = threadIdx.x & 31;
 	unsigned long long t_start = 0;
 	if (lane == 0) t_start = global_ns();
@@ -116,14 +121,16 @@ __global__ void __launch_bounds__(256, 4) minimize_rigid_kernel(const MinLaunch 
 	}
 }
 
+static size_t min_stage_bytes(int threads) { return (size_t)((threads + 31) / 32) * sizeof(WarpStage); }
+
 cudaError_t launch_minimize_rigid(const MinLaunch& L, int blocks, int threads, cudaStream_t s) {
-	minimize_rigid_kernel<<<blocks, threads, 0, s>>>(L);
+	minimize_rigid_kernel<<<blocks, threads, min_stage_bytes(threads), s>>>(L);
 	return cudaGetLastError();
 }
 
 int minimize_blocks_per_sm(int threads) {
 	int nb = 0;
-	cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, minimize_rigid_kernel, threads, 0);
+	cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, minimize_rigid_kernel, threads, min_stage_bytes(threads));
 	return nb > 0 ? nb : 1;
 }
 

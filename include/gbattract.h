@@ -208,11 +208,12 @@ int gba_energy_6d(gba_ctx* ctx, gba_id rec, gba_id lig, gba_id grid, gba_id para
 		const gba_dof6d* dofs, size_t n, gba_result6d* out, void* stream);
 
 /* gba_energy_6d for device pointers that allocates nothing (no counterpart in
- * the reference): the visiting-order scratch lives in a static 2 MiB device
- * array per device, resolved with cudaGetSymbolAddress on the first call on
- * each device -- make that first call before any stream capture.  At most
- * 65536 poses per call (more: GBA_ERR_INVALID_ARGUMENT).  Nothing must be
- * zeroed beforehand.  Calls that overlap on one device (any stream, thread or
+ * the reference): the pose counter and the visiting-order scratch live in a
+ * static 2 MiB device array per device, resolved with cudaGetSymbolAddress on
+ * the first call on each device -- make that first call before any stream
+ * capture.  At most 65536 poses per call (more: GBA_ERR_INVALID_ARGUMENT).
+ * Nothing must be zeroed beforehand (the call clears what it needs with
+ * cudaMemsetAsync).  Calls that overlap on one device (any stream, thread or
  * context) share the array and race: serialize them.  Asynchronous on
  * `stream`; results equal gba_energy_6d's bit for bit. */
 int gba_energy_6d_noalloc(gba_ctx* ctx, gba_id rec, gba_id lig, gba_id grid, gba_id params,

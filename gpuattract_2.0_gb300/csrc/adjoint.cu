@@ -24,6 +24,8 @@
  * Parameter gradients accumulate in FP64 shared-memory partials per block and
  * are flushed with FP64 global atomics.
  */
+#include <cub/cub.cuh>
+
 #include "gba_context.h"
 #include "rigid_pose.cuh"
 
@@ -52,6 +54,7 @@ struct PairwiseLaunch {
 	double* g_eps;         /* T*T */
 	const float4* tab;     /* 3*T*T: per type pair the constants of lj86 (lj_table_kernel) */
 	unsigned long long* next;   /* pose counter, zero at launch (PoseFeed) */
+	const uint32_t* order;      /* visiting order (nearest ligands first), or nullptr */
 };
 
 namespace {
@@ -77,6 +80,41 @@ __global__ void lj_table_kernel(uint32_t T2, const float* __restrict__ r0v, cons
 	tab[3 * k + 1] = make_float4(ok ? -3.f * emin / rc : 0.f, ok ? 4.f * emin / ac : 0.f, 8.f * (r0_6 * r0),
 			6.f * (r0_2 * r0_2 * r0));
 	tab[3 * k + 2] = make_float4(r0_8, r0_6, eps, (float)ipon[k]);
+}
+
+/* Sort keys of the visiting order: the bits of |t|^2 for the pose's
+ * translation t (non-negative floats order like their bit patterns; NaN
+ * sorts last).  Ligands near the receptor's centre meet the most neighbour
+ * pairs, so taking them first leaves cheap poses for the end of the launch. */
+__global__ void near_first_keys_kernel(const gba_dof6d* __restrict__ dofs, uint32_t n, uint32_t* __restrict__ keys,
+		uint32_t* __restrict__ idx) {
+	const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+	if (p >= n) return;
+	const float* d = reinterpret_cast<const float*>(dofs + p);
+	const float x = __ldg(d), y = __ldg(d + 1), z = __ldg(d + 2);
+	keys[p] = __float_as_uint(x * x + y * y + z * z);
+	idx[p] = p;
+}
+
+/* Poses ordered nearest first (sorted on the top 16 bits of the key: the
+ * exponent and 7 mantissa bits of |t|^2, about 0.4 % bins), scratch from S. */
+const uint32_t* near_first_order(const gba_dof6d* dofs, size_t n, StreamScratch& S, cudaStream_t s) {
+	cub::DoubleBuffer<uint32_t> kb(nullptr, nullptr), ib(nullptr, nullptr);
+	size_t tmp = 0;
+	check_cuda(cub::DeviceRadixSort::SortPairs(nullptr, tmp, kb, ib, (int)n, 16, 32, s), "pairwise order: size");
+	const size_t a = (n * sizeof(uint32_t) + 255) & ~(size_t)255;
+	char* base = (char*)S.get(4 * a + tmp, s);
+	uint32_t* k0 = (uint32_t*)base;
+	uint32_t* k1 = (uint32_t*)(base + a);
+	uint32_t* i0 = (uint32_t*)(base + 2 * a);
+	uint32_t* i1 = (uint32_t*)(base + 3 * a);
+	near_first_keys_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(dofs, (uint32_t)n, k0, i0);
+	check_cuda(cudaGetLastError(), "pairwise order: keys");
+	kb = cub::DoubleBuffer<uint32_t>(k0, k1);
+	ib = cub::DoubleBuffer<uint32_t>(i0, i1);
+	check_cuda(cub::DeviceRadixSort::SortPairs(base + 4 * a, tmp, kb, ib, (int)n, 16, 32, s),
+			"pairwise order: sort");
+	return ib.Current();
 }
 
 /* LJ energy, radial force factor and d/d(r0, eps) of one 8-6 pair from the
@@ -120,6 +158,7 @@ struct PairStage {
 	uint8_t own[64];                 /* PairWindow: slot of the bead starting at window position b */
 };
 constexpr int kPairwiseThreads = 256;
+constexpr size_t kNearFirstMinPoses = 2048;
 
 /* One warp per pose, the ligand in rounds of 64 beads like the rigid kernel:
  * lane-per-bead staging (transform, neighbour-list voxel), then the round's
@@ -144,7 +183,8 @@ __global__ void __launch_bounds__(kPairwiseThreads) pairwise_kernel(const Pairwi
 	PairStage& W = stage[threadIdx.x >> 5];
 	const bool cdiel = L.dielec == GBA_DIELEC_CONSTANT;
 	PoseFeed feed(L.next);
-	for (size_t p = feed.take(lane); p < L.n; p = feed.take(lane)) {
+	for (size_t k = feed.take(lane); k < L.n; k = feed.take(lane)) {
+		const size_t p = L.order ? (size_t)__ldg(&L.order[k]) : k;
 		const float* dofp = reinterpret_cast<const float*>(L.dofs + p);
 		const float dv = lane < 6 ? __ldg(dofp + lane) : 0.f;
 		float c[6];
@@ -339,6 +379,8 @@ extern "C" int gba_pairwise_6d(gba_ctx* ctx, gba_id rec, gba_id lig, gba_id grid
 		float4* tab = (float4*)scratch.get(3 * (size_t)std::max<uint32_t>(T2, 1) * sizeof(float4), s);
 		L.next = (unsigned long long*)scratch.get(sizeof(unsigned long long), s);
 		check_cuda(cudaMemsetAsync(L.next, 0, sizeof(unsigned long long), s), "pairwise: pose counter");
+		/* a few poses per warp: the launch's end is set by its slowest poses */
+		L.order = (n >= kNearFirstMinPoses && n <= 0xffffffffu) ? near_first_order(dofs, n, scratch, s) : nullptr;
 		if (T2 > 0) {
 			lj_table_kernel<<<(T2 + 255) / 256, 256, 0, s>>>(T2, L.r0, L.eps, L.ipon, tab);
 			check_cuda(cudaGetLastError(), "pairwise: parameter table");

@@ -156,6 +156,22 @@ def test_pose_order_does_not_change_results(small_case, ctx):
     assert np.array_equal(plain, ordered)
 
 
+@pytest.mark.parametrize("n", [1, 31, 4863, 4865, 9731])
+def test_pose_counter_visits_every_pose_once(small_case, ctx, n):
+    """Warps claim poses from a per-launch counter: every pose of a batch is
+    evaluated exactly once and lands in its own slot, whatever the batch size
+    relative to the resident warps, and equals the same pose scored in small
+    batches (other launch shapes, fewer poses than warps)."""
+    wl, grid = small_case
+    ids = upload(ctx, wl.rec, wl.lig, grid, wl.params)
+    rng = np.random.default_rng(n)
+    dofs = wl.dofs[rng.integers(0, len(wl.dofs), n)]
+    dofs[:, :3] += rng.normal(0, 3.0, (n, 3)).astype(np.float32)
+    whole = ctx.energy_6d(*ids, dofs)
+    pieces = np.concatenate([ctx.energy_6d(*ids, dofs[k:k + 97]) for k in range(0, n, 97)])
+    assert np.array_equal(whole, pieces)
+
+
 def test_octet_layout_does_not_change_results(small_case, ctx):
     """The duplicated-octet layout reads the same corners: with one lane per
     lookup the results are bit-identical to the native layout.  (The 8-lane

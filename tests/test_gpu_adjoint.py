@@ -133,3 +133,34 @@ def test_grid_energy_backward_is_minus_result(small_case, pkg):
         assert np.array_equal(E.detach().cpu().numpy(), res[:, 0])
         want = -res[:, 1:7] * w.cpu().numpy()[:, None]
         assert np.allclose(d.grad.cpu().numpy(), want, rtol=1e-6, atol=0)
+
+
+def test_nearest_first_order_keeps_every_result(adj_case):
+    """From 2,048 poses on, the pairwise kernels visit poses nearest the
+    receptor centre first; each pose's energy and DOF gradient is its own
+    (bit for bit the same as in batches below the threshold, which keep
+    submission order), and the summed parameter gradients agree up to FP64
+    summation order."""
+    import torch
+    from gbattract.autograd import PairwiseEnergy
+    c = adj_case
+    rng = np.random.default_rng(47)
+    base = c["wl"].dofs
+    dofs = base[rng.integers(0, len(base), 2600)].copy()
+    dofs[:, :3] += rng.normal(0, 2.0, (len(dofs), 3)).astype(np.float32)
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda().requires_grad_(True)
+
+    def run(d_np):
+        d, ql, qr, r0, eps = (t(d_np), t(c["q_lig"]), t(c["q_rec"]), t(c["r0"]), t(c["eps"]))
+        E = PairwiseEnergy.apply(d, ql, qr, r0, eps, c["sysm"])
+        E.sum().backward()
+        return [x.detach().cpu().numpy().astype(np.float64) for x in (E, d.grad, ql.grad, qr.grad, r0.grad, eps.grad)]
+
+    whole = run(dofs)
+    parts = [run(dofs[k:k + 650]) for k in range(0, len(dofs), 650)]
+    assert np.array_equal(whole[0], np.concatenate([p[0] for p in parts]))
+    assert np.array_equal(whole[1], np.concatenate([p[1] for p in parts]))
+    for i in range(2, 6):
+        summed = np.sum([p[i] for p in parts], axis=0)
+        scale = np.max(np.abs(summed)) + 1e-30
+        assert np.max(np.abs(whole[i] - summed)) <= 1e-5 * scale

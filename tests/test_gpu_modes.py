@@ -130,3 +130,22 @@ def test_zero_amplitudes_match_rigid(small_case, pkg, oracle, ctx):
     for e in pose_errors(got[:, :7], rigid, st):
         assert float(e.max()) <= 1e-5
     assert np.all(got[:, 7:] == 0)
+
+
+def test_modes_pose_counter_visits_every_pose_once(pkg, oracle, ctx):
+    """Warps of the modes kernel claim poses from a per-launch counter: a
+    batch larger than the resident warps gives every pose its own result,
+    bit for bit the same as the pose scored in small batches (NaN where the
+    deformation overflows, in the same places)."""
+    wl = pkg.synth.make_pair(2, 130, 70, 96, (16.0, 24.0), n_modes=5, seed=515)
+    rng = np.random.default_rng(5)
+    n = 5003
+    dofs = wl.dofs[rng.integers(0, len(wl.dofs), n)].copy()
+    dofs[:, :3] += rng.normal(0, 2.0, (n, 3)).astype(np.float32)
+    gr = oracle.build_grid(wl.rec, wl.params, pkg.GridOptions())
+    gl = oracle.build_grid(wl.lig, wl.params, pkg.GridOptions())
+    ids = (ctx.upload_protein(wl.rec), ctx.upload_protein(wl.lig), ctx.upload_grid(gr),
+           ctx.upload_grid(gl), ctx.upload_params(wl.params))
+    whole = ctx.energy_6d_modes(*ids, dofs)
+    pieces = np.concatenate([ctx.energy_6d_modes(*ids, dofs[k:k + 333]) for k in range(0, n, 333)])
+    assert np.array_equal(whole, pieces, equal_nan=True)

@@ -183,8 +183,8 @@ __global__ void __launch_bounds__(kPairwiseThreads) pairwise_kernel(const Pairwi
 	PairStage& W = stage[threadIdx.x >> 5];
 	const bool cdiel = L.dielec == GBA_DIELEC_CONSTANT;
 	PoseFeed feed(L.next);
-	for (size_t k = feed.take(lane); k < L.n; k = feed.take(lane)) {
-		const size_t p = L.order ? (size_t)__ldg(&L.order[k]) : k;
+	for (size_t slot = feed.take(lane); slot < L.n; slot = feed.take(lane)) {
+		const size_t p = L.order ? (size_t)__ldg(&L.order[slot]) : slot;
 		const float* dofp = reinterpret_cast<const float*>(L.dofs + p);
 		const float dv = lane < 6 ? __ldg(dofp + lane) : 0.f;
 		float c[6];
@@ -380,7 +380,8 @@ extern "C" int gba_pairwise_6d(gba_ctx* ctx, gba_id rec, gba_id lig, gba_id grid
 		L.next = (unsigned long long*)scratch.get(sizeof(unsigned long long), s);
 		check_cuda(cudaMemsetAsync(L.next, 0, sizeof(unsigned long long), s), "pairwise: pose counter");
 		/* a few poses per warp: the launch's end is set by its slowest poses */
-		L.order = (n >= kNearFirstMinPoses && n <= 0xffffffffu) ? near_first_order(dofs, n, scratch, s) : nullptr;
+		/* the sort takes an int item count: larger batches keep submission order */
+		L.order = (n >= kNearFirstMinPoses && n <= 0x7fffffffu) ? near_first_order(dofs, n, scratch, s) : nullptr;
 		if (T2 > 0) {
 			lj_table_kernel<<<(T2 + 255) / 256, 256, 0, s>>>(T2, L.r0, L.eps, L.ipon, tab);
 			check_cuda(cudaGetLastError(), "pairwise: parameter table");

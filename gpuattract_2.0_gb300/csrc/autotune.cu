@@ -149,7 +149,7 @@ extern "C" int gba_autotune(gba_ctx* ctx, gba_id rec, gba_id lig, gba_id grid, g
 				const int evals = std::min(std::max(max_evals, 1), 50);
 				for (int threads : {64, 128, 256}) {
 					for (int chunk : {1, 2, 4}) {
-						ctx->tune["minimize"] = TuneParams{threads, 64, chunk};
+						ctx->set_tuned("minimize", TuneParams{threads, 64, chunk});
 						MinLaunch L{};
 						L.models = (const RigidModel*)mb.ptr;
 						L.start = d;
@@ -168,8 +168,8 @@ extern "C" int gba_autotune(gba_ctx* ctx, gba_id rec, gba_id lig, gba_id grid, g
 				cache_store(cache_path, mk, tm);
 			}
 		}
-		ctx->tune["energy"] = te;
-		ctx->tune["minimize"] = tm;
+		ctx->set_tuned("energy", te);
+		ctx->set_tuned("minimize", tm);
 		if (out) {
 			out->energy_threads = te.threads;
 			out->energy_blocks_per_sm = te.blocks_per_sm;

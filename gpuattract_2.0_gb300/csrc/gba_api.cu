@@ -7,6 +7,7 @@
  * entry point throws or exits: failures come back as a status code with the
  * message in gba_last_error().
  */
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <memory>
@@ -23,6 +24,7 @@ using namespace gba;
 
 namespace {
 thread_local std::string t_create_error;
+std::atomic<uint64_t> g_allocations{0};
 }
 
 /* ------------------------------------------------------------------------ */
@@ -31,9 +33,12 @@ thread_local std::string t_create_error;
 
 namespace gba {
 
+void note_allocation() { g_allocations.fetch_add(1, std::memory_order_relaxed); }
+
 void DevBuffer::alloc(size_t b) {
 	release();
 	if (b == 0) return;
+	note_allocation();
 	cudaError_t e = cudaMalloc(&ptr, b);
 	if (e != cudaSuccess) {
 		ptr = nullptr;
@@ -80,6 +85,23 @@ Item* Context::find(gba_id id, ItemKind kind) {
 
 gba_id Context::add(std::unique_ptr<Item> item) {
 	Lock g(mu);
+	if (item->kind == ItemKind::Grid) {
+		const float p2 = static_cast<GridItem*>(item.get())->dev.nl.dPlateau2;
+		uint32_t key;
+		std::memcpy(&key, &p2, 4);
+		if (!plateau_keys.count(key)) {
+			for (auto& kv : items)
+				if (kv.second->kind == ItemKind::Params)
+					static_cast<ParamsItem*>(kv.second.get())->pair_table(p2);
+			plateau_keys.insert(key);
+		}
+	} else if (item->kind == ItemKind::Params) {
+		for (uint32_t key : plateau_keys) {
+			float p2;
+			std::memcpy(&p2, &key, 4);
+			static_cast<ParamsItem*>(item.get())->pair_table(p2);
+		}
+	}
 	gba_id id = next_id++;
 	items.emplace(id, std::move(item));
 	return id;
@@ -96,13 +118,20 @@ void* Context::pinned(int slot, size_t bytes) {
 		if (pinned_buf[slot]) cudaFreeHost(pinned_buf[slot]);
 		pinned_buf[slot] = nullptr;
 		pinned_bytes[slot] = 0;
+		note_allocation();
 		check_cuda(cudaMallocHost(&pinned_buf[slot], bytes + bytes / 4), "cudaMallocHost");
 		pinned_bytes[slot] = bytes + bytes / 4;
 	}
 	return pinned_buf[slot];
 }
 
+void Context::set_tuned(const std::string& key, const TuneParams& p) {
+	std::lock_guard<std::mutex> g(tune_mu);
+	tune[key] = p;
+}
+
 TuneParams Context::tuned(const std::string& kind, size_t) const {
+	std::lock_guard<std::mutex> g(tune_mu);
 	auto it = tune.find(kind);
 	if (it != tune.end()) return it->second;
 	/* defaults until gba_autotune has run: full occupancy */
@@ -194,6 +223,12 @@ std::vector<float> nl_ratio_table(float dPlateau2) {
 extern "C" {
 
 const char* gba_version(void) { return "gbattract 0.1 (sm_103a)"; }
+
+int gba_allocation_count(uint64_t* out) {
+	if (!out) return GBA_ERR_INVALID_ARGUMENT;
+	*out = g_allocations.load(std::memory_order_relaxed);
+	return GBA_OK;
+}
 
 int gba_create(int device, gba_ctx** out) {
 	if (!out) {
@@ -399,11 +434,13 @@ int gba_upload_params(gba_ctx* ctx, uint32_t num_types, const gba_ffparam* table
  * changes no bit of the result.  Stored transposed against the host table
  * (which is indexed receptor type major): the pairs of one ligand bead then
  * read one contiguous row. */
-const float4* ParamsItem::pair_table(float dPlateau2) {
+const float4* ParamsItem::pair_table(float dPlateau2, bool may_allocate) {
 	uint32_t key;
 	std::memcpy(&key, &dPlateau2, 4);
 	auto it = pair_tables.find(key);
 	if (it != pair_tables.end()) return (const float4*)it->second->ptr;
+	if (!may_allocate)
+		throw ApiError(GBA_ERR_INVALID_ARGUMENT, "no pair-term table for this grid's plateau and parameter table");
 	const size_t T2 = host_table.size();
 	std::vector<float4> t(2 * T2);
 	const float p2inv = 1.0f / dPlateau2;
@@ -607,7 +644,7 @@ RigidLaunch Context::rigid_launch(gba_id rec, gba_id lig, gba_id grid, gba_id pa
 	L.m.lig = Lg->dev;
 	L.m.grid = apply_kernel_options(G->dev);
 	L.m.par = P->dev;
-	L.m.par.pair = P->pair_table(G->dev.nl.dPlateau2);
+	L.m.par.pair = P->pair_table(G->dev.nl.dPlateau2, may_allocate);
 	L.bound4 = (kernel_opts & GBA_KOPT_FOUR_BLOCKS) ? 1 : 0;
 	if (kernel_opts & GBA_KOPT_TYPED_LIST)
 		L.m.grid.nl.typed_list = typed_list(*G, rec, *R, may_allocate);

@@ -6,6 +6,7 @@
 
 #include <map>
 #include <memory>
+#include <set>
 #include <atomic>
 #include <mutex>
 #include <thread>
@@ -48,6 +49,10 @@ using Lock = std::lock_guard<CheckedMutex>;
 
 void check_cuda(cudaError_t e, const char* what);
 bool is_device_pointer(const void* p);
+
+/* Counts every device or pinned-host allocation the library makes
+ * (gba_allocation_count). */
+void note_allocation();
 
 /* One cudaMalloc'd buffer, freed on destruction. */
 struct DevBuffer {
@@ -119,7 +124,9 @@ struct ParamsItem : Item {
 	/* per plateau^2 (bit pattern): the pair-term table with the plateau
 	 * terms folded in (plateau_table) */
 	std::map<uint32_t, std::unique_ptr<DevBuffer>> pair_tables;
-	const float4* pair_table(float dPlateau2);
+	/* the table for plateau^2 dPlateau2; built on first use when
+	 * may_allocate, else an ApiError if it does not exist yet */
+	const float4* pair_table(float dPlateau2, bool may_allocate = true);
 };
 
 /* Visiting order of n poses (grouped by translation cell) computed in the
@@ -171,7 +178,11 @@ struct Context {
 	const char* last_error() const { std::lock_guard<std::mutex> g(err_mu); return err.c_str(); }
 
 	Item* find(gba_id id, ItemKind kind);
+	/* registers an item; a grid or parameter table also gets the pair-term
+	 * tables it forms with the items already present (one per parameter
+	 * table and distinct plateau), so that no scoring call has to build one */
 	gba_id add(std::unique_ptr<Item> item);
+	std::set<uint32_t> plateau_keys;   /* plateau^2 bit patterns of every grid added */
 	void* staging(int slot, size_t bytes);
 	void* pinned(int slot, size_t bytes);
 
@@ -184,7 +195,13 @@ struct Context {
 	std::map<GraphKey, cudaGraphExec_t> graphs;
 	cudaStream_t capture_stream = nullptr;
 	uint32_t deadline_ms = 0;
+	mutable std::mutex tune_mu;    /* guards tune (gba_autotune writes it while calls read it) */
 	std::map<std::string, TuneParams> tune;
+	void set_tuned(const std::string& key, const TuneParams& p);
+
+	/* device address of the static scratch of gba_energy_6d_noalloc,
+	 * resolved by the first such call on this context */
+	void* noalloc_scratch = nullptr;
 
 	/* spatial visiting order of large batches (pose_order.cu) */
 	static constexpr size_t kOrderMinPoses = 4096;

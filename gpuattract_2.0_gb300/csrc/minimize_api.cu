@@ -54,6 +54,7 @@ void Context::run_minimize(MinLaunch& L, cudaStream_t s, int32_t* status_out) {
 	L.chunk = tp.chunk;
 	if (!aux.ptr) {
 		aux.alloc(64);
+		note_allocation();
 		check_cuda(cudaMallocHost((void**)&pinned_status, sizeof(int32_t)), "cudaMallocHost");
 	}
 	/* aux: [0,8) cursor, [8,12) status, [16,24) modes cursor, [32,40) earliest warp start */
@@ -414,6 +415,7 @@ int gba_minimize_6d_modes(gba_ctx* ctx, gba_id rec, gba_id lig, gba_id grid_rec,
 	}
 	if (!ctx->aux.ptr) {
 		ctx->aux.alloc(64);
+		note_allocation();
 		check_cuda(cudaMallocHost((void**)&ctx->pinned_status, sizeof(int32_t)), "cudaMallocHost");
 	}
 	/* aux [12,16): modes status, [16,24): modes cursor */

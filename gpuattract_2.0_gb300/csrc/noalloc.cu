@@ -6,22 +6,27 @@
  * stream-ordered allocator.  The call performs no device or host memory
  * allocation: no cudaMalloc / cudaMallocAsync / cudaFree, no allocating
  * library routine; the pose counter and the cell counts are cleared with
- * cudaMemsetAsync on every call.
+ * cudaMemsetAsync on every call.  Everything else it reads was made when the
+ * data was uploaded: the pair-term table of a (parameter table, plateau)
+ * combination is built when the second of the two is added to the context.
+ * The receptor-typed copy of a neighbour list is the one exception: it is
+ * built by the first allocating scoring call of a (grid, receptor)
+ * combination; until then this call walks the plain list and gathers each
+ * neighbour's type (the same results bit for bit, a little slower).
  *
  * Scratch: one file-scope __device__ array of kNoAllocScratchBytes per device
- * (2 MiB), addressed through cudaGetSymbolAddress on the first call made on
- * each device (with that device current); that first call may load the
- * module, so make it before any stream capture.  Batches of more than
- * kNoAllocMaxPoses poses are rejected with GBA_ERR_INVALID_ARGUMENT.  The
- * first 256 bytes hold the pose counter; nothing else in the scratch has to
- * start at zero: the order kernel writes every key and index it sorts, the
- * sort writes its own temporary state.  The array is
- * shared by every call on a device: overlapping calls (other streams, threads
- * or contexts on the same device) race on it and must be serialized by the
- * caller.
+ * (2 MiB), addressed through cudaGetSymbolAddress by the first call made on
+ * each context (with the context's device current) and kept with the
+ * context; that first call may load the module, so make it before any stream
+ * capture.  Batches of more than kNoAllocMaxPoses poses are rejected with
+ * GBA_ERR_INVALID_ARGUMENT.  The first 256 bytes hold the pose counter,
+ * cleared by every call like the cell counts after it; nothing else in the
+ * scratch has to start at zero: the order kernels write every key and index
+ * they read back.  The array is shared by every
+ * call on a device: overlapping calls (other streams, threads or contexts on
+ * the same device) race on it and must be serialized by the caller.
  */
 #include <algorithm>
-#include <mutex>
 #include <string>
 
 #include "gba_context.h"
@@ -34,26 +39,16 @@ constexpr size_t kCounterBytes = 256;   /* the pose counter, keeping the order s
 
 __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
-namespace {
-
-constexpr int kMaxDevices = 64;
-std::mutex g_scratch_mu;
-void* g_scratch_ptr[kMaxDevices] = {};
-
-/* Device address of this device's scratch array (resolved once per device). */
-void* noalloc_scratch(int device) {
-	if (device < 0 || device >= kMaxDevices)
-		throw ApiError(GBA_ERR_INVALID_ARGUMENT, "gba_energy_6d_noalloc: device ordinal out of range");
-	std::lock_guard<std::mutex> g(g_scratch_mu);
-	if (!g_scratch_ptr[device]) {
+/* Device address of the scratch array, resolved once per context (with the
+ * context's device current, before the first launch that uses it). */
+void* noalloc_scratch(Context& ctx) {
+	if (!ctx.noalloc_scratch) {
 		void* p = nullptr;
 		check_cuda(cudaGetSymbolAddress(&p, g_noalloc_scratch), "gba_energy_6d_noalloc: cudaGetSymbolAddress");
-		g_scratch_ptr[device] = p;
+		ctx.noalloc_scratch = p;
 	}
-	return g_scratch_ptr[device];
+	return ctx.noalloc_scratch;
 }
-
-}  // namespace
 
 }  // namespace gba
 
@@ -71,7 +66,7 @@ extern "C" int gba_energy_6d_noalloc(gba_ctx* ctx, gba_id rec, gba_id lig, gba_i
 		ctx->bind();
 		if (!is_device_pointer(dofs) || !is_device_pointer(out))
 			throw ApiError(GBA_ERR_INVALID_ARGUMENT, "gba_energy_6d_noalloc: device pointers required");
-		void* scratch = noalloc_scratch(ctx->device);
+		void* scratch = noalloc_scratch(*ctx);
 		RigidLaunch L = ctx->rigid_launch(rec, lig, grid, params, false);
 		cudaStream_t s = (cudaStream_t)stream;
 		L.n = n;

@@ -234,6 +234,7 @@ const uint32_t* pose_order_in(const void* dofs, size_t stride_floats, size_t n, 
 
 void* StreamScratch::get(size_t bytes, cudaStream_t s) {
 	void* p = nullptr;
+	note_allocation();
 	if (pool)
 		check_cuda(cudaMallocFromPoolAsync(&p, bytes ? bytes : 16, pool, s), "cudaMallocFromPoolAsync");
 	else

@@ -102,6 +102,12 @@ typedef struct { uint32_t numEl; uint32_t idx; } gba_neighbour_desc;
 /* Version string of the library. */
 const char* gba_version(void);
 
+/* Number of device and pinned-host allocations (cudaMalloc, cudaMallocHost,
+ * stream-ordered pool allocations) the library has made in this process.
+ * No reference counterpart (instrumentation: lets a caller check that a
+ * call allocated nothing). */
+int gba_allocation_count(uint64_t* out);
+
 /* Opens a context on CUDA device `device`.  Stands in for the per-device state
  * the reference keeps in DeviceManager/DataManager (src/server/DeviceManager.cpp:29-59)
  * plus the per-worker GPUEnergyService6D buffers (src/service/GPUEnergyService6D.tpp:100-160). */
@@ -208,14 +214,22 @@ int gba_energy_6d(gba_ctx* ctx, gba_id rec, gba_id lig, gba_id grid, gba_id para
 		const gba_dof6d* dofs, size_t n, gba_result6d* out, void* stream);
 
 /* gba_energy_6d for device pointers that allocates nothing (no counterpart in
- * the reference): the pose counter and the visiting-order scratch live in a
- * static 2 MiB device array per device, resolved with cudaGetSymbolAddress on
- * the first call on each device -- make that first call before any stream
- * capture.  At most 65536 poses per call (more: GBA_ERR_INVALID_ARGUMENT).
- * Nothing must be zeroed beforehand (the call clears what it needs with
- * cudaMemsetAsync).  Calls that overlap on one device (any stream, thread or
- * context) share the array and race: serialize them.  Asynchronous on
- * `stream`; results equal gba_energy_6d's bit for bit. */
+ * the reference), for callers that must not allocate while they score: a
+ * service running under a fixed device-memory budget, or a host that has
+ * reserved all device memory up front.  The pose counter and the
+ * visiting-order scratch live in a static 2 MiB device array per device,
+ * whose address the first call on each context resolves with
+ * cudaGetSymbolAddress -- make that first call before any stream capture.
+ * At most 65536 poses per call (more: GBA_ERR_INVALID_ARGUMENT).  Nothing
+ * must be zeroed beforehand (the call clears what it needs with
+ * cudaMemsetAsync).  The pair-term tables it reads are built when the grids
+ * and parameter tables are uploaded; a grid's receptor-typed neighbour list
+ * (GBA_KOPT_TYPED_LIST) is built only by an allocating scoring call, and
+ * until one has run for that grid and receptor this call gathers each
+ * neighbour's type instead (identical results, a little slower).  Calls
+ * that overlap on one device (any stream, thread or context) share the
+ * array and race: serialize them.  Asynchronous on `stream`; results equal
+ * gba_energy_6d's bit for bit. */
 int gba_energy_6d_noalloc(gba_ctx* ctx, gba_id rec, gba_id lig, gba_id grid, gba_id params,
 		const gba_dof6d* dofs, size_t n, gba_result6d* out, void* stream);
 

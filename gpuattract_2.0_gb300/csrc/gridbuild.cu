@@ -15,6 +15,14 @@
  *   voxel v's neighbour list holds, in increasing index, every receptor bead
  *   (type != 0) with |p_v - x_j|^2 <= nl_cutoff^2, tested in double with
  *   unfused operations so the lists are bit-identical to the CPU builder.
+ * Arithmetic of the potentials (the CPU builder performs the same operations
+ * in the same order, so both produce the same bits): the voxel centre in
+ * double, unfused, rounded to float; per bead the separation, its square,
+ * the plateau rescaling (plateau / sqrt(r^2)) and 1/r^2 in IEEE-rounded FP32
+ * (no approximate reciprocal or square root, nothing contracted); the pair
+ * terms of energy_dev.cuh; FP32 partial sums over each block of 256
+ * consecutive receptor beads, in bead order; those partials added in double,
+ * block after block; the total rounded to float.
  * Layout: inner box = bead bounding box + margin, spacing d; outer grid
  * spacing 2d, extended by outer_ext inner voxels per side; NL grid = inner.
  */
@@ -52,9 +60,10 @@ __global__ void __launch_bounds__(kTile) grid_potential_kernel(BuildArgs a, gba_
 	const uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
 	const bool valid = v < N;
 	const uint32_t x = valid ? v % Nx : 0, y = valid ? (v / Nx) % Ny : 0, z = valid ? v / (Nx * Ny) : 0;
-	const float px = (float)((double)d.posMin[0] + x * (double)d.gridSpacing);
-	const float py = (float)((double)d.posMin[1] + y * (double)d.gridSpacing);
-	const float pz = (float)((double)d.posMin[2] + z * (double)d.gridSpacing);
+	const double sp = (double)d.gridSpacing;
+	const float px = (float)__dadd_rn((double)d.posMin[0], __dmul_rn((double)x, sp));
+	const float py = (float)__dadd_rn((double)d.posMin[1], __dmul_rn((double)y, sp));
+	const float pz = (float)__dadd_rn((double)d.posMin[2], __dmul_rn((double)z, sp));
 	const uint32_t c0 = blockIdx.y * kGroup;
 	const uint32_t C = a.n_alphabet + 1;
 	const bool shape86 = a.par.potshape == GBA_POTSHAPE_8_6;
@@ -83,27 +92,27 @@ __global__ void __launch_bounds__(kTile) grid_potential_kernel(BuildArgs a, gba_
 			const uint32_t tr = stype[b];
 			if (tr == 0) continue;
 			const float4 r = sb[b];
-			float ex = px - r.x, ey = py - r.y, ez = pz - r.z;
-			float e2 = ex * ex + ey * ey + ez * ez;
+			float ex = fsub(px, r.x), ey = fsub(py, r.y), ez = fsub(pz, r.z);
+			float e2 = fadd(fadd(fmul(ex, ex), fmul(ey, ey)), fmul(ez, ez));
 			bool dirless = false;
 			if (e2 < a.plat2) {
 				if (e2 > 0.f) {
-					const float s = a.plateau * rsqrtf(e2);
-					ex *= s; ey *= s; ez *= s;
+					const float sc = __fdiv_rn(a.plateau, __fsqrt_rn(e2));
+					ex = fmul(ex, sc); ey = fmul(ey, sc); ez = fmul(ez, sc);
 				} else {
 					dirless = true;
 				}
 				e2 = a.plat2;
 			}
-			const float rr2 = 1.0f / e2;
-			const float ux = dirless ? 0.f : ex * rr2, uy = dirless ? 0.f : ey * rr2,
-					uz = dirless ? 0.f : ez * rr2;
+			const float rr2 = __fdiv_rn(1.0f, e2);
+			const float ux = dirless ? 0.f : fmul(ex, rr2), uy = dirless ? 0.f : fmul(ey, rr2),
+					uz = dirless ? 0.f : fmul(ez, rr2);
 #pragma unroll
 			for (int g = 0; g < kGroup; ++g) {
 				const uint32_t c = c0 + g;
 				float fx, fy, fz, e;
 				if (c == 0) {
-					const float qf = r.w * a.par.ffelec;
+					const float qf = fmul(r.w, a.par.ffelec);
 					if (!(fabsf(qf) > 0.001f)) continue;
 					charge_pot_force(rr2, ux, uy, uz, qf, cdiel, fx, fy, fz, e);
 				} else {
@@ -112,13 +121,16 @@ __global__ void __launch_bounds__(kTile) grid_potential_kernel(BuildArgs a, gba_
 					lj_pot_force(e2, rr2, ux, uy, uz, __ldg(&a.par.lj[k]), __ldg(&a.par.ivor[k]),
 							shape86, fx, fy, fz, e);
 				}
-				tacc[g][0] += fx; tacc[g][1] += fy; tacc[g][2] += fz; tacc[g][3] += e;
+				tacc[g][0] = fadd(tacc[g][0], fx);
+				tacc[g][1] = fadd(tacc[g][1], fy);
+				tacc[g][2] = fadd(tacc[g][2], fz);
+				tacc[g][3] = fadd(tacc[g][3], e);
 			}
 		}
 #pragma unroll
 		for (int g = 0; g < kGroup; ++g)
 #pragma unroll
-			for (int k = 0; k < 4; ++k) acc[g][k] += (double)tacc[g][k];
+			for (int k = 0; k < 4; ++k) acc[g][k] = __dadd_rn(acc[g][k], (double)tacc[g][k]);
 		__syncthreads();
 	}
 	if (!valid) return;

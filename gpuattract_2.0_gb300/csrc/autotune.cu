@@ -157,7 +157,7 @@ extern "C" int gba_autotune(gba_ctx* ctx, gba_id rec, gba_id lig, gba_id grid, g
 						L.out_result = rs;
 						L.n = n;
 						L.max_evals = evals;
-						const float ms = T.best_ms([&] { ctx->run_minimize(L, s, nullptr); }, s, 2);
+						const float ms = T.best_ms([&] { ctx->run_minimize(L, s, nullptr, (base.m.lig.n + 63) / 64); }, s, 2);
 						if (ms < best_m) {
 							best_m = ms;
 							tm = TuneParams{threads, 64, chunk};

@@ -19,8 +19,9 @@
 namespace gba {
 
 /* BOUND4: registers capped for four resident 256-thread blocks per SM
- * (GBA_KOPT_FOUR_BLOCKS). */
-template <bool CENSUS, bool BOUND4>
+ * (GBA_KOPT_FOUR_BLOCKS).  ROUNDWISE: the minimizers' round-wise summation
+ * order (the plain per-step minimization form's launches). */
+template <bool CENSUS, bool BOUND4, bool ROUNDWISE = false>
 __global__ void __launch_bounds__(256, BOUND4 ? 4 : 1) rigid_energy_kernel(const RigidLaunch L) {
 	__shared__ WarpStage stage[8];   /* one per warp of a <=256-thread block */
 	const int lane = threadIdx.x & 31;
@@ -36,7 +37,7 @@ __global__ void __launch_bounds__(256, BOUND4 ? 4 : 1) rigid_energy_kernel(const
 		const float a1 = __shfl_sync(GBA_FULL_MASK, dv, 4);
 		const float a2 = __shfl_sync(GBA_FULL_MASK, dv, 5);
 		float res[7];
-		eval_pose_rigid<CENSUS>(L.m, tx, ty, tz, a0, a1, a2, lane, stage[threadIdx.x >> 5], res,
+		eval_pose_rigid<CENSUS, ROUNDWISE>(L.m, tx, ty, tz, a0, a1, a2, lane, stage[threadIdx.x >> 5], res,
 				CENSUS ? L.census + p : nullptr);
 		store_result7(reinterpret_cast<float*>(L.out + p), res, lane);
 	}
@@ -68,6 +69,10 @@ cudaError_t launch_batch_energy(const BatchEnergyLaunch& L, int blocks, int thre
 cudaError_t launch_rigid_energy(const RigidLaunch& L, int blocks, int threads, cudaStream_t s) {
 	if (L.census)
 		rigid_energy_kernel<true, false><<<blocks, threads, 0, s>>>(L);
+	else if (L.roundwise && L.bound4)
+		rigid_energy_kernel<false, true, true><<<blocks, threads, 0, s>>>(L);
+	else if (L.roundwise)
+		rigid_energy_kernel<false, false, true><<<blocks, threads, 0, s>>>(L);
 	else if (L.bound4)
 		rigid_energy_kernel<false, true><<<blocks, threads, 0, s>>>(L);
 	else
@@ -77,11 +82,11 @@ cudaError_t launch_rigid_energy(const RigidLaunch& L, int blocks, int threads, c
 
 /* resident blocks per SM, queried once per device, instantiation and block
  * size (the query costs host time on every launch otherwise) */
-int rigid_blocks_per_sm(int threads, bool census, bool bound4) {
-	static std::atomic<int> cache[64][3][33];
+int rigid_blocks_per_sm(int threads, bool census, bool bound4, bool roundwise) {
+	static std::atomic<int> cache[64][5][33];
 	int dev = 0;
 	cudaGetDevice(&dev);
-	const int v = census ? 0 : (bound4 ? 1 : 2), t = threads / 32;
+	const int v = census ? 0 : (roundwise ? (bound4 ? 3 : 4) : (bound4 ? 1 : 2)), t = threads / 32;
 	const bool cacheable = dev >= 0 && dev < 64 && threads % 32 == 0 && t >= 1 && t <= 32;
 	if (cacheable) {
 		const int c = cache[dev][v][t].load(std::memory_order_relaxed);
@@ -90,6 +95,10 @@ int rigid_blocks_per_sm(int threads, bool census, bool bound4) {
 	int nb = 0;
 	if (census)
 		cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, rigid_energy_kernel<true, false>, threads, 0);
+	else if (roundwise && bound4)
+		cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, rigid_energy_kernel<false, true, true>, threads, 0);
+	else if (roundwise)
+		cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, rigid_energy_kernel<false, false, true>, threads, 0);
 	else if (bound4)
 		cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, rigid_energy_kernel<false, true>, threads, 0);
 	else

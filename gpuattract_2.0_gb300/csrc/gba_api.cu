@@ -752,7 +752,8 @@ void Context::run_rigid(RigidLaunch& L, cudaStream_t s) {
 	const TuneParams tp = tuned("energy", L.n);
 	const int threads = tp.threads;
 	const int warps_per_block = threads / 32;
-	const int bps = std::min(tp.blocks_per_sm, rigid_blocks_per_sm(threads, L.census != nullptr, L.bound4 && !L.census));
+	const int bps = std::min(tp.blocks_per_sm, rigid_blocks_per_sm(threads, L.census != nullptr, L.bound4 && !L.census,
+			L.roundwise && !L.census));
 	size_t want = (L.n + warps_per_block - 1) / warps_per_block;
 	size_t blocks = std::min<size_t>(want, (size_t)num_sms * bps);
 	if (blocks == 0) blocks = 1;

@@ -144,6 +144,9 @@ struct TuneParams {
 	int threads = 128;
 	int blocks_per_sm = 64;   /* capped by occupancy */
 	int chunk = 1;
+	/* minimizer: warps per pose (1 = one warp per pose, 2..8 = the team
+	 * kernel), 0 = chosen from the job size */
+	int team = 0;
 };
 
 /* Signature of a captured minimizer pipeline. */
@@ -216,7 +219,12 @@ struct Context {
 			const DevIntrpl& box, const RigidModel* models, const uint32_t* pair_of, const uint32_t* pair_rank,
 			size_t npairs, cudaStream_t s);
 	TuneParams tuned(const std::string& kind, size_t n) const;
-	void run_minimize(MinLaunch& L, cudaStream_t s, int32_t* status_out);
+	/* lig_rounds: the largest ligand of the launch in 64-bead rounds (caps
+	 * the team size) */
+	void run_minimize(MinLaunch& L, cudaStream_t s, int32_t* status_out, uint32_t lig_rounds);
+	/* warps per pose the minimizer uses for n poses */
+	int minimize_team(const TuneParams& tp, size_t n, uint32_t lig_rounds) const;
+	int team_override = 0;         /* gba_set_minimize_team; 0 = tuned or automatic */
 	void clear_graphs();
 
 	/* may_allocate = false: the typed list is used only if it already exists

@@ -112,6 +112,7 @@ struct RigidLaunch {
 	const uint32_t* order;    /* visiting order (nullptr: submission order) */
 	size_t n;
 	int bound4;               /* launch the four-blocks-per-SM instantiation */
+	int roundwise;            /* the minimizers' round-wise summation order (plain form) */
 	unsigned long long* next; /* pose counter, zero at launch (PoseFeed); nullptr: fixed stride */
 };
 
@@ -143,6 +144,12 @@ struct MinLaunch {
 
 cudaError_t launch_minimize_rigid(const MinLaunch& L, int blocks, int threads, cudaStream_t s);
 int minimize_blocks_per_sm(int threads);
+/* the team form: `team` (1..kMaxTeam) warps split each pose's ligand rounds,
+ * plus a control warp running VA13; two poses per block; same results bit
+ * for bit */
+constexpr int kMaxTeam = 7;
+cudaError_t launch_minimize_rigid_team(const MinLaunch& L, int blocks, int team, cudaStream_t s);
+int minimize_team_blocks_per_sm(int team);
 
 /* multi-pair scoring: one launch over the poses of many pairs */
 struct BatchEnergyLaunch {
@@ -193,7 +200,7 @@ cudaError_t launch_minimize_modes(const ModesMinLaunch& M, int blocks, int threa
 int minimize_modes_blocks_per_sm(int threads, const ModesLaunch& L);
 
 /* Number of resident blocks per SM of the rigid kernel for `threads`. */
-int rigid_blocks_per_sm(int threads, bool census, bool bound4 = false);
+int rigid_blocks_per_sm(int threads, bool census, bool bound4 = false, bool roundwise = false);
 
 }  // namespace gba
 

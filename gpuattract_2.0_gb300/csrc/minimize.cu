@@ -13,6 +13,18 @@
  * per pose the last evaluated DOF and Result and the evaluation count are
  * written -- what RequestHandler::getResultStates / getResultEnGrads report.
  *
+ * Both kernels sum each pose round-wise (rigid_pose.cuh), as the plain
+ * per-step form's scoring launches do, so all three give the same bits.
+ *
+ * Small jobs (fewer poses than the GPU has warp slots) run the team kernel
+ * instead: a team of G warps evaluates one pose, warp t taking the ligand's
+ * 64-bead rounds t, t + G, ... and the team's first warp adding the round
+ * totals in order (eval_pose_rigid_team) -- the same bits as one warp doing
+ * every round -- so a 200-bead ligand (four rounds) evaluates in about the
+ * time of one round.  Each block adds a control warp and holds two poses:
+ * while the team evaluates one, the control warp's lane 0 runs the other's
+ * VA13 step (FP64, as slow as the evaluation on GB300).
+ *
  * Termination is bounded by construction: every path through the machine
  * either requests an evaluation (nfun <= maxFunEval) or finishes; a pose that
  * went past maxFunEval + 1 evaluations would raise GBA_ERR_DEVICE_CHECK.  A
@@ -52,6 +64,9 @@ extern __shared__ __align__(16) unsigned char min_stage_smem[];
 
 __global__ void __launch_bounds__(256, 4) minimize_rigid_kernel(const MinLaunch L) {
 	WarpStage* stage = reinterpret_cast<WarpStage*>(min_stage_smem);
+	/* per warp, after the staging areas: the VA13 state of its pose (shared
+	 * memory keeps it next to the SM between steps; see TeamShared) */
+	VA13<6>* vas = reinterpret_cast<VA13<6>*>(stage + (blockDim.x >> 5));
 	const int lane = threadIdx.x & 31;
 	unsigned long long t_start = 0;
 	if (lane == 0) t_start = global_ns();
@@ -72,7 +87,7 @@ __global__ void __launch_bounds__(256, 4) minimize_rigid_kernel(const MinLaunch 
 		for (size_t slot = base; slot < end; ++slot) {
 			const size_t p = L.order ? (size_t)__ldg(&L.order[slot]) : slot;
 			const RigidModel& M = L.models[L.pair_of ? __ldg(&L.pair_of[p]) : 0u];
-			VA13<6> va;
+			VA13<6>& va = vas[threadIdx.x >> 5];
 			float cur[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
 			float res[7];
 			int nev = 0;
@@ -90,7 +105,7 @@ __global__ void __launch_bounds__(256, 4) minimize_rigid_kernel(const MinLaunch 
 				}
 #pragma unroll
 				for (int k = 0; k < 6; ++k) cur[k] = __shfl_sync(GBA_FULL_MASK, cur[k], 0);
-				eval_pose_rigid<false>(M, cur[0], cur[1], cur[2], cur[3], cur[4], cur[5], lane, stage[threadIdx.x >> 5], res,
+				eval_pose_rigid<false, true>(M, cur[0], cur[1], cur[2], cur[3], cur[4], cur[5], lane, stage[threadIdx.x >> 5], res,
 						nullptr);
 				++nev;
 				int done = 0;
@@ -121,16 +136,166 @@ __global__ void __launch_bounds__(256, 4) minimize_rigid_kernel(const MinLaunch 
 	}
 }
 
-static size_t min_stage_bytes(int threads) { return (size_t)((threads + 31) / 32) * sizeof(WarpStage); }
+/* One pose slot of a pipelined team block. */
+struct PipeSlot {
+	VA13<6> va;                /* the pose's minimizer state (kept in shared memory: in
+	                              thread-local memory the evaluation's traffic evicted it
+	                              from L1 between steps) */
+	float cur[6];              /* the point to evaluate / last evaluated (DOF_6D order) */
+	float res[7];              /* its Result_6D */
+	int active;                /* a pose occupies the slot */
+	int evaluated;             /* res holds the evaluation of cur, not yet given to VA13 */
+	int nev;                   /* evaluations so far */
+	int pad;
+	unsigned long long p;      /* the pose */
+};
+
+struct PipeShared {
+	PipeSlot slot[2];
+	int more[2];               /* loop continues at half-step h: more[h & 1] */
+};
+
+/* Thread 0: the next pose into slot S (VA13 started, first point ready) or
+ * the slot closed when the queue is empty or the budget is spent. */
+__device__ __forceinline__ void pipe_claim(const MinLaunch& L, PipeSlot& S, unsigned long long t_start,
+		unsigned long long budget) {
+	unsigned long long slot = atomicAdd(L.counter, 1ull);
+	if (slot < L.n && global_ns() - t_start > budget) {
+		atomicExch(L.status, GBA_ERR_TIMEOUT);
+		slot = ~0ull;
+	}
+	if (slot >= L.n) {
+		S.active = 0;
+		return;
+	}
+	const size_t p = L.order ? (size_t)__ldg(&L.order[slot]) : (size_t)slot;
+	const gba_dof6d s0 = L.start[p];
+	/* TypesConverter<DOF_6D, Vector>: (ang xyz, pos xyz), src/apps/em/meta.h:66-97 */
+	const double x0[6] = {s0.ang[0], s0.ang[1], s0.ang[2], s0.pos[0], s0.pos[1], s0.pos[2]};
+	S.va.start(x0, 6, L.max_evals);
+	const double* pt = S.va.point();
+	S.cur[0] = (float)pt[3]; S.cur[1] = (float)pt[4]; S.cur[2] = (float)pt[5];
+	S.cur[3] = (float)pt[0]; S.cur[4] = (float)pt[1]; S.cur[5] = (float)pt[2];
+	S.p = p;
+	S.nev = 0;
+	S.evaluated = 0;
+	S.active = 1;
+}
+
+/* Thread 0: hands the evaluation of slot S to its VA13; on the pose's end
+ * writes its outputs and refills the slot. */
+__device__ __forceinline__ void pipe_consume(const MinLaunch& L, PipeSlot& S, unsigned long long t_start,
+		unsigned long long budget) {
+	S.evaluated = 0;
+	++S.nev;
+	/* objective E, gradient -(ang, pos), src/apps/em/meta.h:114-121 */
+	const double g[6] = {-(double)S.res[4], -(double)S.res[5], -(double)S.res[6],
+			-(double)S.res[1], -(double)S.res[2], -(double)S.res[3]};
+	S.va.provide((double)S.res[0], g);
+	bool stop = S.va.done();
+	/* VA13 ends within max_evals + 1 evaluations; anything past that is a
+	 * broken machine, reported instead of looping */
+	if (!stop && S.nev > L.max_evals + 1) {
+		atomicExch(L.status, GBA_ERR_DEVICE_CHECK);
+		stop = true;
+	}
+	if (!stop && (S.nev & 15) == 0 && global_ns() - t_start > budget) {
+		atomicExch(L.status, GBA_ERR_TIMEOUT);
+		stop = true;
+	}
+	if (!stop) {
+		const double* pt = S.va.point();
+		S.cur[0] = (float)pt[3]; S.cur[1] = (float)pt[4]; S.cur[2] = (float)pt[5];
+		S.cur[3] = (float)pt[0]; S.cur[4] = (float)pt[1]; S.cur[5] = (float)pt[2];
+		return;
+	}
+	float* r = reinterpret_cast<float*>(L.out_result + S.p);
+	float* x = reinterpret_cast<float*>(L.out_state + S.p);
+	for (int k = 0; k < 7; ++k) r[k] = S.res[k];
+	for (int k = 0; k < 6; ++k) x[k] = S.cur[k];
+	if (L.out_nevals) L.out_nevals[S.p] = S.nev;
+	if (L.done_ns) L.done_ns[S.p] = global_ns();
+	pipe_claim(L, S, t_start, budget);
+}
+
+/* The pipelined team kernel: warp 0 is the control warp (its lane 0 runs
+ * VA13), warps 1..G evaluate.  A block holds two poses; in half-step h the
+ * evaluators score slot h & 1 while the control lane gives slot h & 1 ^ 1's
+ * fresh evaluation to its VA13 -- the FP64 minimizer step, about as long as
+ * the evaluation on GB300, runs beside it instead of after it.  Each pose
+ * still alternates evaluation and VA13 step exactly as in the other forms. */
+__global__ void __launch_bounds__(256, 4) minimize_rigid_team_kernel(const MinLaunch L) {
+	const int G = (blockDim.x >> 5) - 1;
+	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+	WarpStage* stage = reinterpret_cast<WarpStage*>(min_stage_smem);
+	float* slots = reinterpret_cast<float*>(stage + G);
+	PipeShared& sh = *reinterpret_cast<PipeShared*>(slots + 16 * G);
+	unsigned long long t_start = 0;
+	const unsigned long long budget = L.budget_ns ? L.budget_ns : kMinimizeHardCapNs;
+	if (threadIdx.x == 0) {
+		t_start = global_ns();
+		if (L.t0) atomicMin(L.t0, t_start);
+		pipe_claim(L, sh.slot[0], t_start, budget);
+		pipe_claim(L, sh.slot[1], t_start, budget);
+		sh.more[0] = sh.slot[0].active | sh.slot[1].active;
+	}
+	for (int h = 0;; ++h) {
+		__syncthreads();
+		if (!sh.more[h & 1]) break;
+		const int e = h & 1;
+		if (warp == 0) {
+			if (lane == 0) {
+				PipeSlot& S = sh.slot[e ^ 1];
+				if (S.active && S.evaluated) pipe_consume(L, S, t_start, budget);
+				sh.more[(h + 1) & 1] = sh.slot[0].active | sh.slot[1].active;
+			}
+		} else {
+			PipeSlot& S = sh.slot[e];
+			if (S.active && !S.evaluated) {
+				const RigidModel& M = L.models[L.pair_of ? __ldg(&L.pair_of[S.p]) : 0u];
+				float res[7];
+				eval_pose_rigid_team(M, S.cur[0], S.cur[1], S.cur[2], S.cur[3], S.cur[4], S.cur[5], lane,
+						warp - 1, G, stage, slots, res, 1);
+				if (warp == 1) {
+					if (lane < 7) S.res[lane] = res[lane];
+					__syncwarp();
+					if (lane == 0) S.evaluated = 1;
+				}
+			}
+		}
+	}
+}
+
+static size_t min_stage_bytes(int threads) {
+	return (size_t)((threads + 31) / 32) * (sizeof(WarpStage) + sizeof(VA13<6>));
+}
+
+/* shared memory of the team kernel with `team` evaluation warps */
+static size_t team_smem_bytes(int team) {
+	return (size_t)team * (sizeof(WarpStage) + sizeof(float) * 16) + sizeof(PipeShared);
+}
 
 cudaError_t launch_minimize_rigid(const MinLaunch& L, int blocks, int threads, cudaStream_t s) {
 	minimize_rigid_kernel<<<blocks, threads, min_stage_bytes(threads), s>>>(L);
 	return cudaGetLastError();
 }
 
+cudaError_t launch_minimize_rigid_team(const MinLaunch& L, int blocks, int team, cudaStream_t s) {
+	if (team < 1 || team > kMaxTeam) return cudaErrorInvalidValue;
+	minimize_rigid_team_kernel<<<blocks, 32 * (team + 1), team_smem_bytes(team), s>>>(L);
+	return cudaGetLastError();
+}
+
 int minimize_blocks_per_sm(int threads) {
 	int nb = 0;
 	cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, minimize_rigid_kernel, threads, min_stage_bytes(threads));
+	return nb > 0 ? nb : 1;
+}
+
+int minimize_team_blocks_per_sm(int team) {
+	int nb = 0;
+	cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, minimize_rigid_team_kernel, 32 * (team + 1),
+			team_smem_bytes(team));
 	return nb > 0 ? nb : 1;
 }
 

@@ -3,7 +3,8 @@
  *
  *   gba_minimize_6d        batched form: one persistent work-queue launch,
  *                          VA13 on the device, the whole pipeline (cursor
- *                          reset, copies, kernel) replayed as a cached CUDA graph
+ *                          reset, copies, kernel) replayed as a cached CUDA
+ *                          graph; small jobs give each pose a team of warps
  *   gba_minimize_6d_plain  the reference's execution model on the same GPU:
  *                          VA13 per pose on the host, one energy launch plus
  *                          host<->device copies per evaluation round
@@ -42,16 +43,37 @@ struct Placement {
 
 }  // namespace
 
+int Context::minimize_team(const TuneParams& tp, size_t n, uint32_t lig_rounds) const {
+	int team = team_override ? team_override : tp.team;
+	if (team == 0) {
+		/* fewer poses than the one-warp kernel has resident warps: give each
+		 * pose as many warps as fill them, up to its ligand's rounds */
+		const size_t slots = (size_t)num_sms * minimize_blocks_per_sm(tp.threads) * (tp.threads / 32);
+		team = n > 0 && n * 2 <= slots ? (int)std::min<size_t>(kMaxTeam, slots / n) : 1;
+	}
+	team = std::min<int>(team, (int)std::max<uint32_t>(1, lig_rounds));
+	return std::max(1, std::min(team, kMaxTeam));
+}
+
 /* Runs the persistent minimizer over `total` poses whose inputs/outputs live
  * in device memory; captured in a CUDA graph cached by launch signature. */
-void Context::run_minimize(MinLaunch& L, cudaStream_t s, int32_t* status_out) {
+void Context::run_minimize(MinLaunch& L, cudaStream_t s, int32_t* status_out, uint32_t lig_rounds) {
 	TuneParams tp = tuned("minimize", L.n);
-	const int threads = tp.threads;
-	const int bps = std::min(tp.blocks_per_sm, minimize_blocks_per_sm(threads));
-	const size_t warps = (size_t)num_sms * bps * (threads / 32);
-	size_t blocks = (size_t)num_sms * bps;
-	if (warps > L.n) blocks = std::max<size_t>(1, (L.n * 32 + threads - 1) / threads);
-	L.chunk = tp.chunk;
+	const int team = minimize_team(tp, L.n, lig_rounds);
+	int threads = tp.threads;
+	size_t blocks;
+	if (team > 1) {
+		/* team evaluation warps plus a control warp; two poses per block */
+		threads = 32 * (team + 1);
+		blocks = std::min<size_t>((L.n + 1) / 2, (size_t)num_sms * minimize_team_blocks_per_sm(team));
+		L.chunk = 1;
+	} else {
+		const int bps = std::min(tp.blocks_per_sm, minimize_blocks_per_sm(threads));
+		const size_t warps = (size_t)num_sms * bps * (threads / 32);
+		blocks = (size_t)num_sms * bps;
+		if (warps > L.n) blocks = std::max<size_t>(1, (L.n * 32 + threads - 1) / threads);
+		L.chunk = tp.chunk;
+	}
 	if (!aux.ptr) {
 		aux.alloc(64);
 		note_allocation();
@@ -75,7 +97,7 @@ void Context::run_minimize(MinLaunch& L, cudaStream_t s, int32_t* status_out) {
 	key.p0 = L.max_evals;
 	key.p1 = (int)blocks;
 	key.p2 = threads;
-	key.p3 = L.chunk;
+	key.p3 = L.chunk | team << 16;
 	key.deadline = L.budget_ns;
 	cudaGraphExec_t exec = nullptr;
 	auto it = graphs.find(key);
@@ -87,7 +109,8 @@ void Context::run_minimize(MinLaunch& L, cudaStream_t s, int32_t* status_out) {
 		check_cuda(cudaStreamBeginCapture(capture_stream, cudaStreamCaptureModeThreadLocal), "capture");
 		cudaMemsetAsync(aux.ptr, 0, 16, capture_stream);
 		cudaMemsetAsync((char*)aux.ptr + 32, 0xff, 8, capture_stream);
-		cudaError_t le = launch_minimize_rigid(L, (int)blocks, threads, capture_stream);
+		cudaError_t le = team > 1 ? launch_minimize_rigid_team(L, (int)blocks, team, capture_stream)
+		                          : launch_minimize_rigid(L, (int)blocks, threads, capture_stream);
 		cudaMemcpyAsync(pinned_status, L.status, sizeof(int32_t), cudaMemcpyDeviceToHost, capture_stream);
 		cudaGraph_t g = nullptr;
 		cudaError_t ce = cudaStreamEndCapture(capture_stream, &g);
@@ -171,6 +194,18 @@ void copy_out(void* dst, const void* src, size_t bytes, cudaStream_t s) {
 
 extern "C" {
 
+int gba_set_minimize_team(gba_ctx* ctx, int warps_per_pose) {
+	if (!ctx) return GBA_ERR_INVALID_ARGUMENT;
+	GBA_TRY
+	if (warps_per_pose < 0 || warps_per_pose > kMaxTeam)
+		throw ApiError(GBA_ERR_INVALID_ARGUMENT, "gba_set_minimize_team: warps per pose must be 0.." +
+				std::to_string(kMaxTeam));
+	ctx->bind();
+	Lock g(ctx->stage_mu);
+	ctx->team_override = warps_per_pose;
+	GBA_CATCH(ctx)
+}
+
 int gba_minimize_6d(gba_ctx* ctx, gba_id rec, gba_id lig, gba_id grid, gba_id params,
 		const gba_dof6d* start, size_t n, int max_evals, gba_dof6d* out_state,
 		gba_result6d* out_result, int32_t* out_nevals, void* stream) {
@@ -243,7 +278,9 @@ int gba_batch_minimize_6d(gba_ctx* ctx, const gba_pair_job* jobs, size_t njobs, 
 	L.order = ctx->pose_order_persistent(L.start, 6, n, G.models[0].grid.outer, L.models, L.pair_of,
 			pair_rank, njobs, s);
 	int32_t status = GBA_OK;
-	ctx->run_minimize(L, s, &status);
+	uint32_t lig_rounds = 1;
+	for (const RigidModel& m : G.models) lig_rounds = std::max(lig_rounds, (m.lig.n + 63) / 64);
+	ctx->run_minimize(L, s, &status, lig_rounds);
 	if (!single_dev) {
 		for (size_t j = 0; j < njobs; ++j) {
 			const size_t o = G.offset[j], m = jobs[j].n;
@@ -359,6 +396,7 @@ int gba_minimize_6d_plain(gba_ctx* ctx, gba_id rec, gba_id lig, gba_id grid, gba
 			L.out = dout + b;
 			L.n = m;
 			L.census = nullptr;
+			L.roundwise = 1;      /* the device minimizer's summation order */
 			ctx->run_rigid(L, s);
 			check_cuda(cudaMemcpyAsync(hout + b, dout + b, m * sizeof(gba_result6d), cudaMemcpyDeviceToHost, s),
 					"plain: D2H");

@@ -23,9 +23,20 @@
  *      measured on GB300, this order is faster.
  * Every lookup and pair contributes straight to the pose sums: energy,
  * force and the torque matrix sum_i x_i (x) f_i are linear in the bead
- * forces, so no per-bead force is kept.  The warp then reduces with
- * shuffles (reducePotForce / reduceTorque, src/model/reduction.h:40-103) and
- * every lane ends with the 7 result values.
+ * forces, so no per-bead force is kept (reducePotForce / reduceTorque,
+ * src/model/reduction.h:40-103).  Two summation orders exist:
+ *   per pose   (scoring kernels) each lane accumulates over all rounds and
+ *              the warp reduces once per pose;
+ *   round-wise (minimizer kernels and the plain per-step form's launches)
+ *              each 64-bead round is reduced on its own by a fixed 16-value
+ *              reduce-scatter (round_reduce) and the round totals are added
+ *              in round order, so a pose's result does not depend on which
+ *              warp evaluates which round: a team of warps splitting one
+ *              pose (eval_pose_rigid_team) gives the same bits as one warp.
+ * Both are deterministic; they differ from each other in the last bits.  The
+ * per-pose order stays in the scoring kernels because the round-wise
+ * reduction costs them registers at their 64-register bound (it spills and
+ * measured 13 % slower on config 1).
  */
 #ifndef GBA_RIGID_POSE_CUH_
 #define GBA_RIGID_POSE_CUH_
@@ -51,6 +62,9 @@ struct WarpStage {
 	/* the pose: rotation matrix [0, 9), sin/cos of phi, ssi, rot [9, 15),
 	 * translation [15, 18); kept here rather than in registers */
 	float pose[18];
+	/* round-wise order: running total of the rounds, component c in tot[c]
+	 * (written by lane 2c) */
+	float tot[16];
 };
 
 /* Stores the pose rotation and translation in the warp's staging area. */
@@ -502,114 +516,231 @@ __device__ __forceinline__ void pair_term(const RigidModel& M, const WarpStage& 
 		S.add(e, fx, fy, fz, u.x, u.y, u.z);
 }
 
-/* res: E, force xyz, Euler gradient xyz (Result_6D order); identical on all
- * lanes.  W is this warp's shared staging area. */
+/* Per-pose counters of the census (CENSUS instantiations only). */
+struct RoundCensus {
+	uint32_t grid = 0, charged = 0, nl = 0, ent = 0;
+};
+
+/* One round: beads [i0, i0 + 64) of the pose staged in W, added to the
+ * lane sums S. */
 template <bool CENSUS>
-__device__ __forceinline__ void eval_pose_rigid(const RigidModel& M, float tx, float ty, float tz,
-		float a0, float a1, float a2, int lane, WarpStage& W, float res[7], PoseCensus* census) {
-	put_pose(W, pose_rotation(a0, a1, a2, lane), tx, ty, tz, lane);
-	PoseSums S;
-	uint32_t c_grid = 0, c_charged = 0, c_nl = 0, c_ent = 0;
-	for (uint32_t i0 = 0; i0 < M.lig.n; i0 += kBeadsPerRound) {
-		/* 1. stage 64 beads, two per lane: lane, then lane + 32 */
-		float ttx, tty, ttz;
-		const PoseRot R = get_pose(W, ttx, tty, ttz);
-		uint32_t nlk[2], nln[2];
-		BeadGrid bg[2];
+__device__ __forceinline__ void eval_round(const RigidModel& M, uint32_t i0, int lane, WarpStage& W,
+		RoundCensus& cen, PoseSums& S) {
+	/* 1. stage 64 beads, two per lane: lane, then lane + 32 */
+	float ttx, tty, ttz;
+	const PoseRot R = get_pose(W, ttx, tty, ttz);
+	uint32_t nlk[2], nln[2];
+	BeadGrid bg[2];
 #pragma unroll
-		for (int h = 0; h < 2; ++h) {
-			const int s = lane + 32 * h;
-			const uint32_t i = i0 + s;
-			nlk[h] = 0;
-			nln[h] = 0;
-			bg[h] = BeadGrid{0u, 0u};
-			bool in_nl = false;
-			if (i < M.lig.n) {
-				const float4 b = __ldg(&M.lig.xyzq[i]);
-				const uint32_t tm = __ldg(&M.lig.tm[i]);
-				const uint32_t type = tm & 0xffffu, mapped = tm >> 16;
-				float px, py, pz;
-				rot_apply(R.m, b.x, b.y, b.z, px, py, pz);
-				px = fadd(px, ttx); py = fadd(py, tty); pz = fadd(pz, ttz);
-				put_bead(W, s, b.x, b.y, b.z, px, py, pz, b.w, type);
-				nlk[h] = stage_grid(M.grid, px, py, pz, mapped, b.w, s, W, bg[h]);
-				if (type != 0) nln[h] = stage_nl(M.grid.nl, px, py, pz, s, W, in_nl);
-			}
-			if (CENSUS) {
-				c_grid += nlk[h] > 0;
-				c_charged += nlk[h] > 1;
-				c_nl += in_nl;
-				c_ent += nln[h];
-			}
+	for (int h = 0; h < 2; ++h) {
+		const int s = lane + 32 * h;
+		const uint32_t i = i0 + s;
+		nlk[h] = 0;
+		nln[h] = 0;
+		bg[h] = BeadGrid{0u, 0u};
+		bool in_nl = false;
+		if (i < M.lig.n) {
+			const float4 b = __ldg(&M.lig.xyzq[i]);
+			const uint32_t tm = __ldg(&M.lig.tm[i]);
+			const uint32_t type = tm & 0xffffu, mapped = tm >> 16;
+			float px, py, pz;
+			rot_apply(R.m, b.x, b.y, b.z, px, py, pz);
+			px = fadd(px, ttx); py = fadd(py, tty); pz = fadd(pz, ttz);
+			put_bead(W, s, b.x, b.y, b.z, px, py, pz, b.w, type);
+			nlk[h] = stage_grid(M.grid, px, py, pz, mapped, b.w, s, W, bg[h]);
+			if (type != 0) nln[h] = stage_nl(M.grid.nl, px, py, pz, s, W, in_nl);
 		}
-		const uint32_t n_look = queue_lookups(W, nlk, bg, lane);
-		uint32_t start[2];
-		const uint32_t n_pair = queue_pairs(W, nln, lane, start);
-		__syncwarp();
-
-		/* 2. neighbour pairs, two per lane and window so that both gather
-		 * chains (list entry -> receptor bead -> parameters) are in flight
-		 * together, the next window's list entries already on their way */
-		PairWindow win;
-		/* list entries of the next window are loaded while this one is
-		 * computed; typed entries carry the receptor type in bits 24..31 */
-		const uint32_t* lst = M.grid.nl.typed_list ? M.grid.nl.typed_list : M.grid.nl.list;
-		const bool typed = M.grid.nl.typed_list != nullptr;
-		uint32_t sa = 0, sb = 0, ea = 0, eb = 0;
-		if (n_pair > 0) {
-			win.owners(W, 0, start, nln, lane, sa, sb);
-			if ((uint32_t)lane < n_pair) ea = __ldg(&lst[W.lbase[sa] + lane]);
-			if ((uint32_t)lane + 32 < n_pair) eb = __ldg(&lst[W.lbase[sb] + lane + 32]);
+		if (CENSUS) {
+			cen.grid += nlk[h] > 0;
+			cen.charged += nlk[h] > 1;
+			cen.nl += in_nl;
+			cen.ent += nln[h];
 		}
-		for (uint32_t w = 0; w < n_pair; w += 64) {
-			const uint32_t k = w + lane, k2 = k + 32;
-			const uint32_t csa = sa, csb = sb, cea = ea, ceb = eb;
-			if (w + 64 < n_pair) {
-				win.owners(W, w + 64, start, nln, lane, sa, sb);
-				if (k + 64 < n_pair) ea = __ldg(&lst[W.lbase[sa] + k + 64]);
-				if (k2 + 64 < n_pair) eb = __ldg(&lst[W.lbase[sb] + k2 + 64]);
-			}
-			if (k >= n_pair) continue;
-			const bool has2 = k2 < n_pair;
-			const uint32_t eb2 = has2 ? ceb : cea;
-			const uint32_t ja = typed ? cea & 0xffffffu : cea;
-			const uint32_t jb = typed ? eb2 & 0xffffffu : eb2;
-			const float4 ra = __ldg(&M.rec.xyzq[ja]);
-			const float4 rb = __ldg(&M.rec.xyzq[jb]);
-			const uint32_t ta = typed ? cea >> 24 : __ldg(&M.rec.tm[ja]) & 0xffffu;
-			const uint32_t tb = typed ? eb2 >> 24 : __ldg(&M.rec.tm[jb]) & 0xffffu;
-			pair_term(M, W, csa, ra, ta, S);
-			if (has2) pair_term(M, W, csb, rb, tb, S);
-		}
-
-		/* 3. grid lookups (cooperative sums folded per round) */
-		{
-			CoopSums Cr;
-			drain_lookups(M.grid, W, n_look, lane, S, Cr);
-			fold_coop(Cr, S, lane);
-		}
-		__syncwarp();
 	}
-	float sE = warp_sum(S.E), sFx = warp_sum(S.Fx), sFy = warp_sum(S.Fy), sFz = warp_sum(S.Fz);
-	float T[9];
+	const uint32_t n_look = queue_lookups(W, nlk, bg, lane);
+	uint32_t start[2];
+	const uint32_t n_pair = queue_pairs(W, nln, lane, start);
+	__syncwarp();
+
+	/* 2. neighbour pairs, two per lane and window so that both gather
+	 * chains (list entry -> receptor bead -> parameters) are in flight
+	 * together, the next window's list entries already on their way */
+	PairWindow win;
+	/* list entries of the next window are loaded while this one is
+	 * computed; typed entries carry the receptor type in bits 24..31 */
+	const uint32_t* lst = M.grid.nl.typed_list ? M.grid.nl.typed_list : M.grid.nl.list;
+	const bool typed = M.grid.nl.typed_list != nullptr;
+	uint32_t sa = 0, sb = 0, ea = 0, eb = 0;
+	if (n_pair > 0) {
+		win.owners(W, 0, start, nln, lane, sa, sb);
+		if ((uint32_t)lane < n_pair) ea = __ldg(&lst[W.lbase[sa] + lane]);
+		if ((uint32_t)lane + 32 < n_pair) eb = __ldg(&lst[W.lbase[sb] + lane + 32]);
+	}
+	for (uint32_t w = 0; w < n_pair; w += 64) {
+		const uint32_t k = w + lane, k2 = k + 32;
+		const uint32_t csa = sa, csb = sb, cea = ea, ceb = eb;
+		if (w + 64 < n_pair) {
+			win.owners(W, w + 64, start, nln, lane, sa, sb);
+			if (k + 64 < n_pair) ea = __ldg(&lst[W.lbase[sa] + k + 64]);
+			if (k2 + 64 < n_pair) eb = __ldg(&lst[W.lbase[sb] + k2 + 64]);
+		}
+		if (k >= n_pair) continue;
+		const bool has2 = k2 < n_pair;
+		const uint32_t eb2 = has2 ? ceb : cea;
+		const uint32_t ja = typed ? cea & 0xffffffu : cea;
+		const uint32_t jb = typed ? eb2 & 0xffffffu : eb2;
+		const float4 ra = __ldg(&M.rec.xyzq[ja]);
+		const float4 rb = __ldg(&M.rec.xyzq[jb]);
+		const uint32_t ta = typed ? cea >> 24 : __ldg(&M.rec.tm[ja]) & 0xffffu;
+		const uint32_t tb = typed ? eb2 >> 24 : __ldg(&M.rec.tm[jb]) & 0xffffu;
+		pair_term(M, W, csa, ra, ta, S);
+		if (has2) pair_term(M, W, csb, rb, tb, S);
+	}
+
+	/* 3. grid lookups (cooperative sums folded per round) */
+	{
+		CoopSums Cr;
+		drain_lookups(M.grid, W, n_look, lane, S, Cr);
+		fold_coop(Cr, S, lane);
+	}
+	__syncwarp();
+}
+
+/* Reduce-scatter of a round's lane sums over the warp in a fixed butterfly:
+ * lane l returns component l >> 1 of (E, Fx, Fy, Fz, T[0..8], 0, 0, 0)
+ * summed over all 32 lanes (lanes 2c and 2c + 1 hold the same value). */
+__device__ __forceinline__ float round_reduce(const PoseSums& S, int lane) {
+	const float v[16] = {S.E, S.Fx, S.Fy, S.Fz, S.T[0], S.T[1], S.T[2], S.T[3], S.T[4], S.T[5], S.T[6],
+			S.T[7], S.T[8], 0.f, 0.f, 0.f};
+	const bool b4 = lane & 16, b3 = lane & 8, b2 = lane & 4, b1 = lane & 2;
+	float m8[8];
 #pragma unroll
-	for (int k = 0; k < 9; ++k) T[k] = warp_sum(S.T[k]);
+	for (int j = 0; j < 8; ++j)
+		m8[j] = fadd(b4 ? v[8 + j] : v[j], __shfl_xor_sync(GBA_FULL_MASK, b4 ? v[j] : v[8 + j], 16));
+	float m4[4];
+#pragma unroll
+	for (int j = 0; j < 4; ++j)
+		m4[j] = fadd(b3 ? m8[4 + j] : m8[j], __shfl_xor_sync(GBA_FULL_MASK, b3 ? m8[j] : m8[4 + j], 8));
+	float m2[2];
+#pragma unroll
+	for (int j = 0; j < 2; ++j)
+		m2[j] = fadd(b2 ? m4[2 + j] : m4[j], __shfl_xor_sync(GBA_FULL_MASK, b2 ? m4[j] : m4[2 + j], 4));
+	const float m1 = fadd(b1 ? m2[1] : m2[0], __shfl_xor_sync(GBA_FULL_MASK, b1 ? m2[0] : m2[1], 2));
+	return fadd(m1, __shfl_xor_sync(GBA_FULL_MASK, m1, 1));
+}
+
+/* Clears the warp's round totals. */
+__device__ __forceinline__ void clear_totals(WarpStage& W, int lane) {
+	if (lane < 16) W.tot[lane] = 0.f;
+	__syncwarp();
+}
+
+/* Adds a round's component (lane 2c holds component c) to the totals. */
+__device__ __forceinline__ void add_round(WarpStage& W, float v, int lane) {
+	if ((lane & 1) == 0) W.tot[lane >> 1] = fadd(W.tot[lane >> 1], v);
+}
+
+/* The pose result from the round totals: ForceLim on the force sum and the
+ * TorqueMat contraction, on every lane. */
+__device__ __forceinline__ void finish_pose(const WarpStage& W, float res[7]) {
+	__syncwarp();
+	const volatile float* t = W.tot;
+	float c[13];
+#pragma unroll
+	for (int k = 0; k < 13; ++k) c[k] = t[k];
+	float sFx = c[1], sFy = c[2], sFz = c[3];
 	force_lim(sFx, sFy, sFz);
 	float ang[3];
 	float ttx, tty, ttz;
-	torque_reduce(get_pose(W, ttx, tty, ttz), T, ang);
-	res[0] = sE; res[1] = sFx; res[2] = sFy; res[3] = sFz;
+	torque_reduce(get_pose(W, ttx, tty, ttz), c + 4, ang);
+	res[0] = c[0]; res[1] = sFx; res[2] = sFy; res[3] = sFz;
 	res[4] = ang[0]; res[5] = ang[1]; res[6] = ang[2];
+}
+
+/* res: E, force xyz, Euler gradient xyz (Result_6D order); identical on all
+ * lanes.  W is this warp's shared staging area.  ROUNDWISE selects the
+ * round-wise summation order (see the file comment). */
+template <bool CENSUS, bool ROUNDWISE = false>
+__device__ __forceinline__ void eval_pose_rigid(const RigidModel& M, float tx, float ty, float tz,
+		float a0, float a1, float a2, int lane, WarpStage& W, float res[7], PoseCensus* census) {
+	put_pose(W, pose_rotation(a0, a1, a2, lane), tx, ty, tz, lane);
+	RoundCensus cen;
+	if (ROUNDWISE) {
+		clear_totals(W, lane);
+		for (uint32_t i0 = 0; i0 < M.lig.n; i0 += kBeadsPerRound) {
+			PoseSums S;
+			eval_round<CENSUS>(M, i0, lane, W, cen, S);
+			add_round(W, round_reduce(S, lane), lane);
+		}
+		finish_pose(W, res);
+	} else {
+		PoseSums S;
+		for (uint32_t i0 = 0; i0 < M.lig.n; i0 += kBeadsPerRound) eval_round<CENSUS>(M, i0, lane, W, cen, S);
+		float sE = warp_sum(S.E), sFx = warp_sum(S.Fx), sFy = warp_sum(S.Fy), sFz = warp_sum(S.Fz);
+		float T[9];
+#pragma unroll
+		for (int k = 0; k < 9; ++k) T[k] = warp_sum(S.T[k]);
+		force_lim(sFx, sFy, sFz);
+		float ang[3];
+		float ttx, tty, ttz;
+		torque_reduce(get_pose(W, ttx, tty, ttz), T, ang);
+		res[0] = sE; res[1] = sFx; res[2] = sFy; res[3] = sFz;
+		res[4] = ang[0]; res[5] = ang[1]; res[6] = ang[2];
+	}
 	if (CENSUS) {
 #pragma unroll
 		for (int o = 16; o > 0; o >>= 1) {
-			c_grid += __shfl_xor_sync(GBA_FULL_MASK, c_grid, o);
-			c_charged += __shfl_xor_sync(GBA_FULL_MASK, c_charged, o);
-			c_nl += __shfl_xor_sync(GBA_FULL_MASK, c_nl, o);
-			c_ent += __shfl_xor_sync(GBA_FULL_MASK, c_ent, o);
+			cen.grid += __shfl_xor_sync(GBA_FULL_MASK, cen.grid, o);
+			cen.charged += __shfl_xor_sync(GBA_FULL_MASK, cen.charged, o);
+			cen.nl += __shfl_xor_sync(GBA_FULL_MASK, cen.nl, o);
+			cen.ent += __shfl_xor_sync(GBA_FULL_MASK, cen.ent, o);
 		}
-		if (lane == 0) *census = PoseCensus{c_grid, c_charged, c_nl, c_ent};
+		if (lane == 0) *census = PoseCensus{cen.grid, cen.charged, cen.nl, cen.ent};
 	}
+}
+
+/* Barrier of the `nthreads` threads that use barrier `id` (a named barrier:
+ * a subset of the block's warps). */
+__device__ __forceinline__ void group_sync(int id, int nthreads) {
+	asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
+}
+
+/* One pose evaluated by a team of G warps (t = 0..G-1) that synchronize
+ * with named barrier bar_id: warp t takes rounds t, t + G, t + 2G, ...;
+ * after each group of G rounds the warps park their round components in
+ * slots[16 t + c] and warp 0 adds them in round order -- the arithmetic of
+ * eval_pose_rigid<_, true>, so the result is the same bit for bit.  Warp 0
+ * computes the rotation (double sincos: GB300's FP64 pipe is narrow) and the
+ * others copy it.  Every warp of the team must call it; res is valid in
+ * warp 0.  stages: the G warps' staging areas. */
+__device__ __forceinline__ void eval_pose_rigid_team(const RigidModel& M, float tx, float ty, float tz,
+		float a0, float a1, float a2, int lane, int t, int G, WarpStage* stages, float* slots, float res[7],
+		int bar_id) {
+	const int nthreads = 32 * G;
+	WarpStage& W = stages[t];
+	if (t == 0) put_pose(W, pose_rotation(a0, a1, a2, lane), tx, ty, tz, lane);
+	group_sync(bar_id, nthreads);
+	if (t != 0) {
+		if (lane < 18) W.pose[lane] = stages[0].pose[lane];
+		__syncwarp();
+	}
+	clear_totals(W, lane);
+	const uint32_t rounds = (M.lig.n + kBeadsPerRound - 1) / kBeadsPerRound;
+	RoundCensus cen;
+	for (uint32_t r0 = 0; r0 < rounds; r0 += G) {
+		const uint32_t r = r0 + t;
+		if (r < rounds) {
+			PoseSums S;
+			eval_round<false>(M, r * kBeadsPerRound, lane, W, cen, S);
+			const float v = round_reduce(S, lane);
+			if ((lane & 1) == 0) slots[16 * t + (lane >> 1)] = v;
+		}
+		group_sync(bar_id, nthreads);
+		if (t == 0)
+			for (int u = 0; u < G && r0 + u < rounds; ++u) add_round(W, slots[16 * u + (lane >> 1)], lane);
+		group_sync(bar_id, nthreads);
+	}
+	if (t == 0) finish_pose(W, res);
 }
 
 /* Lanes 0..6 store the 7 result floats (one coalesced 28-byte write). */

@@ -313,6 +313,19 @@ int gba_minimize_6d_modes_plain(gba_ctx* ctx, gba_id rec, gba_id lig, gba_id gri
 		size_t item_size, gba_dof6d_modes* out_state, gba_result6d_modes* out_result,
 		int32_t* out_nevals, void* stream);
 
+/* Warps per pose of the device minimizer (no reference counterpart; a
+ * launch-shape choice): 0 (default) = chosen from the job size -- jobs with
+ * fewer poses than the one-warp kernel has resident warps give each pose a
+ * team of up to 7 warps, never more than its ligand has 64-bead rounds;
+ * 1 = one warp per pose; 2..7 = teams of that many warps (capped by the
+ * ligand's rounds), each block adding a control warp that runs one pose's
+ * VA13 step while the team evaluates the block's other pose.  The result of
+ * every pose is the same bit for bit whatever the setting: the minimizers
+ * reduce each 64-bead round on its own and add the rounds in order (the
+ * plain per-step form's launches do the same; gba_energy_6d reduces once
+ * per pose, which differs in the last bits). */
+int gba_set_minimize_team(gba_ctx* ctx, int warps_per_pose);
+
 /* Wall-time budget for device minimization (0 = none): warps stop claiming
  * poses once it is spent and the call returns GBA_ERR_TIMEOUT; the
  * counterpart of Server::setWaitTime (src/server/Server.h:71). */

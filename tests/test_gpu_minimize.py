@@ -17,6 +17,12 @@ from test_gpu_rigid import upload
 pytestmark = pytest.mark.gpu
 
 
+def evaluate_roundwise(ctx, ids, dofs):
+    """One energy evaluation per pose in the minimizers' round-wise summation
+    order: the plain form with a zero evaluation budget."""
+    return ctx.minimize_6d_plain(*ids, dofs, max_evals=0)[1]
+
+
 @pytest.fixture(scope="module")
 def ctx(pkg):
     from gbattract.context import GbaContext
@@ -32,7 +38,7 @@ def min_case(pkg, oracle):
     return wl, grid
 
 
-def test_device_equals_plain_form(min_case, ctx):
+def test_device_equals_plain_form(min_case, oracle, ctx):
     wl, grid = min_case
     ids = upload(ctx, wl.rec, wl.lig, grid, wl.params)
     s1, r1, n1 = ctx.minimize_6d(*ids, wl.dofs, max_evals=100)
@@ -47,8 +53,14 @@ def test_device_equals_plain_form(min_case, ctx):
     # the minimizer lowers the energy of the start poses
     e0 = ctx.energy_6d(*ids, wl.dofs)[:, 0]
     assert np.mean(r1[:, 0] <= e0 + 1e-6 * np.abs(e0)) > 0.95
-    # the reported result is the energy of the reported state
-    assert np.array_equal(ctx.energy_6d(*ids, s1), r1)
+    # the reported result is the energy of the reported state: bit for bit in
+    # the minimizers' round-wise summation order (one plain evaluation), and
+    # within rounding of the scoring kernel's per-pose order
+    assert np.array_equal(evaluate_roundwise(ctx, ids, s1), r1)
+    from test_gpu_rigid import pose_errors
+    _, st = oracle.energy_6d(wl.rec, wl.lig, grid, wl.params, s1, stats=True)
+    for e in pose_errors(ctx.energy_6d(*ids, s1), r1, st):
+        assert float(e.max()) <= 1e-4
 
 
 def test_against_cpu_oracle_va13(pkg, oracle, ctx):
@@ -94,12 +106,40 @@ def test_against_cpu_oracle_va13(pkg, oracle, ctx):
     assert abs(st["a_at_least_as_low"] - st["b_at_least_as_low"]) <= 0.05
     for qa, qb in zip(st["a_quantiles"], st["b_quantiles"]):
         assert abs(qa - qb) <= 0.02 * abs(qb)
-    e0 = ctx.energy_6d(*ids, wl.dofs)[:, 0]
-    assert np.all(r_dev[:, 0] <= e0)
+    # VA13 reports the last evaluated point, not the best: almost every pose
+    # still ends below its start
+    e0 = evaluate_roundwise(ctx, ids, wl.dofs)[:, 0]
+    assert np.mean(r_dev[:, 0] <= e0) >= 0.99
     with oracle.exact_sincos():
         ref, est = oracle.energy_6d(wl.rec, wl.lig, grid, wl.params, s_dev, stats=True)
     for e in pose_errors(r_dev, ref, est):
         assert float(e.max()) <= 1e-4
+    for i in (gid, lig, rec, par):
+        ctx.release(i)
+
+
+def test_team_sizes_give_identical_results(pkg, ctx):
+    """One warp per pose, teams of 2..7 warps splitting a pose's ligand
+    rounds, and the automatic choice give the same trajectories bit for bit
+    (each 64-bead round is reduced on its own, rounds are added in order),
+    and so does the plain per-step form, whose scoring launches give each
+    pose one warp.  A 260-bead ligand has five rounds, so teams of 2, 3 and
+    4 all split unevenly."""
+    wl = pkg.synth.make_pair(0, 500, 260, 300, (38.0, 46.0), seed=4242)
+    rec, lig, par = ctx.upload_protein(wl.rec), ctx.upload_protein(wl.lig), ctx.upload_params(wl.params)
+    gid = ctx.build_grid(rec, par, pkg.GridOptions())
+    ctx.grid_octets(gid, True)
+    ids = (rec, lig, gid, par)
+    ref = ctx.minimize_6d_plain(*ids, wl.dofs, max_evals=40)
+    try:
+        for team in (1, 2, 3, 4, 5, 7, 0):
+            ctx.set_minimize_team(team)
+            got = ctx.minimize_6d(*ids, wl.dofs, max_evals=40)
+            for a, b in zip(got, ref):
+                assert np.array_equal(a, b), f"team {team}"
+    finally:
+        ctx.set_minimize_team(0)
+    assert np.array_equal(evaluate_roundwise(ctx, ids, ref[0]), ref[1])
     for i in (gid, lig, rec, par):
         ctx.release(i)
 
@@ -133,7 +173,7 @@ def test_device_pointers_and_zero_budget(min_case, ctx):
     s0, r0, n0 = ctx.minimize_6d(*ids, wl.dofs[:10], max_evals=0)
     assert np.all(n0 == 1)
     assert np.array_equal(s0, wl.dofs[:10])
-    assert np.array_equal(r0, ctx.energy_6d(*ids, wl.dofs[:10]))
+    assert np.array_equal(r0, evaluate_roundwise(ctx, ids, wl.dofs[:10]))
 
 
 def test_autotune_and_cache(min_case, ctx, tmp_path):

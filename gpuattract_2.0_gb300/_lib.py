@@ -46,7 +46,8 @@ class PairJobC(C.Structure):
 class TuneResultC(C.Structure):
     _fields_ = [("energy_threads", C.c_int), ("energy_blocks_per_sm", C.c_int),
                 ("minimize_threads", C.c_int), ("minimize_chunk", C.c_int),
-                ("energy_ms", C.c_float), ("minimize_ms", C.c_float), ("from_cache", C.c_int)]
+                ("energy_ms", C.c_float), ("minimize_ms", C.c_float), ("from_cache", C.c_int),
+                ("minimize_team", C.c_int)]
 
 
 class GbaError(RuntimeError):
@@ -100,6 +101,7 @@ def load() -> C.CDLL:
         "gba_kernel_time": ([P, C.POINTER(C.c_double), C.POINTER(C.c_uint64), C.c_int32], I),
         "gba_grid_octets": ([P, U32, I], I),
         "gba_autotune": ([P, U32, U32, U32, U32, P, SZ, I, C.c_char_p, C.POINTER(TuneResultC)], I),
+        "gba_set_pair_shape": ([P, U32, U32, U32, U32, C.POINTER(TuneResultC)], I),
         "gba_minimize_6d_modes": ([P, U32, U32, U32, U32, U32, P, SZ, I, P, P, P, P], I),
         "gba_minimize_6d_modes_plain": ([P, U32, U32, U32, U32, U32, P, SZ, I, SZ, P, P, P, P], I),
     }

@@ -294,6 +294,15 @@ class GbaContext:
                                           cache_path.encode() if cache_path else None, C.byref(r)))
         return {k: getattr(r, k) for k, _ in _lib.TuneResultC._fields_}
 
+    def set_pair_shape(self, rec: int, lig: int, grid: int, params: int, energy_threads: int = 256,
+                       energy_blocks_per_sm: int = 64, minimize_threads: int = 128, minimize_chunk: int = 1,
+                       minimize_team: int = 1):
+        """Sets the pair's launch shapes without timing (as gba_autotune keeps them)."""
+        r = _lib.TuneResultC(energy_threads=energy_threads, energy_blocks_per_sm=energy_blocks_per_sm,
+                             minimize_threads=minimize_threads, minimize_chunk=minimize_chunk,
+                             minimize_team=minimize_team)
+        self._check(self.lib.gba_set_pair_shape(self.h, rec, lig, grid, params, C.byref(r)))
+
     def grid_octets(self, grid: int, enable: bool = True):
         """Adds / drops the duplicated-octet copy of a grid (8x memory, same results)."""
         self._check(self.lib.gba_grid_octets(self.h, grid, int(bool(enable))))

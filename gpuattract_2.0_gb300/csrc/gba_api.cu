@@ -130,6 +130,20 @@ void Context::set_tuned(const std::string& key, const TuneParams& p) {
 	tune[key] = p;
 }
 
+void Context::set_pair_tuned(const std::string& kind, const PairKey& key, const TuneParams& p) {
+	std::lock_guard<std::mutex> g(tune_mu);
+	pair_tune[{kind, key}] = p;
+}
+
+TuneParams Context::pair_tuned(const std::string& kind, const PairKey& key) const {
+	{
+		std::lock_guard<std::mutex> g(tune_mu);
+		auto it = pair_tune.find({kind, key});
+		if (it != pair_tune.end()) return it->second;
+	}
+	return tuned(kind, 0);
+}
+
 TuneParams Context::tuned(const std::string& kind, size_t) const {
 	std::lock_guard<std::mutex> g(tune_mu);
 	auto it = tune.find(kind);
@@ -145,7 +159,10 @@ Context::~Context() {
 		cudaEventDestroy(e.second);
 	}
 	if (capture_stream) cudaStreamDestroy(capture_stream);
+	for (cudaStream_t st : group_streams) cudaStreamDestroy(st);
+	for (cudaEvent_t ev : group_events) cudaEventDestroy(ev);
 	if (pinned_status) cudaFreeHost(pinned_status);
+	if (pinned_group_status) cudaFreeHost(pinned_group_status);
 	for (void* p : pinned_buf)
 		if (p) cudaFreeHost(p);
 	/* frees still in flight complete before the pool's memory is released */
@@ -566,7 +583,8 @@ int gba_energy_6d(gba_ctx* ctx, gba_id rec, gba_id lig, gba_id grid, gba_id para
 	if (!din)
 		check_cuda(cudaMemcpyAsync((void*)L.dofs, dofs, n * sizeof(gba_dof6d), cudaMemcpyHostToDevice, s),
 				"gba_energy_6d: H2D");
-	ctx->run_rigid(L, s);
+	const TuneParams shape = ctx->pair_tuned("energy", PairKey{rec, lig, grid, params});
+	ctx->run_rigid(L, s, &shape);
 	if (!dout)
 		check_cuda(cudaMemcpyAsync(out, L.out, n * sizeof(gba_result6d), cudaMemcpyDeviceToHost, s),
 				"gba_energy_6d: D2H");
@@ -744,12 +762,12 @@ void Context::run_modes(ModesLaunch& L, cudaStream_t s) {
 	check_cuda(launch_modes_energy(L, (int)blocks, threads, s), "modes energy launch");
 }
 
-void Context::run_rigid(RigidLaunch& L, cudaStream_t s) {
+void Context::run_rigid(RigidLaunch& L, cudaStream_t s, const TuneParams* shape) {
 	StreamScratch scratch(scratch_pool);
 	L.order = pose_order(L.dofs, 6, L.n, L.m.grid.outer, s, scratch);
 	L.next = (unsigned long long*)scratch.get(sizeof(unsigned long long), s);
 	check_cuda(cudaMemsetAsync(L.next, 0, sizeof(unsigned long long), s), "rigid energy: pose counter");
-	const TuneParams tp = tuned("energy", L.n);
+	const TuneParams tp = shape ? *shape : tuned("energy", L.n);
 	const int threads = tp.threads;
 	const int warps_per_block = threads / 32;
 	const int bps = std::min(tp.blocks_per_sm, rigid_blocks_per_sm(threads, L.census != nullptr, L.bound4 && !L.census,

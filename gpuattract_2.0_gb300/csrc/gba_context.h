@@ -4,6 +4,7 @@
 #ifndef GBA_CONTEXT_H_
 #define GBA_CONTEXT_H_
 
+#include <array>
 #include <map>
 #include <memory>
 #include <set>
@@ -144,10 +145,16 @@ struct TuneParams {
 	int threads = 128;
 	int blocks_per_sm = 64;   /* capped by occupancy */
 	int chunk = 1;
-	/* minimizer: warps per pose (1 = one warp per pose, 2..8 = the team
-	 * kernel), 0 = chosen from the job size */
+	/* minimizer: warps per pose (1 = one warp per pose, 2..7 = the team
+	 * kernel), 0 = chosen from the job size; a tuned team applies to jobs of
+	 * at most team_poses poses (the size it was timed on), larger ones
+	 * choose their own */
 	int team = 0;
+	size_t team_poses = 0;
 };
+
+/* Ids of one receptor-ligand pair's data: (receptor, ligand, grid, parameter table). */
+using PairKey = std::array<gba_id, 4>;
 
 /* Signature of a captured minimizer pipeline. */
 struct GraphKey {
@@ -198,9 +205,14 @@ struct Context {
 	std::map<GraphKey, cudaGraphExec_t> graphs;
 	cudaStream_t capture_stream = nullptr;
 	uint32_t deadline_ms = 0;
-	mutable std::mutex tune_mu;    /* guards tune (gba_autotune writes it while calls read it) */
+	mutable std::mutex tune_mu;    /* guards tune and pair_tune (gba_autotune writes them while calls read them) */
 	std::map<std::string, TuneParams> tune;
+	/* per pair: the shapes gba_autotune chose for it ("energy", "minimize") */
+	std::map<std::pair<std::string, PairKey>, TuneParams> pair_tune;
 	void set_tuned(const std::string& key, const TuneParams& p);
+	void set_pair_tuned(const std::string& kind, const PairKey& key, const TuneParams& p);
+	/* the pair's tuned shape, else the context-wide one */
+	TuneParams pair_tuned(const std::string& kind, const PairKey& key) const;
 
 	/* device address of the static scratch of gba_energy_6d_noalloc,
 	 * resolved by the first such call on this context */
@@ -221,7 +233,22 @@ struct Context {
 	TuneParams tuned(const std::string& kind, size_t n) const;
 	/* lig_rounds: the largest ligand of the launch in 64-bead rounds (caps
 	 * the team size) */
-	void run_minimize(MinLaunch& L, cudaStream_t s, int32_t* status_out, uint32_t lig_rounds);
+	void run_minimize(MinLaunch& L, cudaStream_t s, int32_t* status_out, uint32_t lig_rounds,
+			const TuneParams& tp);
+	/* One launch per group of pairs, each with its own shape, concurrently
+	 * in one captured graph: group g takes the queue slots
+	 * [off[g], off[g] + n[g]) of L.order. */
+	struct MinGroup {
+		size_t off, n;
+		TuneParams tp;
+	};
+	void run_minimize_groups(MinLaunch& L, const std::vector<MinGroup>& groups, cudaStream_t s,
+			int32_t* status_out);
+	static constexpr size_t kMaxGroups = 16;
+	std::vector<cudaStream_t> group_streams;
+	std::vector<cudaEvent_t> group_events;
+	DevBuffer group_aux;          /* per group: cursor, status; then the earliest warp start */
+	int32_t* pinned_group_status = nullptr;
 	/* warps per pose the minimizer uses for n poses */
 	int minimize_team(const TuneParams& tp, size_t n, uint32_t lig_rounds) const;
 	int team_override = 0;         /* gba_set_minimize_team; 0 = tuned or automatic */
@@ -235,7 +262,8 @@ struct Context {
 	const uint32_t* typed_list(GridItem& g, gba_id rec_id, const ProteinItem& rec, bool may_allocate);
 	void validate_pair(const ProteinItem& rec, const ProteinItem& lig, const GridItem& g,
 			const ParamsItem& p);
-	void run_rigid(RigidLaunch& L, cudaStream_t s);
+	/* tp: launch shape (nullptr: the context-wide "energy" shape) */
+	void run_rigid(RigidLaunch& L, cudaStream_t s, const TuneParams* tp = nullptr);
 	ModesLaunch modes_launch(gba_id rec, gba_id lig, gba_id grid_rec, gba_id grid_lig, gba_id params);
 	void run_modes(ModesLaunch& L, cudaStream_t s);
 

@@ -33,6 +33,7 @@
  * GBA_ERR_TIMEOUT in a device status word.
  */
 #include <algorithm>
+#include <atomic>
 #include <vector>
 
 #include "gba_context.h"
@@ -286,13 +287,31 @@ cudaError_t launch_minimize_rigid_team(const MinLaunch& L, int blocks, int team,
 	return cudaGetLastError();
 }
 
+/* Dynamic shared memory above the 48 KB default (eight one-warp staging
+ * areas with their VA13 states need ~53 KB): allowed once per device, before
+ * any occupancy query or capture. */
+static void allow_minimize_smem() {
+	static std::atomic<int> done[64];
+	int dev = 0;
+	cudaGetDevice(&dev);
+	if (dev >= 0 && dev < 64 && done[dev].load()) return;
+	cudaFuncSetAttribute(minimize_rigid_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+			(int)min_stage_bytes(256));
+	cudaFuncSetAttribute(minimize_rigid_team_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+			(int)team_smem_bytes(kMaxTeam));
+	cudaGetLastError();
+	if (dev >= 0 && dev < 64) done[dev].store(1);
+}
+
 int minimize_blocks_per_sm(int threads) {
+	allow_minimize_smem();
 	int nb = 0;
 	cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, minimize_rigid_kernel, threads, min_stage_bytes(threads));
 	return nb > 0 ? nb : 1;
 }
 
 int minimize_team_blocks_per_sm(int team) {
+	allow_minimize_smem();
 	int nb = 0;
 	cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, minimize_rigid_team_kernel, 32 * (team + 1),
 			team_smem_bytes(team));

@@ -44,7 +44,8 @@ struct Placement {
 }  // namespace
 
 int Context::minimize_team(const TuneParams& tp, size_t n, uint32_t lig_rounds) const {
-	int team = team_override ? team_override : tp.team;
+	int team = team_override;
+	if (team == 0 && tp.team > 0 && n <= tp.team_poses) team = tp.team;
 	if (team == 0) {
 		/* fewer poses than the one-warp kernel has resident warps: give each
 		 * pose as many warps as fill them, up to its ligand's rounds */
@@ -55,25 +56,43 @@ int Context::minimize_team(const TuneParams& tp, size_t n, uint32_t lig_rounds) 
 	return std::max(1, std::min(team, kMaxTeam));
 }
 
-/* Runs the persistent minimizer over `total` poses whose inputs/outputs live
- * in device memory; captured in a CUDA graph cached by launch signature. */
-void Context::run_minimize(MinLaunch& L, cudaStream_t s, int32_t* status_out, uint32_t lig_rounds) {
-	TuneParams tp = tuned("minimize", L.n);
-	const int team = minimize_team(tp, L.n, lig_rounds);
-	int threads = tp.threads;
+namespace {
+
+/* Launch shape of one persistent minimizer launch over n poses. */
+struct MinShape {
+	int team, threads, chunk;
 	size_t blocks;
+};
+
+MinShape min_shape(const Context& ctx, const TuneParams& tp, size_t n, int team) {
+	MinShape m{team, tp.threads, 1, 1};
 	if (team > 1) {
 		/* team evaluation warps plus a control warp; two poses per block */
-		threads = 32 * (team + 1);
-		blocks = std::min<size_t>((L.n + 1) / 2, (size_t)num_sms * minimize_team_blocks_per_sm(team));
-		L.chunk = 1;
+		m.threads = 32 * (team + 1);
+		m.blocks = std::min<size_t>((n + 1) / 2, (size_t)ctx.num_sms * minimize_team_blocks_per_sm(team));
 	} else {
-		const int bps = std::min(tp.blocks_per_sm, minimize_blocks_per_sm(threads));
-		const size_t warps = (size_t)num_sms * bps * (threads / 32);
-		blocks = (size_t)num_sms * bps;
-		if (warps > L.n) blocks = std::max<size_t>(1, (L.n * 32 + threads - 1) / threads);
-		L.chunk = tp.chunk;
+		const int bps = std::min(tp.blocks_per_sm, minimize_blocks_per_sm(m.threads));
+		const size_t warps = (size_t)ctx.num_sms * bps * (m.threads / 32);
+		m.blocks = (size_t)ctx.num_sms * bps;
+		if (warps > n) m.blocks = std::max<size_t>(1, (n * 32 + m.threads - 1) / m.threads);
+		m.chunk = tp.chunk;
 	}
+	return m;
+}
+
+cudaError_t launch_shape(const MinLaunch& L, const MinShape& m, cudaStream_t s) {
+	return m.team > 1 ? launch_minimize_rigid_team(L, (int)m.blocks, m.team, s)
+	                  : launch_minimize_rigid(L, (int)m.blocks, m.threads, s);
+}
+
+}  // namespace
+
+/* Runs the persistent minimizer over `total` poses whose inputs/outputs live
+ * in device memory; captured in a CUDA graph cached by launch signature. */
+void Context::run_minimize(MinLaunch& L, cudaStream_t s, int32_t* status_out, uint32_t lig_rounds,
+		const TuneParams& tp) {
+	const MinShape m = min_shape(*this, tp, L.n, minimize_team(tp, L.n, lig_rounds));
+	L.chunk = m.chunk;
 	if (!aux.ptr) {
 		aux.alloc(64);
 		note_allocation();
@@ -95,9 +114,9 @@ void Context::run_minimize(MinLaunch& L, cudaStream_t s, int32_t* status_out, ui
 	key.g = (uintptr_t)L.done_ns;
 	key.n = L.n;
 	key.p0 = L.max_evals;
-	key.p1 = (int)blocks;
-	key.p2 = threads;
-	key.p3 = L.chunk | team << 16;
+	key.p1 = (int)m.blocks;
+	key.p2 = m.threads;
+	key.p3 = m.chunk | m.team << 16;
 	key.deadline = L.budget_ns;
 	cudaGraphExec_t exec = nullptr;
 	auto it = graphs.find(key);
@@ -109,11 +128,14 @@ void Context::run_minimize(MinLaunch& L, cudaStream_t s, int32_t* status_out, ui
 		check_cuda(cudaStreamBeginCapture(capture_stream, cudaStreamCaptureModeThreadLocal), "capture");
 		cudaMemsetAsync(aux.ptr, 0, 16, capture_stream);
 		cudaMemsetAsync((char*)aux.ptr + 32, 0xff, 8, capture_stream);
-		cudaError_t le = team > 1 ? launch_minimize_rigid_team(L, (int)blocks, team, capture_stream)
-		                          : launch_minimize_rigid(L, (int)blocks, threads, capture_stream);
+		cudaError_t le = launch_shape(L, m, capture_stream);
 		cudaMemcpyAsync(pinned_status, L.status, sizeof(int32_t), cudaMemcpyDeviceToHost, capture_stream);
 		cudaGraph_t g = nullptr;
 		cudaError_t ce = cudaStreamEndCapture(capture_stream, &g);
+		if (le != cudaSuccess || ce != cudaSuccess) {
+			if (g) cudaGraphDestroy(g);
+			cudaGetLastError();      /* leave no stale error for the next call */
+		}
 		check_cuda(le, "minimize launch (capture)");
 		check_cuda(ce, "end capture");
 		cudaError_t ie = cudaGraphInstantiate(&exec, g, 0);
@@ -125,6 +147,104 @@ void Context::run_minimize(MinLaunch& L, cudaStream_t s, int32_t* status_out, ui
 	check_cuda(cudaGraphLaunch(exec, s), "graph launch");
 	check_cuda(cudaStreamSynchronize(s), "minimize sync");
 	if (status_out) *status_out = *pinned_status;
+}
+
+/* Concurrent launches, one per group: forked from and joined back into the
+ * capture stream, so the whole batch is still one graph launch. */
+void Context::run_minimize_groups(MinLaunch& L, const std::vector<MinGroup>& groups, cudaStream_t s,
+		int32_t* status_out) {
+	const size_t G = groups.size();
+	if (G > kMaxGroups) throw ApiError(GBA_ERR_INVALID_ARGUMENT, "batch minimize: too many launch shapes");
+	if (!group_aux.ptr) {
+		group_aux.alloc(64 * (kMaxGroups + 1));
+		note_allocation();
+		check_cuda(cudaMallocHost((void**)&pinned_group_status, sizeof(int32_t) * kMaxGroups), "cudaMallocHost");
+	}
+	while (group_streams.size() < G) {
+		cudaStream_t st = nullptr;
+		check_cuda(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking), "stream");
+		group_streams.push_back(st);
+	}
+	while (group_events.size() < G + 1) {
+		cudaEvent_t ev = nullptr;
+		check_cuda(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "event");
+		group_events.push_back(ev);
+	}
+	std::vector<MinLaunch> Ls(G, L);
+	std::vector<MinShape> shapes(G);
+	uint64_t h = 1469598103934665603ull;
+	for (size_t g = 0; g < G; ++g) {
+		shapes[g] = min_shape(*this, groups[g].tp, groups[g].n, 1);
+		MinLaunch& Lg = Ls[g];
+		Lg.order = L.order + groups[g].off;
+		Lg.n = groups[g].n;
+		Lg.chunk = shapes[g].chunk;
+		Lg.counter = (unsigned long long*)((char*)group_aux.ptr + 64 * g);
+		Lg.status = (int*)((char*)group_aux.ptr + 64 * g + 8);
+		Lg.t0 = (unsigned long long*)((char*)group_aux.ptr + 64 * kMaxGroups);
+		for (uint64_t v : {(uint64_t)groups[g].off, (uint64_t)groups[g].n, (uint64_t)shapes[g].blocks,
+				(uint64_t)shapes[g].threads, (uint64_t)shapes[g].chunk})
+			h = (h ^ v) * 1099511628211ull;
+	}
+	L.t0 = Ls[0].t0;
+	GraphKey key{};
+	key.kind = 3;
+	key.a = (uintptr_t)L.models;
+	key.b = (uintptr_t)L.pair_of ^ ((uintptr_t)L.order << 1);
+	key.c = (uintptr_t)L.start;
+	key.d = (uintptr_t)L.out_state;
+	key.e = (uintptr_t)L.out_result;
+	key.f = (uintptr_t)L.out_nevals;
+	key.g = (uintptr_t)L.done_ns;
+	key.n = L.n;
+	key.p0 = L.max_evals;
+	key.p1 = (int)G;
+	key.p2 = (int)(h & 0x7fffffff);
+	key.p3 = (int)(h >> 33);
+	key.deadline = L.budget_ns;
+	cudaGraphExec_t exec = nullptr;
+	auto it = graphs.find(key);
+	if (it != graphs.end()) {
+		exec = it->second;
+	} else {
+		if (!capture_stream)
+			check_cuda(cudaStreamCreateWithFlags(&capture_stream, cudaStreamNonBlocking), "stream");
+		check_cuda(cudaStreamBeginCapture(capture_stream, cudaStreamCaptureModeThreadLocal), "capture");
+		cudaError_t le = cudaSuccess;
+		cudaMemsetAsync(group_aux.ptr, 0, 64 * G, capture_stream);
+		cudaMemsetAsync((char*)group_aux.ptr + 64 * kMaxGroups, 0xff, 8, capture_stream);
+		cudaEventRecord(group_events[G], capture_stream);
+		for (size_t g = 0; g < G; ++g) {
+			cudaStreamWaitEvent(group_streams[g], group_events[G], 0);
+			cudaError_t e = launch_shape(Ls[g], shapes[g], group_streams[g]);
+			if (le == cudaSuccess) le = e;
+			cudaEventRecord(group_events[g], group_streams[g]);
+			cudaStreamWaitEvent(capture_stream, group_events[g], 0);
+		}
+		for (size_t g = 0; g < G; ++g)
+			cudaMemcpyAsync(pinned_group_status + g, Ls[g].status, sizeof(int32_t), cudaMemcpyDeviceToHost,
+					capture_stream);
+		cudaGraph_t gr = nullptr;
+		cudaError_t ce = cudaStreamEndCapture(capture_stream, &gr);
+		if (le != cudaSuccess || ce != cudaSuccess) {
+			if (gr) cudaGraphDestroy(gr);
+			cudaGetLastError();      /* leave no stale error for the next call */
+		}
+		check_cuda(le, "minimize launch (capture)");
+		check_cuda(ce, "end capture");
+		cudaError_t ie = cudaGraphInstantiate(&exec, gr, 0);
+		cudaGraphDestroy(gr);
+		check_cuda(ie, "graph instantiate");
+		if (graphs.size() > 64) clear_graphs();
+		graphs.emplace(key, exec);
+	}
+	check_cuda(cudaGraphLaunch(exec, s), "graph launch");
+	check_cuda(cudaStreamSynchronize(s), "minimize sync");
+	if (status_out) {
+		*status_out = GBA_OK;
+		for (size_t g = 0; g < G; ++g)
+			if (pinned_group_status[g] != GBA_OK) *status_out = pinned_group_status[g];
+	}
 }
 
 void Context::clear_graphs() {
@@ -261,26 +381,78 @@ int gba_batch_minimize_6d(gba_ctx* ctx, const gba_pair_job* jobs, size_t njobs, 
 		for (size_t j = 0; j < njobs; ++j)
 			if (jobs[j].n) copy_in((void*)(L.start + G.offset[j]), jobs[j].start, jobs[j].n * sizeof(gba_dof6d), s);
 	}
+	/* launch shapes: the pairs' tuned shapes (gba_autotune), else the
+	 * context's; a job small enough for teams runs as one team launch */
+	uint32_t lig_rounds = 1;
+	for (const RigidModel& m : G.models) lig_rounds = std::max(lig_rounds, (m.lig.n + 63) / 64);
+	std::vector<TuneParams> tps(njobs);
+	for (size_t j = 0; j < njobs; ++j)
+		tps[j] = ctx->pair_tuned("minimize", PairKey{jobs[j].rec, jobs[j].lig, jobs[j].grid, jobs[j].params});
+	const TuneParams base_tp = njobs == 1 ? tps[0] : ctx->tuned("minimize", n);
+	const bool team_launch = ctx->minimize_team(base_tp, n, lig_rounds) > 1;
+	/* group index of each job: one per distinct (threads, chunk) */
+	std::vector<uint32_t> group_of(njobs, 0);
+	std::vector<TuneParams> group_tp{tps[0]};
+	if (!team_launch)
+		for (size_t j = 1; j < njobs; ++j) {
+			size_t g = 0;
+			while (g < group_tp.size() &&
+					!(group_tp[g].threads == tps[j].threads && group_tp[g].chunk == tps[j].chunk &&
+					  group_tp[g].blocks_per_sm == tps[j].blocks_per_sm))
+				++g;
+			if (g == group_tp.size()) group_tp.push_back(tps[j]);
+			group_of[j] = (uint32_t)g;
+		}
+	const bool grouped = group_tp.size() > 1;
+	if (group_tp.size() > Context::kMaxGroups) throw ApiError(GBA_ERR_INVALID_ARGUMENT,
+			"gba_batch_minimize_6d: more than " + std::to_string(Context::kMaxGroups) + " tuned launch shapes");
 	/* visit poses grouped by pair, in Morton order of the start translation;
 	 * pairs with larger ligands (more work per evaluation) first, so that the
-	 * poses still running when the queue empties are cheap ones */
+	 * poses still running when the queue empties are cheap ones; with
+	 * several launch shapes the pairs of one shape come together */
 	const uint32_t* pair_rank = nullptr;
+	std::vector<uint32_t> by_cost(njobs), rank(njobs);
+	for (size_t j = 0; j < njobs; ++j) by_cost[j] = (uint32_t)j;
+	std::stable_sort(by_cost.begin(), by_cost.end(), [&](uint32_t a, uint32_t b) {
+		if (group_of[a] != group_of[b]) return group_of[a] < group_of[b];
+		return G.models[a].lig.n > G.models[b].lig.n;
+	});
+	for (size_t r = 0; r < njobs; ++r) rank[by_cost[r]] = (uint32_t)r;
 	if (njobs > 1) {
-		std::vector<uint32_t> by_cost(njobs), rank(njobs);
-		for (size_t j = 0; j < njobs; ++j) by_cost[j] = (uint32_t)j;
-		std::stable_sort(by_cost.begin(), by_cost.end(), [&](uint32_t a, uint32_t b) {
-			return G.models[a].lig.n > G.models[b].lig.n;
-		});
-		for (size_t r = 0; r < njobs; ++r) rank[by_cost[r]] = (uint32_t)r;
 		ctx->rank_buf.upload(rank.data(), njobs * sizeof(uint32_t));
 		pair_rank = (const uint32_t*)ctx->rank_buf.ptr;
 	}
 	L.order = ctx->pose_order_persistent(L.start, 6, n, G.models[0].grid.outer, L.models, L.pair_of,
 			pair_rank, njobs, s);
 	int32_t status = GBA_OK;
-	uint32_t lig_rounds = 1;
-	for (const RigidModel& m : G.models) lig_rounds = std::max(lig_rounds, (m.lig.n + 63) / 64);
-	ctx->run_minimize(L, s, &status, lig_rounds);
+	if (!grouped) {
+		ctx->run_minimize(L, s, &status, lig_rounds, base_tp);
+	} else {
+		if (!L.order) {
+			/* no spatial order (small batch or switched off): pairs of one
+			 * shape together, each pair's poses in submission order */
+			std::vector<uint32_t> ord;
+			ord.reserve(n);
+			for (uint32_t j : by_cost)
+				for (size_t k = 0; k < jobs[j].n; ++k) ord.push_back((uint32_t)(G.offset[j] + k));
+			DevBuffer& b = ctx->order_buf;
+			if (b.bytes < n * sizeof(uint32_t)) b.alloc(n * sizeof(uint32_t) + 256);
+			check_cuda(cudaMemcpyAsync(b.ptr, ord.data(), n * sizeof(uint32_t), cudaMemcpyHostToDevice, s),
+					"batch minimize: order");
+			L.order = (const uint32_t*)b.ptr;
+		}
+		std::vector<Context::MinGroup> groups(group_tp.size());
+		size_t off = 0;
+		for (size_t g = 0; g < group_tp.size(); ++g) {
+			groups[g].off = off;
+			groups[g].tp = group_tp[g];
+			groups[g].n = 0;
+			for (size_t j = 0; j < njobs; ++j)
+				if (group_of[j] == g) groups[g].n += jobs[j].n;
+			off += groups[g].n;
+		}
+		ctx->run_minimize_groups(L, groups, s, &status);
+	}
 	if (!single_dev) {
 		for (size_t j = 0; j < njobs; ++j) {
 			const size_t o = G.offset[j], m = jobs[j].n;
@@ -358,6 +530,7 @@ int gba_minimize_6d_plain(gba_ctx* ctx, gba_id rec, gba_id lig, gba_id grid, gba
 	ctx->bind();
 	cudaStream_t s = (cudaStream_t)stream;
 	RigidLaunch L = ctx->rigid_launch(rec, lig, grid, params);
+	const TuneParams shape = ctx->pair_tuned("energy", PairKey{rec, lig, grid, params});
 	Lock lk(ctx->stage_mu);
 	/* pinned request/result buffers, like the server's HostPinnedAllocator
 	 * buffers (src/service/GPUEnergyService.tpp:22-23) */
@@ -397,7 +570,7 @@ int gba_minimize_6d_plain(gba_ctx* ctx, gba_id rec, gba_id lig, gba_id grid, gba
 			L.n = m;
 			L.census = nullptr;
 			L.roundwise = 1;      /* the device minimizer's summation order */
-			ctx->run_rigid(L, s);
+			ctx->run_rigid(L, s, &shape);
 			check_cuda(cudaMemcpyAsync(hout + b, dout + b, m * sizeof(gba_result6d), cudaMemcpyDeviceToHost, s),
 					"plain: D2H");
 		}

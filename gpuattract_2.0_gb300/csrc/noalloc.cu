@@ -80,7 +80,7 @@ extern "C" int gba_energy_6d_noalloc(gba_ctx* ctx, gba_id rec, gba_id lig, gba_i
 						kNoAllocScratchBytes - kCounterBytes, s)
 				: nullptr;
 		/* launch shape as gba_energy_6d chooses it */
-		const TuneParams tp = ctx->tuned("energy", n);
+		const TuneParams tp = ctx->pair_tuned("energy", PairKey{rec, lig, grid, params});
 		const int threads = tp.threads;
 		const int bps = std::min(tp.blocks_per_sm, rigid_blocks_per_sm(threads, false, L.bound4 != 0));
 		size_t blocks = std::min<size_t>((n + threads / 32 - 1) / (threads / 32), (size_t)ctx->num_sms * bps);

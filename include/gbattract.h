@@ -372,17 +372,34 @@ typedef struct {
 	int minimize_threads, minimize_chunk;       /* persistent minimizer: block size, poses per grab */
 	float energy_ms, minimize_ms;               /* best sample times (-1 when taken from the cache) */
 	int from_cache;                             /* bit 0: energy, bit 1: minimize read from cache */
+	int minimize_team;                          /* warps per pose (1, or a team of 2..7 plus a control warp) */
 } gba_tune_result;
 
 /* Times candidate launch shapes of the scoring kernel (threads per block x
  * resident blocks per SM) and of the persistent minimizer (threads per block x
- * poses per queue grab) on `sample` poses of this pair and keeps the fastest
- * for the context.  With cache_path, results are read from / appended to that
- * text file (keyed by device, SM count and pair size).  No reference
- * counterpart: the reference fixes 128-thread blocks (src/service/GPUEnergyService6D.tpp:440-441). */
+ * poses per queue grab with one warp per pose, or teams of 2..7 warps per pose
+ * -- poses per CTA below one) on `sample` poses of this pair and keeps the
+ * fastest for this pair: gba_energy_6d, gba_minimize_6d and the plain form
+ * launch the pair with them, and a gba_batch_minimize_6d batch launches the
+ * pairs of each tuned shape as one persistent kernel, the groups running
+ * concurrently in one CUDA graph.  A tuned team applies to minimizations of
+ * at most the sample's size.  With cache_path, results are read from /
+ * appended to that text file (keyed by device, SM count and pair size).  No
+ * reference counterpart: the reference fixes 128-thread blocks
+ * (src/service/GPUEnergyService6D.tpp:440-441) and sizes its reduction block
+ * from the device (src/service/GPUEnergyService6D.tpp:184-198). */
 int gba_autotune(gba_ctx* ctx, gba_id rec, gba_id lig, gba_id grid, gba_id params,
 		const gba_dof6d* sample, size_t n, int max_evals, const char* cache_path,
 		gba_tune_result* out);
+
+/* Sets the pair's launch shapes directly (for instance ones an earlier
+ * gba_autotune reported), as gba_autotune would keep them; energy_ms,
+ * minimize_ms and from_cache are ignored.  energy_threads 32..256 (multiple
+ * of 32), energy_blocks_per_sm >= 1; minimize_team 1..7; with team 1,
+ * minimize_threads 32..256 (multiple of 32) and minimize_chunk 1..16.  A team
+ * set here applies to minimizations of any size.  No reference counterpart. */
+int gba_set_pair_shape(gba_ctx* ctx, gba_id rec, gba_id lig, gba_id grid, gba_id params,
+		const gba_tune_result* shape);
 
 /* ---- grid builder --------------------------------------------------------- */
 

@@ -183,14 +183,51 @@ def test_autotune_and_cache(min_case, ctx, tmp_path):
     before = ctx.minimize_6d(*ids, wl.dofs[:64], max_evals=40)
     cache = str(tmp_path / "tune.txt")
     r1 = ctx.autotune(*ids, wl.dofs, max_evals=20, cache_path=cache)
-    assert r1["energy_threads"] in (128, 256) and r1["minimize_threads"] in (64, 128, 256)
-    assert r1["minimize_chunk"] in (1, 2, 4) and r1["from_cache"] == 0 and r1["energy_ms"] > 0
+    assert r1["energy_threads"] in (128, 256) and 1 <= r1["minimize_team"] <= 2   # a 70-bead ligand: 2 rounds
+    if r1["minimize_team"] == 1:
+        assert r1["minimize_threads"] in (64, 128, 256) and r1["minimize_chunk"] in (1, 2, 4)
+    else:
+        assert r1["minimize_threads"] == 32 * (r1["minimize_team"] + 1)
+    assert r1["from_cache"] == 0 and r1["energy_ms"] > 0
     r2 = ctx.autotune(*ids, wl.dofs, max_evals=20, cache_path=cache)
     assert r2["from_cache"] == 3
-    assert r2["energy_threads"] == r1["energy_threads"] and r2["minimize_chunk"] == r1["minimize_chunk"]
+    for k in ("energy_threads", "energy_blocks_per_sm", "minimize_threads", "minimize_chunk", "minimize_team"):
+        assert r2[k] == r1[k], k
     after = ctx.minimize_6d(*ids, wl.dofs[:64], max_evals=40)
     for a, b in zip(before, after):
         assert np.array_equal(a, b)
+
+
+def test_per_pair_shapes_and_grouped_batch(pkg, oracle, ctx):
+    """Shapes kept per pair: a batch whose pairs carry different shapes runs
+    one persistent launch per shape, concurrently in one graph, and gives the
+    same results as each pair minimized alone and as the batch with one shape
+    for all (launch shapes never change a result)."""
+    pairs = []
+    for k, (nr, nl, npz) in enumerate([(140, 60, 70), (180, 90, 45), (120, 50, 90)]):
+        wl = pkg.synth.make_pair(4, nr, nl, npz, (18.0, 28.0), seed=2300 + k)
+        rec, lig, par = ctx.upload_protein(wl.rec), ctx.upload_protein(wl.lig), ctx.upload_params(wl.params)
+        gid = ctx.build_grid(rec, par, pkg.GridOptions())
+        pairs.append((rec, lig, gid, par, wl.dofs))
+    ctx.set_minimize_team(1)          # one warp per pose: the grouped path
+    try:
+        plain_batch = ctx.batch_minimize_6d(pairs, max_evals=40)
+        ctx.set_pair_shape(*pairs[0][:4], minimize_threads=64, minimize_chunk=1)
+        ctx.set_pair_shape(*pairs[1][:4], minimize_threads=256, minimize_chunk=4)
+        ctx.set_pair_shape(*pairs[2][:4], minimize_threads=64, minimize_chunk=1)
+        grouped = ctx.batch_minimize_6d(pairs, max_evals=40)
+        alone = [ctx.minimize_6d(*p[:4], p[4], max_evals=40) for p in pairs]
+    finally:
+        ctx.set_minimize_team(0)
+    for g, b, a in zip(grouped, plain_batch, alone):
+        for x, y, z in zip(g, b, a):
+            assert np.array_equal(x, y) and np.array_equal(x, z)
+    from gbattract import GbaError
+    with pytest.raises(GbaError):
+        ctx.set_pair_shape(*pairs[0][:4], minimize_team=9)
+    for p in pairs:
+        for i in p[:4]:
+            ctx.release(i)
 
 
 def test_wall_time_budget_raises_timeout(pkg, ctx, min_case):

@@ -14,8 +14,18 @@ metric = energy+gradient evaluations per second.
            index, receptor xyz, type, charge) / energy-kernel time (CUDA events
            the library records around the launch), against the measured HBM
            copy bandwidth
+           (plus the same achieved figure against an L2 copy bandwidth measured
+           in the run: "roofline.l2")
   cpu_baseline  the CPU oracle (a C++ port of the reference CPU path) on a
            bounded sample of the same workload, all host threads
+  parity   the timed workload's own GPU results on the first 20,000 poses
+           against the oracle (FP32, FP64, correctly rounded sin/cos)
+  minimization   config 0 (1,000 poses, maxFunEval 100): device-resident
+           batched form vs the plain per-step forms and the CPU oracle
+  batched_uneven config 4 (64 pairs, 1.65 M poses, maxFunEval 500): one
+           persistent work-queue launch in a CUDA graph with default and with
+           autotuned per-pair shapes, vs the plain per-step form on every 8th
+           pair, per-pair completion times, oracle agreement on a sample
 
 `--impl reference` times the reference's CPU implementation of the path (the
 port, or the reference build in oracle/_ref where it exists) on the same
@@ -108,17 +118,16 @@ class ClockSampler:
 
 
 def traffic_per_pose(variant: str):
-    """DRAM bytes per pose of the energy kernel, from the committed ncu summary
-    of the same kernel and variant (a line 'traffic-per-pose: <variant> <bytes>'
-    under profiles/), or None.  The capture is of a smaller pose count; the
-    traffic is scaled by the poses processed."""
-    import re
-    for f in sorted((ROOT / "profiles").glob("*.md")):
-        for line in f.read_text().splitlines():
-            m = re.match(r"traffic-per-pose: (\S+) ([0-9.]+)", line.strip("` "))
-            if m and m.group(1) == variant:
-                return float(m.group(2)), f.name
-    return None, None
+    """DRAM bytes per pose of the energy kernel from profiles/traffic.json
+    (one ncu capture of the same kernel and variant, with its command), or
+    None for another variant."""
+    p = ROOT / "profiles" / "traffic.json"
+    if not p.exists():
+        return None, None
+    d = json.loads(p.read_text()).get("rigid_energy_kernel", {})
+    if d.get("variant") != variant:
+        return None, None
+    return float(d["dram_bytes_per_pose"]), "profiles/traffic.json (" + d.get("summary", "") + ")"
 
 
 def measured_peaks():
@@ -174,6 +183,60 @@ def cpu_rate(pkg, wl, grid_host, seconds: float, nthreads: int):
     po.energy_6d(wl.rec, wl.lig, grid_host, wl.params, sample, nthreads=nthreads)
     dt = time.perf_counter() - t0
     return n / dt, n, dt
+
+
+def timed_result_parity(wl, grid_host, got, m: int, nthreads: int):
+    """Parity of the timed workload's own GPU results (the first m poses)
+    against the CPU oracle on the same, device-built grid: the scaled error
+    bound of the tests, the share of poses within 1e-4 of the bare relative
+    error, the errors of the GPU and of the FP32 oracle against the FP64
+    oracle; and the same against the oracle with correctly rounded sin/cos
+    (the C library's sinf/cosf misround a few percent of angles by one ulp)."""
+    from oracle import pyoracle as po
+    d = wl.dofs[:m]
+    ref, st = po.energy_6d(wl.rec, wl.lig, grid_host, wl.params, d, stats=True, nthreads=nthreads)
+    ref64 = po.energy_6d_f64(wl.rec, wl.lig, grid_host, wl.params, d, nthreads=nthreads)
+    with po.exact_sincos():
+        ref_x = po.energy_6d(wl.rec, wl.lig, grid_host, wl.params, d, nthreads=nthreads)
+    exact = po.libm_sincos_rounds_exactly(d[:, 3:6])
+    out = po.parity_stats(got[:m], ref, st, ref64)
+    out["poses_with_correctly_rounded_libm_sincos"] = int(exact.sum())
+    out["max_scaled_err_those_poses"] = po.parity_stats(got[:m][exact], ref[exact], st[exact])["max_scaled_err"]
+    vs_x = po.parity_stats(got[:m], ref_x, st)
+    out["vs_correctly_rounded_sincos_oracle"] = {k: vs_x[k] for k in ("max_scaled_err", "frac_within_1e-4_bare")}
+    out["bound"] = "per pose |d| / max(|ref|, 0.05 S) <= 1e-4 for E, force and torque, S = sum of |terms|"
+    return out
+
+
+def measured_l2_peak(device: str = "cuda"):
+    """Copy bandwidth of a 2 x 48 MB working set, resident in the 129 MB L2:
+    50 back-to-back copies replayed from a CUDA graph (no launch gaps), best
+    of 5 replays (read + write bytes)."""
+    import torch
+    n = 48 * 1024 * 1024 // 4
+    a = torch.ones(n, dtype=torch.float32, device=device)
+    b = torch.empty_like(a)
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(s):
+        for _ in range(3):
+            b.copy_(a)
+    torch.cuda.current_stream().wait_stream(s)
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        for _ in range(50):
+            b.copy_(a)
+    g.replay()
+    torch.cuda.synchronize()
+    best = float("inf")
+    for _ in range(5):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        g.replay()
+        e1.record()
+        torch.cuda.synchronize()
+        best = min(best, e0.elapsed_time(e1) / 1000.0)
+    return 50 * 2 * a.numel() * 4 / best / 1e9
 
 
 def run_reference(args):
@@ -367,10 +430,16 @@ def bench_adjoint(ctx, pkg, n_poses: int):
             "timing": "wall clock of 3 synchronised torch.autograd calls"}
 
 
-def bench_batched_uneven(ctx, pkg, pose_scale: float, steps: int):
+def bench_batched_uneven(ctx, pkg, pose_scale: float, steps: int, plain_every: int = 1, tune: bool = True,
+                         with_cpu: bool = True, nthreads: int = 1):
     """Config 4: 64 pairs of uneven sizes, each with its own grids, minimized in
-    one persistent launch vs the plain per-step form run pair after pair."""
+    one persistent launch (default launch shapes, then the shapes gba_autotune
+    picks per pair) against the plain per-step form run pair after pair on
+    every plain_every-th pair (the same pairs timed batched), with per-pair
+    completion times and, on a seeded sample, the symmetric agreement of the
+    minimized energies with the CPU oracle's VA13."""
     import torch
+    t_start = time.perf_counter()
     pairs = pkg.synth.make_batch(n_pairs=64, pose_scale=pose_scale)
     jobs, handles = [], []
     for wl in pairs:
@@ -378,6 +447,7 @@ def bench_batched_uneven(ctx, pkg, pose_scale: float, steps: int):
         grid = ctx.build_grid(rec, par, pkg.GridOptions())
         handles += [grid, lig, rec, par]
         jobs.append((rec, lig, grid, par, wl.dofs))
+    torch.cuda.synchronize()
     total = sum(len(j[4]) for j in jobs)
     # octet copies (cooperative lookups) for the pairs with the most poses while
     # more than 80 GB of device memory stays free: all 64 would need ~320 GB
@@ -387,60 +457,96 @@ def bench_batched_uneven(ctx, pkg, pose_scale: float, steps: int):
             break
         ctx.grid_octets(jobs[k][2], True)
         octet_pairs += 1
+    setup_s = time.perf_counter() - t_start
+    log(f"config 4: {total} poses, grids and octets {setup_s:.1f} s")
     ctx.batch_minimize_6d([(*j[:4], j[4][:8]) for j in jobs], max_evals=5)      # warm-up
-    t0 = time.perf_counter()
-    got = ctx.batch_minimize_6d(jobs, max_evals=steps)
-    dt_dev = time.perf_counter() - t0
-    # per-pair time to completion inside the persistent launch
-    import ctypes as C
-    from gbattract import _lib
-    cj = (_lib.PairJobC * len(jobs))()
-    keep, done = [], []
-    for k, (rec, lig, grid, par, dofs) in enumerate(jobs):
-        st = np.empty((len(dofs), 6), np.float32)
-        rs = np.empty((len(dofs), 7), np.float32)
-        dn = np.zeros(len(dofs), np.uint64)
-        keep += [dofs, st, rs]
-        done.append(dn)
-        j = cj[k]
-        j.rec, j.lig, j.grid, j.params = rec, lig, grid, par
-        j.start, j.n = dofs.ctypes.data, len(dofs)
-        j.out_state, j.out_result, j.out_nevals, j.out_done_ns = st.ctypes.data, rs.ctypes.data, None, dn.ctypes.data
-    _lib.check(ctx.h, ctx.lib.gba_batch_minimize_6d(ctx.h, cj, len(jobs), steps, None))
-    pair_done_ms = np.array([dn.max() / 1e6 for dn in done])
+
+    def timed(js):
+        t0 = time.perf_counter()
+        got = ctx.batch_minimize_6d(js, max_evals=steps, done_ns=True)
+        dt = time.perf_counter() - t0
+        return got, dt, np.array([g[3].max() / 1e6 for g in got])
+
+    got_u, dt_u, ms_u = timed(jobs)
+    log(f"config 4: batched, default shapes {dt_u:.1f} s")
+    res = {"workload": f"config 4: 64 pairs, receptor 300-3000 / ligand 100-1500 beads, {total} poses "
+                       f"(pose counts x{pose_scale}), maxFunEval {steps}; octet grids for {octet_pairs} pairs",
+           "batched_default_shapes_poses_per_s": total / dt_u,
+           "batched_default_shapes_pair_completion_ms_p50": float(np.percentile(ms_u, 50)),
+           "batched_default_shapes_pair_completion_ms_p99": float(np.percentile(ms_u, 99))}
+    got, ms = got_u, ms_u
+    if tune:
+        cache = str(Path("/tmp") / "gba_tune_cache.txt")
+        t0 = time.perf_counter()
+        shapes = [ctx.autotune(*j[:4], j[4][:512], max_evals=20, cache_path=cache) for j in jobs]
+        tune_s = time.perf_counter() - t0
+        got, dt_t, ms = timed(jobs)
+        log(f"config 4: autotune {tune_s:.1f} s, batched with tuned shapes {dt_t:.1f} s")
+        kinds = {}
+        for sh in shapes:
+            k = f"{sh['minimize_threads']}x{sh['minimize_chunk']}"
+            kinds[k] = kinds.get(k, 0) + 1
+        res.update({"autotune_s": tune_s, "tuned_minimize_shapes": kinds,
+                    "tuned_energy_threads": sorted({sh["energy_threads"] for sh in shapes}),
+                    "batched_tuned_poses_per_s": total / dt_t,
+                    "tuned_gain": dt_u / dt_t,
+                    "tuned_equals_default": bool(all(np.array_equal(a[1], b[1]) for a, b in zip(got, got_u)))})
+    res["batched_device_poses_per_s"] = total / (dt_t if tune else dt_u)
+    res["batched_pair_completion_ms_p50"] = float(np.percentile(ms, 50))
+    res["batched_pair_completion_ms_p99"] = float(np.percentile(ms, 99))
+    # the plain per-step form (one launch per evaluation round, host VA13),
+    # pair after pair, against the batched form on the same pairs
+    sub = jobs[::plain_every]
+    n_sub = sum(len(j[4]) for j in sub)
+    got_sub, dt_dev_sub, _ = timed(sub) if plain_every > 1 else (got, total / res["batched_device_poses_per_s"], None)
     t0 = time.perf_counter()
     plain_done, plain = [], []
-    for (rec, lig, grid, par, dofs) in jobs:
+    for (rec, lig, grid, par, dofs) in sub:
         plain.append(ctx.minimize_6d_plain(rec, lig, grid, par, dofs, max_evals=steps))
         plain_done.append(1e3 * (time.perf_counter() - t0))
     dt_plain = time.perf_counter() - t0
-    same = all(np.array_equal(a[1], b[1]) for a, b in zip(got, plain))
-    # the reference's execution model (100-pose work items, pair after pair)
-    # on the first 8 pairs, against the batched device form on the same pairs
-    few = jobs[:8]
+    log(f"config 4: plain per-step form on {len(sub)} pairs {dt_plain:.1f} s")
+    pd = np.array(plain_done)
+    res.update({"plain_pairs": len(sub), "plain_poses": n_sub,
+                "plain_per_step_poses_per_s": n_sub / dt_plain,
+                "batched_same_pairs_poses_per_s": n_sub / dt_dev_sub,
+                "speedup": dt_plain / dt_dev_sub,
+                "device_equals_plain": bool(all(np.array_equal(a[1], b[1]) for a, b in zip(got_sub, plain))),
+                "plain_pair_completion_ms_p50": float(np.percentile(pd, 50)),
+                "plain_pair_completion_ms_p99": float(np.percentile(pd, 99))})
+    # the reference's own execution model: 100-pose work items, one launch
+    # each, per evaluation round (src/server/Server.h:39), on two pairs
+    few = [jobs[k] for k in (len(jobs) // 3, 2 * len(jobs) // 3)]
     n_few = sum(len(j[4]) for j in few)
+    got_few, dt_dev_few, _ = timed(few)
     t0 = time.perf_counter()
-    got_few = ctx.batch_minimize_6d(few, max_evals=steps)
-    dt_dev_few = time.perf_counter() - t0
-    t0 = time.perf_counter()
-    items = [ctx.minimize_6d_plain(rec, lig, grid, par, dofs, max_evals=steps, item_size=100)
-             for (rec, lig, grid, par, dofs) in few]
+    items = [ctx.minimize_6d_plain(*j[:4], j[4], max_evals=steps, item_size=100) for j in few]
     dt_items = time.perf_counter() - t0
-    same_items = all(np.array_equal(a[1], b[1]) for a, b in zip(got_few, items))
+    log(f"config 4: 100-pose work items on 2 pairs {dt_items:.1f} s")
+    res.update({"items_pairs": len(few), "items_poses": n_few,
+                "plain_100_pose_items_poses_per_s": n_few / dt_items,
+                "batched_items_pairs_poses_per_s": n_few / dt_dev_few,
+                "speedup_vs_plain_100_pose_items": dt_items / dt_dev_few,
+                "items_equal_device": bool(all(np.array_equal(a[1], b[1]) for a, b in zip(got_few, items)))})
+    if with_cpu:
+        # agreement with the CPU oracle's VA13: 32 seeded poses of every 8th pair
+        from oracle import pyoracle as po
+        rng = np.random.default_rng(404)
+        dev, ref = [], []
+        for k in range(0, len(jobs), 8):
+            rec, lig, grid, par, dofs = jobs[k]
+            idx = np.sort(rng.choice(len(dofs), 32, replace=False))
+            gh = ctx.download_grid(grid)
+            _, r_cpu, _ = po.minimize_6d(pairs[k].rec, pairs[k].lig, gh, pairs[k].params, dofs[idx], steps,
+                                         nthreads=nthreads)
+            dev.append(got[k][1][idx])
+            ref.append(r_cpu)
+        res["oracle_sample"] = {"poses": int(sum(len(r) for r in ref)), "pairs": len(ref),
+                                **po.minimization_stats(np.concatenate(dev), np.concatenate(ref))}
     for i in handles:
         ctx.release(i)
-    pd = np.array(plain_done)
-    return {"workload": f"config 4: 64 pairs, receptor 300-3000 / ligand 100-1500 beads, {total} poses "
-                        f"(pose counts x{pose_scale}), maxFunEval {steps}; octet grids for {octet_pairs} pairs",
-            "batched_device_poses_per_s": total / dt_dev, "plain_per_step_poses_per_s": total / dt_plain,
-            "speedup": dt_plain / dt_dev, "device_equals_plain": bool(same),
-            "first_8_pairs_poses": n_few, "first_8_pairs_device_poses_per_s": n_few / dt_dev_few,
-            "first_8_pairs_plain_100_pose_items_poses_per_s": n_few / dt_items,
-            "speedup_vs_plain_100_pose_items": dt_items / dt_dev_few, "items_equal_device": bool(same_items),
-            "batched_pair_completion_ms_p50": float(np.percentile(pair_done_ms, 50)),
-            "batched_pair_completion_ms_p99": float(np.percentile(pair_done_ms, 99)),
-            "plain_pair_completion_ms_p50": float(np.percentile(pd, 50)),
-            "plain_pair_completion_ms_p99": float(np.percentile(pd, 99))}
+    res["section_s"] = time.perf_counter() - t_start
+    return res
 
 
 def run_modes_only(args):
@@ -459,9 +565,8 @@ def run_modes_only(args):
 
 
 def run_section_only(args):
-    """`--suite adjoint` / `--suite minimize`: the config-3 or the config-0
-    section alone (profiling captures of the pairwise kernels or of the
-    device minimizer)."""
+    """`--suite adjoint` / `--suite minimize` / `--suite batched`: the config-3,
+    config-0 or config-4 section alone (profiling captures, section timings)."""
     import torch
     torch.cuda.set_device(0)
     import __graft_entry__
@@ -470,6 +575,9 @@ def run_section_only(args):
     ctx = GbaContext(0)
     if args.suite == "adjoint":
         res = bench_adjoint(ctx, pkg, n_poses=args.poses or 10_000)
+    elif args.suite == "batched":
+        res = bench_batched_uneven(ctx, pkg, pose_scale=args.batch_scale, steps=500, plain_every=args.plain_every,
+                                   with_cpu=not args.no_cpu, nthreads=os.cpu_count() or 1)
     else:
         res = bench_minimization(ctx, pkg, nthreads=os.cpu_count() or 1, with_cpu=not args.no_cpu)
     ctx.close()
@@ -487,11 +595,13 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--ref-sample", type=int, default=2000)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--no-min", action="store_true", help="skip the minimization report")
-    ap.add_argument("--suite", default="default", choices=["default", "full", "modes", "adjoint", "minimize"],
-                    help="full: also configs 2 (modes), 3 (adjoint), 4 (batched uneven pairs); "
-                         "modes: config 2 alone; adjoint: config 3 alone; minimize: config 0's "
-                         "minimization alone")
+    ap.add_argument("--no-min", action="store_true", help="skip the minimization reports (configs 0 and 4)")
+    ap.add_argument("--no-batch", action="store_true", help="skip the config-4 report")
+    ap.add_argument("--suite", default="default",
+                    choices=["default", "full", "modes", "adjoint", "minimize", "batched"],
+                    help="default: config 1 (timed), config 0 and config 4 minimization; full: also "
+                         "configs 2 (modes) and 3 (adjoint); modes / adjoint / minimize / batched: "
+                         "config 2, 3, 0 or 4 alone")
     ap.add_argument("--modes-poses", type=int, default=50000)
     ap.add_argument("--variant", default="order=1,octets=1",
                     help="layout / visiting-order variant timed, or 'search' to time all four "
@@ -501,8 +611,11 @@ def main():
     ap.add_argument("--kopts", type=int, default=15,
                     help="kernel options (GBA_KOPT_*: 1 computed ratio, 2 cooperative lookup, "
                          "4 four blocks per SM, 8 typed neighbour list)")
-    ap.add_argument("--batch-scale", type=float, default=0.05,
-                    help="fraction of config 4's pose counts used by --suite full")
+    ap.add_argument("--batch-scale", type=float, default=1.0,
+                    help="fraction of config 4's pose counts (1.0: the configuration as stated)")
+    ap.add_argument("--plain-every", type=int, default=8,
+                    help="config 4: the plain per-step form runs on every k-th pair (and the batched "
+                         "form again on the same pairs for the speedup)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -510,7 +623,7 @@ def main():
         return run_reference(args)
     if args.suite == "modes":
         return run_modes_only(args)
-    if args.suite in ("adjoint", "minimize"):
+    if args.suite in ("adjoint", "minimize", "batched"):
         return run_section_only(args)
 
     import torch
@@ -633,6 +746,7 @@ def main():
     ok = bool(np.array_equal(out.cpu().numpy(), ho.numpy()))
 
     cpu = None
+    parity = None
     if rank == 0 and not args.no_cpu:
         subprocess.run(["make", "-s", "-C", str(ROOT / "oracle")], check=True)
         gh = ctx.download_grid(grid)
@@ -640,16 +754,23 @@ def main():
         rate, ns, dt = cpu_rate(pkg, wl, gh, args.cpu_seconds, nthreads)
         cpu = {"value": rate, "unit": UNIT, "cores": nthreads, "kind": "port",
                "sample": f"first {ns} poses of the workload ({dt:.1f} s on {nthreads} threads)"}
+        parity = timed_result_parity(wl, gh, out.cpu().numpy(), min(ns, 20000), nthreads)
 
+    l2_peak = measured_l2_peak() if rank == 0 else None
     minim = None
     if rank == 0 and not args.no_min:
         minim = bench_minimization(ctx, pkg, os.cpu_count() or 1, with_cpu=not args.no_cpu)
+    batched = None
+    if rank == 0 and not args.no_min and not args.no_batch:
+        ctx.grid_octets(grid, False)
+        batched = bench_batched_uneven(ctx, pkg, pose_scale=args.batch_scale, steps=500,
+                                       plain_every=args.plain_every, with_cpu=not args.no_cpu,
+                                       nthreads=os.cpu_count() or 1)
     suite = {}
     if rank == 0 and args.suite == "full":
         ctx.grid_octets(grid, False)
         suite["modes"] = bench_modes(ctx, pkg, n_poses=args.modes_poses, steps=200)
         suite["adjoint"] = bench_adjoint(ctx, pkg, n_poses=10000)
-        suite["batched_uneven"] = bench_batched_uneven(ctx, pkg, pose_scale=args.batch_scale, steps=500)
 
     if rank == 0:
         line = {
@@ -667,12 +788,18 @@ def main():
                          "frac": achieved / peak, "traffic": traffic, "traffic_source": traffic_src,
                          "peak_source": peak_kind,
                          "bytes_per_launch": bytes_launch, "kernel_ms_avg": 1000.0 * kernel_avg_s,
-                         "kernel_launches_timed": kernel_launches},
+                         "kernel_launches_timed": kernel_launches,
+                         "l2": None if l2_peak is None else {
+                             "achieved": achieved, "peak": l2_peak, "frac": achieved / l2_peak,
+                             "peak_source": "measured in this run: graph of 50 copies of a 2 x 48 MB L2-resident "
+                                            "working set"}},
+            "parity": parity,
             "cpu_baseline": cpu, "clocks": clk.summary(),
             # per step: the fused energy kernel (+ the three visiting-order kernels --
             # cell counts, their prefix sum, the scatter -- when the order is on)
             "gpu_launches": args.steps * (4 if best.startswith("order=1") else 1),
             "minimization": minim,
+            "batched_uneven": batched,
             "variants_ms": variants, "variant_timed": best, "kernel_options": args.kopts,
             "suite": suite or None,
             "wall_s_timed": wall, "host_device_paths_equal": ok,

@@ -271,10 +271,19 @@ class GbaContext:
         self._check(self.lib.gba_batch_energy_6d(self.h, jobs, len(pairs), stream))
         return [o[2] for o in outs]
 
-    def batch_minimize_6d(self, pairs, max_evals: int = 500, stream=None):
-        """One persistent launch minimizing the poses of many pairs; list of (state, result, evals)."""
+    def batch_minimize_6d(self, pairs, max_evals: int = 500, stream=None, done_ns: bool = False):
+        """One persistent launch minimizing the poses of many pairs; list of (state, result, evals)
+        per pair, plus (done_ns) each pose's completion time in ns from the launch's start."""
         jobs, outs = self._jobs(pairs, with_state=True)
+        done = []
+        if done_ns:
+            for k, o in enumerate(outs):
+                d = np.zeros(o[0].shape[0], np.uint64)
+                jobs[k].out_done_ns = _lib.ptr(d)
+                done.append(d)
         self._check(self.lib.gba_batch_minimize_6d(self.h, jobs, len(pairs), int(max_evals), stream))
+        if done_ns:
+            return [(o[1], o[2], o[3], d) for o, d in zip(outs, done)]
         return [(o[1], o[2], o[3]) for o in outs]
 
     def set_minimize_team(self, warps_per_pose: int):

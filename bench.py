@@ -329,7 +329,31 @@ def bench_minimization(ctx, pkg, nthreads: int, with_cpu: bool):
     return out
 
 
-def bench_modes(ctx, pkg, n_poses: int, steps: int, minimize: bool = True):
+def modes_roofline(ctx, wl, gr, gl, n: int, launch_s: float):
+    """Algorithmic bytes of the modes kernel from the oracle's per-pose counts
+    on a 2,048-pose sample (bit-exact with the kernel's lookups and neighbour
+    walks): per evaluation 104 B DOF + 108 B result + 128 B per grid-channel
+    lookup of both passes (ligand beads in the receptor grid, receptor beads
+    in the ligand grid) + 8 B per NL voxel lookup + (24 + 12 Mr) B per list
+    entry (index, receptor xyz, type, charge and the receptor's Mr mode
+    vectors, from which the kernel re-deforms the neighbour); per-bead
+    constants count once per batch.  Against the measured HBM copy peak."""
+    from oracle import pyoracle as po
+    m = min(2048, len(wl.dofs))
+    hr, hl = ctx.download_grid(gr), ctx.download_grid(gl)
+    _, st = po.energy_6d_modes(wl.rec, wl.lig, hr, hl, wl.params, wl.dofs[:m], stats=True)
+    Mr = wl.rec.n_modes
+    look = (st["n_grid"].astype(np.float64) + st["n_grid_charged"] + st["n_rec_lookups"]).mean()
+    per = 104 + 108 + 128 * look + 8 * st["n_nl"].mean() + (24 + 12 * Mr) * st["n_nl_entries"].mean()
+    achieved = per * n / launch_s / 1e9
+    peak, kind = measured_peaks()
+    return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "peak_source": kind, "bytes_per_eval": per, "lookups_per_eval": look,
+            "nl_entries_per_eval": float(st["n_nl_entries"].mean()), "kernel_ms_avg": 1000.0 * launch_s,
+            "census_sample_poses": m}
+
+
+def bench_modes(ctx, pkg, n_poses: int, steps: int, minimize: bool = True, with_cpu: bool = True):
     """Config 2: receptor 1500 / ligand 600 beads with 5 modes each: modes
     energy+gradient evals/s, and (minimize) device vs plain minimization."""
     import torch
@@ -343,16 +367,23 @@ def bench_modes(ctx, pkg, n_poses: int, steps: int, minimize: bool = True):
     d = torch.from_numpy(wl.dofs).cuda()
     out = ctx.energy_6d_modes(*ids, d)
     torch.cuda.synchronize()
-    t0 = time.perf_counter()
+    stream = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
     for _ in range(3):
-        ctx.energy_6d_modes(*ids, d, out=out)
+        ctx.energy_6d_modes(*ids, d, out=out, stream=stream.cuda_stream)
+    e1.record(stream)
     torch.cuda.synchronize()
-    evals = 3 * len(wl.dofs) / (time.perf_counter() - t0)
+    launch_s = e0.elapsed_time(e1) / 1000.0 / 3
+    evals = len(wl.dofs) / launch_s
+    roof = None
+    if with_cpu:
+        roof = modes_roofline(ctx, wl, gr, gl, len(wl.dofs), launch_s)
     if not minimize:
         for i in (gr, gl, lig, rec, par):
             ctx.release(i)
         return {"workload": f"config 2: receptor {wl.rec.n} / ligand {wl.lig.n} beads, 5+5 modes; "
-                            f"{len(wl.dofs)} poses scored", "energy_evals_per_s": evals}
+                            f"{len(wl.dofs)} poses scored", "energy_evals_per_s": evals, "roofline": roof}
     sub = wl.dofs
     ctx.minimize_6d_modes(*ids, sub[:64], max_evals=10)
     t0 = time.perf_counter()
@@ -373,7 +404,7 @@ def bench_modes(ctx, pkg, n_poses: int, steps: int, minimize: bool = True):
     dt_items = time.perf_counter() - t0
     res = {"workload": f"config 2: receptor {wl.rec.n} / ligand {wl.lig.n} beads, 5+5 modes; "
                        f"{len(wl.dofs)} poses scored, {len(sub)} minimized (maxFunEval {steps})",
-           "energy_evals_per_s": evals, "minimize_device_poses_per_s": len(sub) / dt_dev,
+           "energy_evals_per_s": evals, "roofline": roof, "minimize_device_poses_per_s": len(sub) / dt_dev,
            "minimize_plain_poses_per_s": len(sub) / dt_plain, "speedup": dt_plain / dt_dev,
            "subset_5000_device_poses_per_s": len(few) / dt_dev_few,
            "subset_5000_plain_100_pose_items_poses_per_s": len(few) / dt_items,
@@ -382,7 +413,13 @@ def bench_modes(ctx, pkg, n_poses: int, steps: int, minimize: bool = True):
            "device_equals_plain": bool(np.array_equal(r1, r2, equal_nan=True)),
            "evals_per_pose_mean": float(n1.mean()),
            "start_E_median": float(np.median(e0)), "minimized_E_median": float(np.median(r1[:, 0])),
-           "lowered_fraction": float(np.mean(r1[:, 0] < e0))}
+           "lowered_fraction": float(np.mean(r1[:, 0] < e0)),
+           # poses whose last evaluation is the start pose again: deep clashes whose
+           # gradient is so large that VA13's line search shrinks the step below the
+           # FP32 resolution of the DOFs (the reference minimizer stalls the same way)
+           "ended_at_start_energy_fraction": float(np.mean(r1[:, 0] == e0)),
+           "final_nan_fraction": float(np.mean(~np.isfinite(r1[:, 0]))),
+           "start_no_contact_fraction": float(np.mean(e0 == 0))}
     for i in (gr, gl, lig, rec, par):
         ctx.release(i)
     return res
@@ -414,7 +451,7 @@ def bench_adjoint(ctx, pkg, n_poses: int):
         with torch.no_grad():
             PairwiseEnergy.apply(d, ql, qr, r0, eps, sysm)
 
-    rates = {}
+    rates, secs = {}, {}
     for name, f in (("fwd_bwd_evals_per_s", fb), ("fwd_evals_per_s", fwd)):
         f()
         torch.cuda.synchronize()
@@ -422,11 +459,31 @@ def bench_adjoint(ctx, pkg, n_poses: int):
         for _ in range(3):
             f()
         torch.cuda.synchronize()
-        rates[name] = 3 * len(wl.dofs) / (time.perf_counter() - t0)
+        secs[name] = (time.perf_counter() - t0) / 3
+        rates[name] = len(wl.dofs) / secs[name]
+    # algorithmic bytes: the pairwise kernels walk the same neighbour lists as
+    # the grid kernel's census counts them; per pose 24 B DOF + 8 B per NL voxel
+    # + 28 B per list entry (index, receptor xyz and charge, type, pairwise
+    # charge), + 4 B energy (forward) or 4 B upstream gradient + 24 B dE/dDOF
+    # (backward); per-bead and per-type-pair constants count once per call
+    cen, _ = ctx.census_6d(rec, lig, grid, par, d.detach())
+    cen = cen.cpu().numpy().astype(np.float64)
+    walk = 8 * cen[:, 2].mean() + 28 * cen[:, 3].mean()
+    peak, kind = measured_peaks()
+    n = len(wl.dofs)
+    t_f = secs["fwd_evals_per_s"]
+    t_b = max(secs["fwd_bwd_evals_per_s"] - t_f, 1e-9)
+    roof = {"forward": {"achieved": (28 + walk) * n / t_f / 1e9}, "backward": {"achieved": (52 + walk) * n / t_b / 1e9}}
+    for v in roof.values():
+        v.update({"peak": peak, "unit": "GB/s", "frac": v["achieved"] / peak, "peak_source": kind})
+    roof["bytes_per_eval_walk"] = walk
+    roof["note"] = ("wall time of synchronised calls; backward = forward+backward minus forward; "
+                    "the pair arithmetic (LJ, Coulomb and their parameter derivatives) bounds these "
+                    "kernels before memory does")
     for i in (grid, lig, rec, par):
         ctx.release(i)
     return {"workload": f"config 3: receptor {wl.rec.n} / ligand {wl.lig.n} beads, {len(wl.dofs)} poses, "
-                        "10 A pairwise cutoff", **rates,
+                        "10 A pairwise cutoff", **rates, "roofline": roof,
             "timing": "wall clock of 3 synchronised torch.autograd calls"}
 
 
@@ -558,7 +615,8 @@ def run_modes_only(args):
     pkg = __graft_entry__.load_package()
     from gbattract.context import GbaContext
     ctx = GbaContext(0)
-    res = bench_modes(ctx, pkg, n_poses=args.modes_poses, steps=200, minimize=not args.no_min)
+    res = bench_modes(ctx, pkg, n_poses=args.modes_poses, steps=200, minimize=not args.no_min,
+                      with_cpu=not args.no_cpu)
     ctx.close()
     print(json.dumps({"suite": {"modes": res}}))
     return 0
@@ -769,7 +827,7 @@ def main():
     suite = {}
     if rank == 0 and args.suite == "full":
         ctx.grid_octets(grid, False)
-        suite["modes"] = bench_modes(ctx, pkg, n_poses=args.modes_poses, steps=200)
+        suite["modes"] = bench_modes(ctx, pkg, n_poses=args.modes_poses, steps=200, with_cpu=not args.no_cpu)
         suite["adjoint"] = bench_adjoint(ctx, pkg, n_poses=10000)
 
     if rank == 0:

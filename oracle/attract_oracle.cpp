@@ -433,13 +433,14 @@ void nl_pot_force(const Sys<R>& S, const orc_protein* rec, const orc_protein* li
 /* reducePotForce, src/model/reduction.h:40-75 (sum + ForceLim clamp) */
 template <typename R>
 void reduce_pot_force(const R* fx, const R* fy, const R* fz, const R* E, unsigned n,
-		R& oE, R& ox, R& oy, R& oz) {
+		R& oE, R& ox, R& oy, R& oz, orc_pose_stats* stats = nullptr) {
 	R e = 0, x = 0, y = 0, z = 0;
 	for (unsigned i = 0; i < n; ++i) { e += E[i]; x += fx[i]; y += fy[i]; z += fz[i]; }
 	for (unsigned i = 0; i < 3; ++i) {
 		R magn2 = x * x + y * y + z * z;
 		if (magn2 > (R)1.0e18f) {
 			x = (R)((W)x * 0.01); y = (R)((W)y * 0.01); z = (R)((W)z * 0.01);
+			if (stats) stats->n_force_lim++;
 		}
 	}
 	oE = e; ox = x; oy = y; oz = z;
@@ -515,7 +516,7 @@ void eval_rigid(const Sys<R>& S, const orc_protein* rec, const orc_protein* lig,
 				nullptr, nullptr, nullptr, st);
 	}
 	reduce_pot_force<R>(w.fx.data(), w.fy.data(), w.fz.data(), w.E.data(), n, out7[0], out7[1],
-			out7[2], out7[3]);
+			out7[2], out7[3], stats);
 	reduce_torque<R>(lig, w.fx.data(), w.fy.data(), w.fz.data(), ang[0], ang[1], ang[2], out7 + 4, st);
 }
 
@@ -607,8 +608,11 @@ void eval_modes(const Sys<R>& SR, const Sys<R>& SL, const orc_protein* rec, cons
 			w.lty.data(), w.ltz.data());
 	/* receptor beads in the ligand grid, forces rotated back by R(ang)
 	 * (rotate_forces with invertedDOF.ang.inv(), src/model/transform_modes.h:146-166) */
+	orc_pose_stats rec_st;
+	std::memset(&rec_st, 0, sizeof(rec_st));
 	pot_force<R>(SL, rec, w.rtx.data(), w.rty.data(), w.rtz.data(), w.rfx.data(), w.rfy.data(),
-			w.rfz.data(), w.rE.data(), Stats{nullptr});
+			w.rfz.data(), w.rE.data(), Stats{stats ? &rec_st : nullptr});
+	if (stats) stats->n_rec_lookups = rec_st.n_grid + rec_st.n_grid_charged;
 	for (unsigned i = 0; i < rec->n; ++i) {
 		R ox, oy, oz;
 		matvec<R>(R0, w.rfx[i], w.rfy[i], w.rfz[i], ox, oy, oz);

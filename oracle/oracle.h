@@ -53,10 +53,13 @@ typedef struct {
 	uint32_t n_nl;          /* beads that looked up an NL voxel */
 	uint32_t n_nl_entries;  /* sum of numEl over those voxels */
 	uint32_t n_pairs;       /* neighbour pairs inside the plateau */
-	uint32_t pad;
+	uint32_t n_rec_lookups; /* modes: channel lookups of the receptor beads in the
+	                           ligand grid (type + charge channels; 0 when rigid) */
 	double abs_E;           /* sum of |energy term| over every term */
 	double abs_F;           /* sum of |force term| (Euclidean) over every term */
 	double abs_T;           /* sum over beads of |x_i| * |f_i| */
+	uint32_t n_force_lim;   /* times the ForceLim clamp scaled the force sum (0..3) */
+	uint32_t pad;
 } orc_pose_stats;
 
 /* Rigid energy+gradient, FP32 exactly as CPUEnergyService6D<float>.

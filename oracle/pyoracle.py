@@ -60,8 +60,9 @@ class OrcGridOpts(C.Structure):
 
 
 STATS_DTYPE = np.dtype([("n_grid", "<u4"), ("n_grid_charged", "<u4"), ("n_nl", "<u4"),
-                        ("n_nl_entries", "<u4"), ("n_pairs", "<u4"), ("pad", "<u4"),
-                        ("abs_E", "<f8"), ("abs_F", "<f8"), ("abs_T", "<f8")])
+                        ("n_nl_entries", "<u4"), ("n_pairs", "<u4"), ("n_rec_lookups", "<u4"),
+                        ("abs_E", "<f8"), ("abs_F", "<f8"), ("abs_T", "<f8"), ("n_force_lim", "<u4"),
+                        ("pad", "<u4")])
 
 _orc = None
 _ref = None

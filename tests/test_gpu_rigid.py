@@ -277,3 +277,26 @@ def test_kernel_options_keep_parity(small_case, oracle, ctx, flags):
     for e in pose_errors(got, ref, st):
         assert float(e.max()) <= RTOL
     assert np.array_equal(cen, cen0)
+
+
+def test_force_lim_clamp_matches_oracle(small_case, oracle, ctx):
+    """Deep clashes (translations scaled to 30 %) push the force sum past
+    |F|^2 = 1e18, where reducePotForce scales it by 0.01 up to three times
+    (src/model/reduction.h:62-72).  The oracle counts the clamps: poses
+    clamped once, twice and three times occur, and the GPU results equal the
+    oracle's within the parity bound on all of them (an unclamped force would
+    be 100x off)."""
+    wl, grid = small_case
+    dofs = wl.dofs.copy()
+    dofs[:, :3] *= 0.3
+    with oracle.exact_sincos():
+        ref, st = oracle.energy_6d(wl.rec, wl.lig, grid, wl.params, dofs, stats=True)
+    counts = np.bincount(st["n_force_lim"], minlength=4)
+    assert counts[1] > 0 and counts[2] > 0 and counts[3] > 0, counts
+    got = ctx.energy_6d(*upload(ctx, wl.rec, wl.lig, grid, wl.params), dofs)
+    assert np.isfinite(got).all()
+    for e in pose_errors(got, ref, st):
+        assert float(e.max()) <= RTOL
+    clamped = st["n_force_lim"] > 0
+    F = np.linalg.norm(got[clamped, 1:4].astype(np.float64), axis=1)
+    assert np.all((F ** 2 <= 1.0e18 * 1.0001) | (st["n_force_lim"][clamped] == 3))

@@ -38,6 +38,8 @@
  * deformed receptor and mode buffers (src/model/neighborlist_modes.cu:81-83,
  * src/model/transform_modes.cu:154, src/model/reduction_modes.cu:68-69).
  */
+#include <algorithm>
+
 #include "rigid_pose.cuh"
 #include "va13.cuh"
 
@@ -114,55 +116,69 @@ __device__ __forceinline__ void project_component(const ModeStage<MM>& S, uint32
 
 }  // namespace
 
-/* One pose of the modes energy.  Lane k (k < 26) brings the k-th float of the
- * DOF_6D_Modes record; returns on lane k (k < 27) the k-th float of the
- * Result_6D_Modes record.  Only the model fields of L are read.  MM >= the
- * receptor's and the ligand's mode counts. */
+/* The pose frame of both passes: the rotation, its "inverted" counterpart
+ * R(-ang) and t' = R^T (-t) (invertDOF, src/model/transform_modes.h:27-41),
+ * and the translation. */
+struct ModesFrame {
+	PoseRot R;
+	float Ri[9];
+	float ip[3];
+	float t[3];
+};
+
+/* Lane k (k < 26) brings the k-th float of the DOF_6D_Modes record; every
+ * lane gets the frame and the amplitudes. */
 template <int MM>
-__device__ __forceinline__ float eval_pose_modes(const ModesLaunch& L, const float dv, const int lane,
-		WarpStage& W, ModeStage<MM>& MS) {
-	const uint32_t Mr = L.rec.n_modes, Ml = L.lig.n_modes;
-	const float tx = __shfl_sync(GBA_FULL_MASK, dv, 0);
-	const float ty = __shfl_sync(GBA_FULL_MASK, dv, 1);
-	const float tz = __shfl_sync(GBA_FULL_MASK, dv, 2);
+__device__ __forceinline__ ModesFrame modes_frame(const float dv, const int lane, float ampR[MM], float ampL[MM]) {
+	ModesFrame F;
+	F.t[0] = __shfl_sync(GBA_FULL_MASK, dv, 0);
+	F.t[1] = __shfl_sync(GBA_FULL_MASK, dv, 1);
+	F.t[2] = __shfl_sync(GBA_FULL_MASK, dv, 2);
 	const float a0 = __shfl_sync(GBA_FULL_MASK, dv, 3);
 	const float a1 = __shfl_sync(GBA_FULL_MASK, dv, 4);
 	const float a2 = __shfl_sync(GBA_FULL_MASK, dv, 5);
-	float ampR[MM], ampL[MM];
 #pragma unroll
 	for (int m = 0; m < MM; ++m) {
 		ampR[m] = __shfl_sync(GBA_FULL_MASK, dv, 6 + m);
 		ampL[m] = __shfl_sync(GBA_FULL_MASK, dv, 16 + m);
 	}
-	const PoseRot R = pose_rotation(a0, a1, a2, lane);
+	F.R = pose_rotation(a0, a1, a2, lane);
+	const PoseRot& R = F.R;
 	/* R(-ang): same sin/cos with the sines negated (exact sign flips) */
-	float Ri[9];
 	{
 		const float cphi = R.cphi, sphi = -R.sphi, cssi = R.cssi, sssi = -R.sssi;
 		const float crot = R.crot, srot = -R.srot;
 		const float cSSI_cPHI = fmul(cssi, cphi), cSSI_sPHI = fmul(cssi, sphi);
 		const float sSSI_cPHI = fmul(sssi, cphi), sSSI_sPHI = fmul(sssi, sphi);
-		Ri[0] = fadd(fmul(crot, cSSI_cPHI), fmul(srot, sphi));
-		Ri[1] = fsub(fmul(srot, cSSI_cPHI), fmul(crot, sphi));
-		Ri[2] = sSSI_cPHI;
-		Ri[3] = fsub(fmul(crot, cSSI_sPHI), fmul(srot, cphi));
-		Ri[4] = fadd(fmul(srot, cSSI_sPHI), fmul(crot, cphi));
-		Ri[5] = sSSI_sPHI;
-		Ri[6] = fmul(-crot, sssi);
-		Ri[7] = fmul(-srot, sssi);
-		Ri[8] = cssi;
+		F.Ri[0] = fadd(fmul(crot, cSSI_cPHI), fmul(srot, sphi));
+		F.Ri[1] = fsub(fmul(srot, cSSI_cPHI), fmul(crot, sphi));
+		F.Ri[2] = sSSI_cPHI;
+		F.Ri[3] = fsub(fmul(crot, cSSI_sPHI), fmul(srot, cphi));
+		F.Ri[4] = fadd(fmul(srot, cSSI_sPHI), fmul(crot, cphi));
+		F.Ri[5] = sSSI_sPHI;
+		F.Ri[6] = fmul(-crot, sssi);
+		F.Ri[7] = fmul(-srot, sssi);
+		F.Ri[8] = cssi;
 	}
 	/* t' = R^T * (-t), RotMat * Vec3 on the transposed matrix */
-	const float ipx = fadd(fadd(fmul(R.m[0], -tx), fmul(R.m[3], -ty)), fmul(R.m[6], -tz));
-	const float ipy = fadd(fadd(fmul(R.m[1], -tx), fmul(R.m[4], -ty)), fmul(R.m[7], -tz));
-	const float ipz = fadd(fadd(fmul(R.m[2], -tx), fmul(R.m[5], -ty)), fmul(R.m[8], -tz));
+	const float tx = F.t[0], ty = F.t[1], tz = F.t[2];
+	F.ip[0] = fadd(fadd(fmul(R.m[0], -tx), fmul(R.m[3], -ty)), fmul(R.m[6], -tz));
+	F.ip[1] = fadd(fadd(fmul(R.m[1], -tx), fmul(R.m[4], -ty)), fmul(R.m[7], -tz));
+	F.ip[2] = fadd(fadd(fmul(R.m[2], -tx), fmul(R.m[5], -ty)), fmul(R.m[8], -tz));
+	return F;
+}
+
+/* Receptor pass: the receptor beads, deformed and moved into the ligand
+ * frame, in the LIGAND grid; each force rotated back by R and projected on
+ * the receptor modes into the lane sums gR. */
+template <int MM>
+__device__ __forceinline__ void modes_rec_pass(const ModesLaunch& L, const ModesFrame& F, const float ampR[MM],
+		const int lane, WarpStage& W, ModeStage<MM>& MS, float gR[MM]) {
+	const uint32_t Mr = L.rec.n_modes;
+	const PoseRot& R = F.R;
+	const float* Ri = F.Ri;
+	const float ipx = F.ip[0], ipy = F.ip[1], ipz = F.ip[2];
 	const int comp = coop_component(lane);
-
-	float gR[MM], gL[MM];
-#pragma unroll
-	for (int m = 0; m < MM; ++m) { gR[m] = 0.f; gL[m] = 0.f; }
-
-	/* ---- receptor beads in the ligand grid ---- */
 	for (uint32_t j0 = 0; j0 < L.rec.n; j0 += kBeadsPerRound) {
 		uint32_t nlk[2];
 		BeadGrid bg[2];
@@ -215,9 +231,20 @@ __device__ __forceinline__ float eval_pose_modes(const ModesLaunch& L, const flo
 		__syncwarp();
 	}
 
-	/* ---- ligand beads in the receptor grid + NL against the deformed receptor ---- */
-	PoseSums S;
-	CoopSums C;
+}
+
+/* Ligand pass: the ligand beads, deformed and moved into the receptor frame,
+ * in the receptor grid, plus the NL pairs against the deformed receptor:
+ * energy, force and torque into S and C, ligand mode projections into gL,
+ * the pairs' reaction forces projected on the receptor modes into gR. */
+template <int MM>
+__device__ __forceinline__ void modes_lig_pass(const ModesLaunch& L, const ModesFrame& F, const float ampR[MM],
+		const float ampL[MM], const int lane, WarpStage& W, ModeStage<MM>& MS, PoseSums& S, CoopSums& C,
+		float gL[MM], float gR[MM]) {
+	const uint32_t Mr = L.rec.n_modes, Ml = L.lig.n_modes;
+	const PoseRot& R = F.R;
+	const float tx = F.t[0], ty = F.t[1], tz = F.t[2];
+	const int comp = coop_component(lane);
 	for (uint32_t i0 = 0; i0 < L.lig.n; i0 += kBeadsPerRound) {
 		uint32_t nlk[2], nln[2];
 		BeadGrid bg[2];
@@ -311,20 +338,31 @@ __device__ __forceinline__ float eval_pose_modes(const ModesLaunch& L, const flo
 		}
 		__syncwarp();
 	}
-	fold_coop(C, S, lane);
+}
 
+/* The Result_6D_Modes record from the ligand pass's sums and the two passes'
+ * receptor-mode gradients (warp-summed, receptor pass first): warp sums,
+ * correctModeForce (delta += 4 k delta^4, src/model/reduction_modes.h:101-115),
+ * ForceLim, TorqueMat.  Lane k (k < 27) returns float k of the record. */
+template <int MM>
+__device__ __forceinline__ float modes_epilogue(const ModesLaunch& L, const ModesFrame& F, PoseSums& S,
+		const CoopSums& C, float gL[MM], const float gR_rec[MM], float gR_nl[MM], const int lane) {
+	const uint32_t Mr = L.rec.n_modes, Ml = L.lig.n_modes;
+	fold_coop(C, S, lane);
 	float sE = warp_sum(S.E), sFx = warp_sum(S.Fx), sFy = warp_sum(S.Fy), sFz = warp_sum(S.Fz);
 	float T[9];
 #pragma unroll
 	for (int k = 0; k < 9; ++k) T[k] = warp_sum(S.T[k]);
+	float gR[MM];
 #pragma unroll
 	for (int m = 0; m < MM; ++m) {
-		if (m < (int)Mr) gR[m] = warp_sum(gR[m]);
+		gR[m] = 0.f;
+		if (m < (int)Mr) gR[m] = fadd(gR_rec[m], warp_sum(gR_nl[m]));
 		if (m < (int)Ml) gL[m] = warp_sum(gL[m]);
 	}
 	force_lim(sFx, sFy, sFz);
 	float ang[3];
-	torque_reduce(R, T, ang);
+	torque_reduce(F.R, T, ang);
 	/* correctModeForce: delta += (float)(4 k * delta^4) */
 #pragma unroll
 	for (int m = 0; m < MM; ++m) {
@@ -356,9 +394,41 @@ __device__ __forceinline__ float eval_pose_modes(const ModesLaunch& L, const flo
 	return v;
 }
 
+/* Warp sums of the receptor pass's mode gradients (every lane). */
+template <int MM>
+__device__ __forceinline__ void sum_rec_modes(uint32_t Mr, float gR[MM]) {
+#pragma unroll
+	for (int m = 0; m < MM; ++m)
+		if (m < (int)Mr) gR[m] = warp_sum(gR[m]);
+}
+
+/* One pose of the modes energy, both passes in one warp (the minimizer's
+ * form).  Lane k (k < 26) brings the k-th float of the DOF_6D_Modes record;
+ * returns on lane k (k < 27) the k-th float of the Result_6D_Modes record.
+ * Only the model fields of L are read.  MM >= the receptor's and the
+ * ligand's mode counts.  Bit for bit the result of the split scoring
+ * kernels (modes_rec_kernel then modes_lig_kernel). */
+template <int MM>
+__device__ __forceinline__ float eval_pose_modes(const ModesLaunch& L, const float dv, const int lane,
+		WarpStage& W, ModeStage<MM>& MS) {
+	float ampR[MM], ampL[MM];
+	const ModesFrame F = modes_frame<MM>(dv, lane, ampR, ampL);
+	float gRr[MM], gRn[MM], gL[MM];
+#pragma unroll
+	for (int m = 0; m < MM; ++m) { gRr[m] = 0.f; gRn[m] = 0.f; gL[m] = 0.f; }
+	modes_rec_pass<MM>(L, F, ampR, lane, W, MS, gRr);
+	sum_rec_modes<MM>(L.rec.n_modes, gRr);
+	PoseSums S;
+	CoopSums C;
+	modes_lig_pass<MM>(L, F, ampR, ampL, lane, W, MS, S, C, gL, gRn);
+	return modes_epilogue<MM>(L, F, S, C, gL, gRr, gRn, lane);
+}
+
 namespace {
 
-constexpr int kModesThreads = 256;       /* scoring kernel block */
+constexpr int kModesThreads = 256;       /* ligand-pass scoring kernel's block */
+constexpr int kModesRecThreads = 128;    /* receptor-pass kernel: block, */
+constexpr int kModesRecBlocks = 5;       /* resident blocks per SM (shared memory allows five) */
 constexpr int kModesMinThreads = 128;    /* minimizer kernel block */
 
 /* mode capacity compiled for a launch: 5 or GBA_MODES_MAX */
@@ -370,17 +440,61 @@ int mode_capacity(const ModesLaunch& L) {
 
 extern __shared__ float4 modes_dyn_smem[];
 
+/* Scoring in two kernels, so that each runs at the occupancy its own
+ * registers allow: the receptor pass (most of the grid lookups) parks its
+ * warp-summed receptor-mode gradients in the result record's modesRec slots;
+ * the ligand pass reads them back, adds its own and writes the record. */
 template <int MM>
-__global__ void __launch_bounds__(kModesThreads) modes_energy_kernel(const ModesLaunch L) {
-	__shared__ WarpStage stage[kModesThreads / 32];
+__global__ void __launch_bounds__(kModesRecThreads, kModesRecBlocks) modes_rec_kernel(const ModesLaunch L) {
+	__shared__ WarpStage stage[kModesRecThreads / 32];
 	ModeStage<MM>* ms = reinterpret_cast<ModeStage<MM>*>(modes_dyn_smem);
 	const int lane = threadIdx.x & 31;
 	const int wib = threadIdx.x >> 5;
+	const uint32_t Mr = L.rec.n_modes;
 	PoseFeed feed(L.next);
 	for (size_t p = feed.take(lane); p < L.n; p = feed.take(lane)) {
 		const float* d = reinterpret_cast<const float*>(L.dofs + p);
 		const float dv = lane < 26 ? __ldg(d + lane) : 0.f;
-		const float v = eval_pose_modes<MM>(L, dv, lane, stage[wib], ms[wib]);
+		float ampR[MM], ampL[MM];
+		const ModesFrame F = modes_frame<MM>(dv, lane, ampR, ampL);
+		float gR[MM];
+#pragma unroll
+		for (int m = 0; m < MM; ++m) gR[m] = 0.f;
+		modes_rec_pass<MM>(L, F, ampR, lane, stage[wib], ms[wib], gR);
+		sum_rec_modes<MM>(Mr, gR);
+		float v = 0.f;
+#pragma unroll
+		for (int m = 0; m < MM; ++m) v = lane == m ? gR[m] : v;
+		if ((uint32_t)lane < Mr) reinterpret_cast<float*>(L.out + p)[7 + lane] = v;
+	}
+}
+
+template <int MM>
+__global__ void __launch_bounds__(kModesThreads, 2) modes_lig_kernel(const ModesLaunch L) {
+	__shared__ WarpStage stage[kModesThreads / 32];
+	ModeStage<MM>* ms = reinterpret_cast<ModeStage<MM>*>(modes_dyn_smem);
+	const int lane = threadIdx.x & 31;
+	const int wib = threadIdx.x >> 5;
+	const uint32_t Mr = L.rec.n_modes;
+	PoseFeed feed(L.next2);
+	for (size_t p = feed.take(lane); p < L.n; p = feed.take(lane)) {
+		const float* d = reinterpret_cast<const float*>(L.dofs + p);
+		const float dv = lane < 26 ? __ldg(d + lane) : 0.f;
+		float ampR[MM], ampL[MM];
+		const ModesFrame F = modes_frame<MM>(dv, lane, ampR, ampL);
+		float gRr[MM], gRn[MM], gL[MM];
+		const float* o = reinterpret_cast<const float*>(L.out + p);
+#pragma unroll
+		for (int m = 0; m < MM; ++m) {
+			gRr[m] = m < (int)Mr ? o[7 + m] : 0.f;
+			gRn[m] = 0.f;
+			gL[m] = 0.f;
+		}
+		__syncwarp();
+		PoseSums S;
+		CoopSums C;
+		modes_lig_pass<MM>(L, F, ampR, ampL, lane, stage[wib], ms[wib], S, C, gL, gRn);
+		const float v = modes_epilogue<MM>(L, F, S, C, gL, gRr, gRn, lane);
 		if (lane < 27) reinterpret_cast<float*>(L.out + p)[lane] = v;
 	}
 }
@@ -495,22 +609,29 @@ cudaError_t allow_smem(K kernel, size_t dyn) {
 	return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
 }
 
-template <int MM>
-cudaError_t launch_modes_mm(const ModesLaunch& L, int blocks, int threads, cudaStream_t s) {
-	const size_t dyn = mode_stage_bytes<MM>(threads);
-	cudaError_t e = allow_smem(modes_energy_kernel<MM>, dyn);
-	if (e != cudaSuccess) return e;
-	modes_energy_kernel<MM><<<blocks, threads, dyn, s>>>(L);
-	return cudaGetLastError();
+template <class K>
+int resident_blocks(K kernel, int threads, size_t dyn) {
+	if (allow_smem(kernel, dyn) != cudaSuccess) return 1;
+	int nb = 0;
+	cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kernel, threads, dyn);
+	return nb > 0 ? nb : 1;
 }
 
 template <int MM>
-int modes_bps_mm(int threads) {
-	const size_t dyn = mode_stage_bytes<MM>(threads);
-	if (allow_smem(modes_energy_kernel<MM>, dyn) != cudaSuccess) return 1;
-	int nb = 0;
-	cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, modes_energy_kernel<MM>, threads, dyn);
-	return nb > 0 ? nb : 1;
+cudaError_t launch_modes_mm(const ModesLaunch& L, int num_sms, cudaStream_t s) {
+	const size_t dyn_r = mode_stage_bytes<MM>(kModesRecThreads);
+	const size_t want_r = (L.n + kModesRecThreads / 32 - 1) / (kModesRecThreads / 32);
+	const size_t br = std::max<size_t>(1, std::min<size_t>(want_r,
+			(size_t)num_sms * resident_blocks(modes_rec_kernel<MM>, kModesRecThreads, dyn_r)));
+	modes_rec_kernel<MM><<<(unsigned)br, kModesRecThreads, dyn_r, s>>>(L);
+	cudaError_t e = cudaGetLastError();
+	if (e != cudaSuccess) return e;
+	const size_t dyn = mode_stage_bytes<MM>(kModesThreads);
+	const size_t want = (L.n + kModesThreads / 32 - 1) / (kModesThreads / 32);
+	const size_t bl = std::max<size_t>(1, std::min<size_t>(want,
+			(size_t)num_sms * resident_blocks(modes_lig_kernel<MM>, kModesThreads, dyn)));
+	modes_lig_kernel<MM><<<(unsigned)bl, kModesThreads, dyn, s>>>(L);
+	return cudaGetLastError();
 }
 
 template <int MM>
@@ -533,14 +654,9 @@ int min_bps_mm(int threads) {
 
 }  // namespace
 
-cudaError_t launch_modes_energy(const ModesLaunch& L, int blocks, int threads, cudaStream_t s) {
-	if (threads != kModesThreads) return cudaErrorInvalidValue;
-	return mode_capacity(L) == 5 ? launch_modes_mm<5>(L, blocks, threads, s)
-	                             : launch_modes_mm<GBA_MODES_MAX>(L, blocks, threads, s);
-}
-
-int modes_blocks_per_sm(int threads, const ModesLaunch& L) {
-	return mode_capacity(L) == 5 ? modes_bps_mm<5>(threads) : modes_bps_mm<GBA_MODES_MAX>(threads);
+cudaError_t launch_modes_energy(const ModesLaunch& L, int num_sms, cudaStream_t s) {
+	return mode_capacity(L) == 5 ? launch_modes_mm<5>(L, num_sms, s)
+	                             : launch_modes_mm<GBA_MODES_MAX>(L, num_sms, s);
 }
 
 cudaError_t launch_minimize_modes(const ModesMinLaunch& M, int blocks, int threads, cudaStream_t s) {

@@ -753,13 +753,10 @@ ModesLaunch Context::modes_launch(gba_id rec, gba_id lig, gba_id grid_rec, gba_i
 
 void Context::run_modes(ModesLaunch& L, cudaStream_t s) {
 	StreamScratch scratch(scratch_pool);
-	L.next = (unsigned long long*)scratch.get(sizeof(unsigned long long), s);
-	check_cuda(cudaMemsetAsync(L.next, 0, sizeof(unsigned long long), s), "modes energy: pose counter");
-	const int threads = 256;
-	int bps = modes_blocks_per_sm(threads, L);
-	size_t want = (L.n + threads / 32 - 1) / (threads / 32);
-	size_t blocks = std::max<size_t>(1, std::min<size_t>(want, (size_t)num_sms * bps));
-	check_cuda(launch_modes_energy(L, (int)blocks, threads, s), "modes energy launch");
+	L.next = (unsigned long long*)scratch.get(2 * sizeof(unsigned long long), s);
+	L.next2 = L.next + 1;
+	check_cuda(cudaMemsetAsync(L.next, 0, 2 * sizeof(unsigned long long), s), "modes energy: pose counters");
+	check_cuda(launch_modes_energy(L, num_sms, s), "modes energy launch");
 }
 
 void Context::run_rigid(RigidLaunch& L, cudaStream_t s, const TuneParams* shape) {

@@ -177,12 +177,13 @@ struct ModesLaunch {
 	const gba_dof6d_modes* dofs;
 	gba_result6d_modes* out;
 	size_t n;
-	unsigned long long* next; /* pose counter, zero at launch (PoseFeed); nullptr: fixed stride */
+	unsigned long long* next; /* pose counters, zero at launch (PoseFeed): receptor pass, */
+	unsigned long long* next2;/* ligand pass; nullptr: fixed stride */
 };
 
-cudaError_t launch_modes_energy(const ModesLaunch& L, int blocks, int threads, cudaStream_t s);
-/* resident blocks of the scoring kernel compiled for L's mode counts */
-int modes_blocks_per_sm(int threads, const ModesLaunch& L);
+/* the two scoring kernels (receptor pass, then ligand pass), each grid sized
+ * to its own occupancy on num_sms SMs */
+cudaError_t launch_modes_energy(const ModesLaunch& L, int num_sms, cudaStream_t s);
 
 struct ModesMinLaunch {
 	ModesLaunch m;                  /* model fields; dofs/out/n unused */

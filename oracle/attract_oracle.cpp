@@ -210,10 +210,14 @@ struct IGrid {
 		for (int a = 0; a < 3; ++a) maxDim[a] = pos[a] + (R)(dimN[a] - 1) * dVox;
 		data = g;
 	}
-	/* outOfBounds_byPos, src/model/IntrplGrid.h:113-117 */
+	/* outOfBounds_byPos, src/model/IntrplGrid.h:113-117, as a negated inside
+	 * test: the same answer for every finite position, and a NaN position
+	 * counts as outside (the reference's comparisons count it as inside and
+	 * index the grid with it -- undefined behaviour; a minimization whose mode
+	 * amplitudes overflow reaches such positions).  The kernels test alike. */
 	bool out_of_bounds(R x, R y, R z) const {
-		return ((x < pos[0]) || (x > maxDim[0])) || ((y < pos[1]) || (y > maxDim[1])) ||
-				((z < pos[2]) || (z > maxDim[2]));
+		return !((x >= pos[0]) && (x <= maxDim[0]) && (y >= pos[1]) && (y <= maxDim[1]) &&
+				(z >= pos[2]) && (z <= maxDim[2]));
 	}
 };
 
@@ -244,9 +248,10 @@ struct NGrid {
 		list = l;
 	}
 	/* outOfBounds(x,y,z), src/model/NLGrid.h:128-133 */
+	/* NLGrid::outOfBounds, src/model/NLGrid.h:128-133, NaN-safe as above */
 	bool out_of_bounds(R x, R y, R z) const {
-		return ((x < pos[0] || x > maxDim[0]) || (y < pos[1] || y > maxDim[1]) ||
-				(z < pos[2] || z > maxDim[2]));
+		return !((x >= pos[0]) && (x <= maxDim[0]) && (y >= pos[1]) && (y <= maxDim[1]) &&
+				(z >= pos[2]) && (z <= maxDim[2]));
 	}
 	/* getIndex, src/model/NLGrid.h:100-108 */
 	void index(R x, R y, R z, int& ix, int& iy, int& iz) const {

@@ -353,11 +353,16 @@ def modes_roofline(ctx, wl, gr, gl, n: int, launch_s: float):
             "census_sample_poses": m}
 
 
-def bench_modes(ctx, pkg, n_poses: int, steps: int, minimize: bool = True, with_cpu: bool = True):
+def bench_modes(ctx, pkg, n_poses: int, steps: int, minimize: bool = True, with_cpu: bool = True,
+                small: bool = False):
     """Config 2: receptor 1500 / ligand 600 beads with 5 modes each: modes
     energy+gradient evals/s, and (minimize) device vs plain minimization."""
     import torch
-    wl = pkg.synth.make_config(2, n_poses=n_poses)
+    if small:
+        c = pkg.synth.CONFIGS[2]
+        wl = pkg.synth.make_pair(2, 700, 300, n_poses, c["shell"], steps=c["steps"], n_modes=c["modes"])
+    else:
+        wl = pkg.synth.make_config(2, n_poses=n_poses)
     rec, lig, par = ctx.upload_protein(wl.rec), ctx.upload_protein(wl.lig), ctx.upload_params(wl.params)
     gr = ctx.build_grid(rec, par, pkg.GridOptions())
     gl = ctx.build_grid(lig, par, pkg.GridOptions())
@@ -382,8 +387,9 @@ def bench_modes(ctx, pkg, n_poses: int, steps: int, minimize: bool = True, with_
     if not minimize:
         for i in (gr, gl, lig, rec, par):
             ctx.release(i)
-        return {"workload": f"config 2: receptor {wl.rec.n} / ligand {wl.lig.n} beads, 5+5 modes; "
-                            f"{len(wl.dofs)} poses scored", "energy_evals_per_s": evals, "roofline": roof}
+        return {"workload": f"config 2{' distributions' if small else ''}: receptor {wl.rec.n} / ligand "
+                            f"{wl.lig.n} beads, 5+5 modes; {len(wl.dofs)} poses scored", "energy_evals_per_s": evals,
+                "roofline": roof}
     sub = wl.dofs
     ctx.minimize_6d_modes(*ids, sub[:64], max_evals=10)
     t0 = time.perf_counter()
@@ -616,7 +622,7 @@ def run_modes_only(args):
     from gbattract.context import GbaContext
     ctx = GbaContext(0)
     res = bench_modes(ctx, pkg, n_poses=args.modes_poses, steps=200, minimize=not args.no_min,
-                      with_cpu=not args.no_cpu)
+                      with_cpu=not args.no_cpu, small=args.modes_small)
     ctx.close()
     print(json.dumps({"suite": {"modes": res}}))
     return 0
@@ -661,6 +667,8 @@ def main():
                          "configs 2 (modes) and 3 (adjoint); modes / adjoint / minimize / batched: "
                          "config 2, 3, 0 or 4 alone")
     ap.add_argument("--modes-poses", type=int, default=50000)
+    ap.add_argument("--modes-small", action="store_true",
+                    help="config 2's distributions with a 700 / 300-bead pair (profiling captures)")
     ap.add_argument("--variant", default="order=1,octets=1",
                     help="layout / visiting-order variant timed, or 'search' to time all four "
                          "and keep the fastest")

@@ -26,6 +26,8 @@ metric = energy+gradient evaluations per second.
            persistent work-queue launch in a CUDA graph with default and with
            autotuned per-pair shapes, vs the plain per-step form on every 8th
            pair, per-pair completion times, oracle agreement on a sample
+  suite    config 2 (normal modes: scoring with its census roofline, device
+           vs plain minimization) and config 3 (pairwise energy and adjoint)
 
 `--impl reference` times the reference's CPU implementation of the path (the
 port, or the reference build in oracle/_ref where it exists) on the same
@@ -661,10 +663,11 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-min", action="store_true", help="skip the minimization reports (configs 0 and 4)")
     ap.add_argument("--no-batch", action="store_true", help="skip the config-4 report")
+    ap.add_argument("--no-suite", action="store_true", help="skip the config-2 and config-3 reports")
     ap.add_argument("--suite", default="default",
                     choices=["default", "full", "modes", "adjoint", "minimize", "batched"],
-                    help="default: config 1 (timed), config 0 and config 4 minimization; full: also "
-                         "configs 2 (modes) and 3 (adjoint); modes / adjoint / minimize / batched: "
+                    help="default (= full): config 1 (timed), config 0 and config 4 minimization, "
+                         "config 2 (modes) and config 3 (adjoint); modes / adjoint / minimize / batched: "
                          "config 2, 3, 0 or 4 alone")
     ap.add_argument("--modes-poses", type=int, default=50000)
     ap.add_argument("--modes-small", action="store_true",
@@ -833,7 +836,7 @@ def main():
                                        plain_every=args.plain_every, with_cpu=not args.no_cpu,
                                        nthreads=os.cpu_count() or 1)
     suite = {}
-    if rank == 0 and args.suite == "full":
+    if rank == 0 and not args.no_suite:
         ctx.grid_octets(grid, False)
         suite["modes"] = bench_modes(ctx, pkg, n_poses=args.modes_poses, steps=200, with_cpu=not args.no_cpu)
         suite["adjoint"] = bench_adjoint(ctx, pkg, n_poses=10000)

@@ -323,7 +323,8 @@ class GbaContext:
     def set_kernel_options(self, flags: int):
         """GBA_KOPT_* flags: 1 = computed plateau ratio, 2 = 8 lanes per grid
         lookup, 4 = four-block instantiation, 8 = list entries carrying the
-        receptor type; the default is 15."""
+        receptor type, 16 = the reference CPU path's summation order (bit for
+        bit the reference's results, slower); the default is 15."""
         self._check(self.lib.gba_set_kernel_options(self.h, int(flags)))
 
     def kernel_timing(self, enable: bool):

@@ -133,7 +133,7 @@ extern "C" int gba_autotune(gba_ctx* ctx, gba_id rec, gba_id lig, gba_id grid, g
 			if (!have_e) {
 				best_e = 1e30f;
 				for (int threads : {128, 256}) {
-					const int maxb = rigid_blocks_per_sm(threads, false, base.bound4 != 0);
+					const int maxb = rigid_blocks_per_sm(threads, false, base.bound4 != 0, false, base.ref_order != 0);
 					for (int bps = 1; bps <= maxb; ++bps) {
 						RigidLaunch L = base;
 						L.dofs = d;

@@ -43,7 +43,28 @@ __global__ void __launch_bounds__(256, BOUND4 ? 4 : 1) rigid_energy_kernel(const
 	}
 }
 
+/* GBA_KOPT_REFERENCE_ORDER: each pose summed in the reference CPU path's
+ * order (eval_pose_rigid_ref).  Compiled for two resident 256-thread blocks
+ * per SM: a lane holds a channel's eight corners at once. */
+__global__ void __launch_bounds__(256, 2) rigid_energy_ref_kernel(const RigidLaunch L) {
+	__shared__ WarpStage stage[8];
+	const int lane = threadIdx.x & 31;
+	PoseFeed feed(L.next);
+	for (size_t k = feed.take(lane); k < L.n; k = feed.take(lane)) {
+		const size_t p = L.order ? (size_t)__ldg(&L.order[k]) : k;
+		const float* dofp = reinterpret_cast<const float*>(L.dofs + p);
+		const float dv = lane < 6 ? __ldg(dofp + lane) : 0.f;
+		float c[6];
+#pragma unroll
+		for (int j = 0; j < 6; ++j) c[j] = __shfl_sync(GBA_FULL_MASK, dv, j);
+		float res[7];
+		eval_pose_rigid_ref(L.m, c[0], c[1], c[2], c[3], c[4], c[5], lane, stage[threadIdx.x >> 5], res);
+		store_result7(reinterpret_cast<float*>(L.out + p), res, lane);
+	}
+}
+
 /* Poses of many pairs in one launch: pose p belongs to pair pair_of[p]. */
+template <bool REF>
 __global__ void __launch_bounds__(256) batch_energy_kernel(const BatchEnergyLaunch L) {
 	__shared__ WarpStage stage[8];   /* one per warp of a <=256-thread block */
 	const int lane = threadIdx.x & 31;
@@ -56,19 +77,28 @@ __global__ void __launch_bounds__(256) batch_energy_kernel(const BatchEnergyLaun
 #pragma unroll
 		for (int k = 0; k < 6; ++k) c[k] = __shfl_sync(GBA_FULL_MASK, dv, k);
 		float res[7];
-		eval_pose_rigid<false>(M, c[0], c[1], c[2], c[3], c[4], c[5], lane, stage[threadIdx.x >> 5], res, nullptr);
+		if (REF)
+			eval_pose_rigid_ref(M, c[0], c[1], c[2], c[3], c[4], c[5], lane, stage[threadIdx.x >> 5], res);
+		else
+			eval_pose_rigid<false>(M, c[0], c[1], c[2], c[3], c[4], c[5], lane, stage[threadIdx.x >> 5], res,
+					nullptr);
 		store_result7(reinterpret_cast<float*>(L.out + p), res, lane);
 	}
 }
 
 cudaError_t launch_batch_energy(const BatchEnergyLaunch& L, int blocks, int threads, cudaStream_t s) {
-	batch_energy_kernel<<<blocks, threads, 0, s>>>(L);
+	if (L.ref_order)
+		batch_energy_kernel<true><<<blocks, threads, 0, s>>>(L);
+	else
+		batch_energy_kernel<false><<<blocks, threads, 0, s>>>(L);
 	return cudaGetLastError();
 }
 
 cudaError_t launch_rigid_energy(const RigidLaunch& L, int blocks, int threads, cudaStream_t s) {
 	if (L.census)
 		rigid_energy_kernel<true, false><<<blocks, threads, 0, s>>>(L);
+	else if (L.ref_order)
+		rigid_energy_ref_kernel<<<blocks, threads, 0, s>>>(L);
 	else if (L.roundwise && L.bound4)
 		rigid_energy_kernel<false, true, true><<<blocks, threads, 0, s>>>(L);
 	else if (L.roundwise)
@@ -82,11 +112,11 @@ cudaError_t launch_rigid_energy(const RigidLaunch& L, int blocks, int threads, c
 
 /* resident blocks per SM, queried once per device, instantiation and block
  * size (the query costs host time on every launch otherwise) */
-int rigid_blocks_per_sm(int threads, bool census, bool bound4, bool roundwise) {
-	static std::atomic<int> cache[64][5][33];
+int rigid_blocks_per_sm(int threads, bool census, bool bound4, bool roundwise, bool ref_order) {
+	static std::atomic<int> cache[64][6][33];
 	int dev = 0;
 	cudaGetDevice(&dev);
-	const int v = census ? 0 : (roundwise ? (bound4 ? 3 : 4) : (bound4 ? 1 : 2)), t = threads / 32;
+	const int v = census ? 0 : ref_order ? 5 : (roundwise ? (bound4 ? 3 : 4) : (bound4 ? 1 : 2)), t = threads / 32;
 	const bool cacheable = dev >= 0 && dev < 64 && threads % 32 == 0 && t >= 1 && t <= 32;
 	if (cacheable) {
 		const int c = cache[dev][v][t].load(std::memory_order_relaxed);
@@ -95,6 +125,8 @@ int rigid_blocks_per_sm(int threads, bool census, bool bound4, bool roundwise) {
 	int nb = 0;
 	if (census)
 		cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, rigid_energy_kernel<true, false>, threads, 0);
+	else if (ref_order)
+		cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, rigid_energy_ref_kernel, threads, 0);
 	else if (roundwise && bound4)
 		cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, rigid_energy_kernel<false, true, true>, threads, 0);
 	else if (roundwise)

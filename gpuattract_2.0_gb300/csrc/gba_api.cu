@@ -529,7 +529,7 @@ int gba_set_kernel_options(gba_ctx* ctx, uint32_t flags) {
 	if (!ctx) return GBA_ERR_INVALID_ARGUMENT;
 	GBA_API_BEGIN
 	if (flags & ~(uint32_t)(GBA_KOPT_RATIO_COMPUTED | GBA_KOPT_COOP_LOOKUP | GBA_KOPT_FOUR_BLOCKS |
-			GBA_KOPT_TYPED_LIST))
+			GBA_KOPT_TYPED_LIST | GBA_KOPT_REFERENCE_ORDER))
 		throw ApiError(GBA_ERR_INVALID_ARGUMENT, "gba_set_kernel_options: unknown flag");
 	ctx->bind();
 	Lock g(ctx->stage_mu);
@@ -664,6 +664,7 @@ RigidLaunch Context::rigid_launch(gba_id rec, gba_id lig, gba_id grid, gba_id pa
 	L.m.par = P->dev;
 	L.m.par.pair = P->pair_table(G->dev.nl.dPlateau2, may_allocate);
 	L.bound4 = (kernel_opts & GBA_KOPT_FOUR_BLOCKS) ? 1 : 0;
+	L.ref_order = (kernel_opts & GBA_KOPT_REFERENCE_ORDER) ? 1 : 0;
 	if (kernel_opts & GBA_KOPT_TYPED_LIST)
 		L.m.grid.nl.typed_list = typed_list(*G, rec, *R, may_allocate);
 	return L;
@@ -768,7 +769,7 @@ void Context::run_rigid(RigidLaunch& L, cudaStream_t s, const TuneParams* shape)
 	const int threads = tp.threads;
 	const int warps_per_block = threads / 32;
 	const int bps = std::min(tp.blocks_per_sm, rigid_blocks_per_sm(threads, L.census != nullptr, L.bound4 && !L.census,
-			L.roundwise && !L.census));
+			L.roundwise && !L.census, L.ref_order && !L.census));
 	size_t want = (L.n + warps_per_block - 1) / warps_per_block;
 	size_t blocks = std::min<size_t>(want, (size_t)num_sms * bps);
 	if (blocks == 0) blocks = 1;

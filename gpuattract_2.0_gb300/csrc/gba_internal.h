@@ -113,6 +113,8 @@ struct RigidLaunch {
 	size_t n;
 	int bound4;               /* launch the four-blocks-per-SM instantiation */
 	int roundwise;            /* the minimizers' round-wise summation order (plain form) */
+	int ref_order;            /* the reference CPU path's summation order (GBA_KOPT_REFERENCE_ORDER;
+	                             takes precedence over roundwise and bound4, not over census) */
 	unsigned long long* next; /* pose counter, zero at launch (PoseFeed); nullptr: fixed stride */
 };
 
@@ -140,10 +142,12 @@ struct MinLaunch {
 	unsigned long long budget_ns;   /* per-warp wall-time budget, 0 = none */
 	unsigned long long* t0;         /* earliest warp start (atomicMin), set to ~0 before launch */
 	unsigned long long* done_ns;    /* per pose completion time (globaltimer), may be nullptr */
+	int ref_order;                  /* GBA_KOPT_REFERENCE_ORDER: the reference's summation order
+	                                   (one warp per pose; no team form) */
 };
 
 cudaError_t launch_minimize_rigid(const MinLaunch& L, int blocks, int threads, cudaStream_t s);
-int minimize_blocks_per_sm(int threads);
+int minimize_blocks_per_sm(int threads, bool ref_order = false);
 /* the team form: `team` (1..kMaxTeam) warps split each pose's ligand rounds,
  * plus a control warp running VA13; two poses per block; same results bit
  * for bit */
@@ -159,6 +163,7 @@ struct BatchEnergyLaunch {
 	gba_result6d* out;
 	size_t n;
 	unsigned long long* next; /* pose counter, zero at launch (PoseFeed); nullptr: fixed stride */
+	int ref_order;            /* GBA_KOPT_REFERENCE_ORDER */
 };
 
 cudaError_t launch_batch_energy(const BatchEnergyLaunch& L, int blocks, int threads, cudaStream_t s);
@@ -201,7 +206,8 @@ cudaError_t launch_minimize_modes(const ModesMinLaunch& M, int blocks, int threa
 int minimize_modes_blocks_per_sm(int threads, const ModesLaunch& L);
 
 /* Number of resident blocks per SM of the rigid kernel for `threads`. */
-int rigid_blocks_per_sm(int threads, bool census, bool bound4 = false, bool roundwise = false);
+int rigid_blocks_per_sm(int threads, bool census, bool bound4 = false, bool roundwise = false,
+		bool ref_order = false);
 
 }  // namespace gba
 

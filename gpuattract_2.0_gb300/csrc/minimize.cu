@@ -15,6 +15,9 @@
  *
  * Both kernels sum each pose round-wise (rigid_pose.cuh), as the plain
  * per-step form's scoring launches do, so all three give the same bits.
+ * With GBA_KOPT_REFERENCE_ORDER the one-warp kernel sums in the reference
+ * CPU path's order instead (eval_pose_rigid_ref) and the team kernel is not
+ * used.
  *
  * Small jobs (fewer poses than the GPU has warp slots) run the team kernel
  * instead: a team of G warps evaluates one pose, warp t taking the ligand's
@@ -63,7 +66,10 @@ __device__ __forceinline__ bool warp_over_budget(unsigned long long t_start, uns
  * blocks per SM instead of four) */
 extern __shared__ __align__(16) unsigned char min_stage_smem[];
 
-__global__ void __launch_bounds__(256, 4) minimize_rigid_kernel(const MinLaunch L) {
+/* REF: GBA_KOPT_REFERENCE_ORDER (eval_pose_rigid_ref), compiled for two
+ * resident blocks per SM */
+template <bool REF>
+__global__ void __launch_bounds__(256, REF ? 2 : 4) minimize_rigid_kernel(const MinLaunch L) {
 	WarpStage* stage = reinterpret_cast<WarpStage*>(min_stage_smem);
 	/* per warp, after the staging areas: the VA13 state of its pose (shared
 	 * memory keeps it next to the SM between steps; see TeamShared) */
@@ -106,8 +112,12 @@ __global__ void __launch_bounds__(256, 4) minimize_rigid_kernel(const MinLaunch 
 				}
 #pragma unroll
 				for (int k = 0; k < 6; ++k) cur[k] = __shfl_sync(GBA_FULL_MASK, cur[k], 0);
-				eval_pose_rigid<false, true>(M, cur[0], cur[1], cur[2], cur[3], cur[4], cur[5], lane, stage[threadIdx.x >> 5], res,
-						nullptr);
+				if (REF)
+					eval_pose_rigid_ref(M, cur[0], cur[1], cur[2], cur[3], cur[4], cur[5], lane, stage[threadIdx.x >> 5],
+							res);
+				else
+					eval_pose_rigid<false, true>(M, cur[0], cur[1], cur[2], cur[3], cur[4], cur[5], lane,
+							stage[threadIdx.x >> 5], res, nullptr);
 				++nev;
 				int done = 0;
 				if (lane == 0) {
@@ -277,12 +287,15 @@ static size_t team_smem_bytes(int team) {
 }
 
 cudaError_t launch_minimize_rigid(const MinLaunch& L, int blocks, int threads, cudaStream_t s) {
-	minimize_rigid_kernel<<<blocks, threads, min_stage_bytes(threads), s>>>(L);
+	if (L.ref_order)
+		minimize_rigid_kernel<true><<<blocks, threads, min_stage_bytes(threads), s>>>(L);
+	else
+		minimize_rigid_kernel<false><<<blocks, threads, min_stage_bytes(threads), s>>>(L);
 	return cudaGetLastError();
 }
 
 cudaError_t launch_minimize_rigid_team(const MinLaunch& L, int blocks, int team, cudaStream_t s) {
-	if (team < 1 || team > kMaxTeam) return cudaErrorInvalidValue;
+	if (team < 1 || team > kMaxTeam || L.ref_order) return cudaErrorInvalidValue;
 	minimize_rigid_team_kernel<<<blocks, 32 * (team + 1), team_smem_bytes(team), s>>>(L);
 	return cudaGetLastError();
 }
@@ -295,7 +308,9 @@ static void allow_minimize_smem() {
 	int dev = 0;
 	cudaGetDevice(&dev);
 	if (dev >= 0 && dev < 64 && done[dev].load()) return;
-	cudaFuncSetAttribute(minimize_rigid_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+	cudaFuncSetAttribute(minimize_rigid_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+			(int)min_stage_bytes(256));
+	cudaFuncSetAttribute(minimize_rigid_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
 			(int)min_stage_bytes(256));
 	cudaFuncSetAttribute(minimize_rigid_team_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
 			(int)team_smem_bytes(kMaxTeam));
@@ -303,10 +318,15 @@ static void allow_minimize_smem() {
 	if (dev >= 0 && dev < 64) done[dev].store(1);
 }
 
-int minimize_blocks_per_sm(int threads) {
+int minimize_blocks_per_sm(int threads, bool ref_order) {
 	allow_minimize_smem();
 	int nb = 0;
-	cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, minimize_rigid_kernel, threads, min_stage_bytes(threads));
+	if (ref_order)
+		cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, minimize_rigid_kernel<true>, threads,
+				min_stage_bytes(threads));
+	else
+		cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, minimize_rigid_kernel<false>, threads,
+				min_stage_bytes(threads));
 	return nb > 0 ? nb : 1;
 }
 

@@ -44,6 +44,8 @@ struct Placement {
 }  // namespace
 
 int Context::minimize_team(const TuneParams& tp, size_t n, uint32_t lig_rounds) const {
+	/* the reference's order sums bead by bead: one warp per pose */
+	if (kernel_opts & GBA_KOPT_REFERENCE_ORDER) return 1;
 	int team = team_override;
 	if (team == 0 && tp.team > 0 && n <= tp.team_poses) team = tp.team;
 	if (team == 0) {
@@ -71,7 +73,8 @@ MinShape min_shape(const Context& ctx, const TuneParams& tp, size_t n, int team)
 		m.threads = 32 * (team + 1);
 		m.blocks = std::min<size_t>((n + 1) / 2, (size_t)ctx.num_sms * minimize_team_blocks_per_sm(team));
 	} else {
-		const int bps = std::min(tp.blocks_per_sm, minimize_blocks_per_sm(m.threads));
+		const int bps = std::min(tp.blocks_per_sm,
+				minimize_blocks_per_sm(m.threads, (ctx.kernel_opts & GBA_KOPT_REFERENCE_ORDER) != 0));
 		const size_t warps = (size_t)ctx.num_sms * bps * (m.threads / 32);
 		m.blocks = (size_t)ctx.num_sms * bps;
 		if (warps > n) m.blocks = std::max<size_t>(1, (n * 32 + m.threads - 1) / m.threads);
@@ -91,6 +94,7 @@ cudaError_t launch_shape(const MinLaunch& L, const MinShape& m, cudaStream_t s) 
  * in device memory; captured in a CUDA graph cached by launch signature. */
 void Context::run_minimize(MinLaunch& L, cudaStream_t s, int32_t* status_out, uint32_t lig_rounds,
 		const TuneParams& tp) {
+	L.ref_order = (kernel_opts & GBA_KOPT_REFERENCE_ORDER) ? 1 : 0;
 	const MinShape m = min_shape(*this, tp, L.n, minimize_team(tp, L.n, lig_rounds));
 	L.chunk = m.chunk;
 	if (!aux.ptr) {
@@ -170,6 +174,7 @@ void Context::run_minimize_groups(MinLaunch& L, const std::vector<MinGroup>& gro
 		check_cuda(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "event");
 		group_events.push_back(ev);
 	}
+	L.ref_order = (kernel_opts & GBA_KOPT_REFERENCE_ORDER) ? 1 : 0;
 	std::vector<MinLaunch> Ls(G, L);
 	std::vector<MinShape> shapes(G);
 	uint64_t h = 1469598103934665603ull;
@@ -497,6 +502,7 @@ int gba_batch_energy_6d(gba_ctx* ctx, const gba_pair_job* jobs, size_t njobs, vo
 	const size_t n = G.total;
 	BatchEnergyLaunch L{};
 	L.n = n;
+	L.ref_order = (ctx->kernel_opts & GBA_KOPT_REFERENCE_ORDER) ? 1 : 0;
 	L.models = models_on_device(ctx, G.models, G.key, s);
 	ctx->pair_buf.upload(G.pair_of.data(), n * sizeof(uint32_t));
 	L.pair_of = (const uint32_t*)ctx->pair_buf.ptr;

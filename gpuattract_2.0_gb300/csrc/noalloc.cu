@@ -82,7 +82,8 @@ extern "C" int gba_energy_6d_noalloc(gba_ctx* ctx, gba_id rec, gba_id lig, gba_i
 		/* launch shape as gba_energy_6d chooses it */
 		const TuneParams tp = ctx->pair_tuned("energy", PairKey{rec, lig, grid, params});
 		const int threads = tp.threads;
-		const int bps = std::min(tp.blocks_per_sm, rigid_blocks_per_sm(threads, false, L.bound4 != 0));
+		const int bps = std::min(tp.blocks_per_sm, rigid_blocks_per_sm(threads, false, L.bound4 != 0, false,
+				L.ref_order != 0));
 		size_t blocks = std::min<size_t>((n + threads / 32 - 1) / (threads / 32), (size_t)ctx->num_sms * bps);
 		if (blocks == 0) blocks = 1;
 		check_cuda(launch_rigid_energy(L, (int)blocks, threads, s), "gba_energy_6d_noalloc: launch");

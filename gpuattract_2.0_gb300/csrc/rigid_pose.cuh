@@ -699,6 +699,241 @@ __device__ __forceinline__ void eval_pose_rigid(const RigidModel& M, float tx, f
 	}
 }
 
+/* ---- the reference CPU path's operation order (GBA_KOPT_REFERENCE_ORDER) ----
+ *
+ * CPUEnergyService6D evaluates a pose bead by bead: the bead's grid term
+ * (type channel, then the charge channel times the charge), then its
+ * neighbour list in list order, each pair adding LJPotForce at r, minus it at
+ * the plateau, and (charged pairs) ChargePotForce at r, minus it at the
+ * plateau, partly in double (src/model/neighborlist.h:70-158,
+ * src/model/forcefield.h:30-146); then the bead forces and energies summed in
+ * bead order (reducePotForce, reduceTorque, src/model/reduction.h:40-103).
+ * These functions repeat that arithmetic operation for operation, so with the
+ * same sin/cos the result equals the reference's bit for bit.  A lane walks a
+ * bead's list by itself (no flattened pair windows) and the bead sums run on
+ * 13 lanes sequentially, so this order is slower than the others; it is used
+ * by the minimizers, the plain per-step form and gba_energy_6d when
+ * GBA_KOPT_REFERENCE_ORDER is set. */
+
+/* One channel of trilinearInterpolation (src/model/trilinIntrpl.h:29-66):
+ * the corner products summed left to right in the order d000, d100, d010,
+ * d001, d101, d011, d110, d111, then times 1/voxelVol.  elem as the lookup
+ * queue encodes it (octet record, or first corner of the native layout). */
+__device__ __forceinline__ float4 ref_channel(const DevIntrpl& g, uint32_t elem, const float* cw) {
+	float4 d[8];
+	if (g.oct) {
+		const float4* b = g.oct + 8 * (size_t)elem;
+#pragma unroll
+		for (int c = 0; c < 8; ++c) d[c] = __ldg(b + c);
+	} else {
+		const float4* b = g.data + elem;
+		const uint32_t sx = g.dimN[0], sxy = g.dimN[0] * g.dimN[1];
+#pragma unroll
+		for (int c = 0; c < 8; ++c) d[c] = __ldg(b + (c & 1) + sx * ((c >> 1) & 1) + sxy * (c >> 2));
+	}
+	/* corner c = x + 2 y + 4 z; the reference's order as corner indices */
+	constexpr int ord[8] = {0, 1, 2, 4, 5, 6, 3, 7};
+	float4 o = make_float4(fmul(d[0].x, cw[0]), fmul(d[0].y, cw[0]), fmul(d[0].z, cw[0]), fmul(d[0].w, cw[0]));
+#pragma unroll
+	for (int k = 1; k < 8; ++k) {
+		const int c = ord[k];
+		o.x = fadd(o.x, fmul(d[c].x, cw[c]));
+		o.y = fadd(o.y, fmul(d[c].y, cw[c]));
+		o.z = fadd(o.z, fmul(d[c].z, cw[c]));
+		o.w = fadd(o.w, fmul(d[c].w, cw[c]));
+	}
+	return make_float4(fmul(o.x, g.voxelVol_inv), fmul(o.y, g.voxelVol_inv), fmul(o.z, g.voxelVol_inv),
+			fmul(o.w, g.voxelVol_inv));
+}
+
+/* LJPotForce (swi = 1) as the reference computes it: the force factor in
+ * double, rounded to float. */
+__device__ __forceinline__ void ref_lj(float dr2, float dr2_inv, float dx, float dy, float dz, const float4 p,
+		float ivor, bool shape86, float& fx, float& fy, float& fz, float& e) {
+	const float rr23 = fmul(fmul(dr2_inv, dr2_inv), dr2_inv);
+	const float rrd = shape86 ? dr2_inv : rr23;
+	const float sd = shape86 ? 2.0f : 6.0f;
+	const float rep = fmul(p.x, rrd);
+	const float vlj = fmul(fsub(rep, p.y), rr23);
+	const double sum = __dadd_rn(__dmul_rn(6.0, (double)vlj), (double)fmul(sd, fmul(rep, rr23)));
+	float fb;
+	if (dr2 < p.z) {
+		e = fadd(vlj, fmul(fsub(ivor, 1.0f), p.w));
+		fb = (float)sum;
+	} else {
+		e = fmul(ivor, vlj);
+		fb = (float)__dmul_rn((double)ivor, sum);
+	}
+	fx = fmul(fb, dx); fy = fmul(fb, dy); fz = fmul(fb, dz);
+}
+
+/* ChargePotForce (swi = 1) as the reference computes it. */
+__device__ __forceinline__ void ref_coulomb(float dr2_inv, float dx, float dy, float dz, float qq, bool cdiel,
+		float& fx, float& fy, float& fz, float& e) {
+	float dd;
+	if (cdiel) dd = (float)__dsub_rn((double)__fsqrt_rn(dr2_inv), 1.0 / 50.0);
+	else dd = (float)__dsub_rn((double)dr2_inv, 1.0 / (50.0 * 50.0));
+	if (dd < 0.0f) dd = 0.0f;
+	e = fmul(qq, dd);
+	if (dd <= 0.0f) {
+		fx = fy = fz = 0.0f;
+		return;
+	}
+	if (cdiel) {
+		const double et2 = (double)fmul(qq, __fsqrt_rn(dr2_inv));
+		fx = (float)__dmul_rn(et2, (double)dx);
+		fy = (float)__dmul_rn(et2, (double)dy);
+		fz = (float)__dmul_rn(et2, (double)dz);
+	} else {
+		const double et2 = __dmul_rn(2.0, (double)fmul(qq, dr2_inv));
+		fx = (float)__dmul_rn(et2, (double)dx);
+		fy = (float)__dmul_rn(et2, (double)dy);
+		fz = (float)__dmul_rn(et2, (double)dz);
+	}
+}
+
+/* The neighbour-list term of one bead in list order (NLPotForce's loop):
+ * returns the bead's accumulated (fx, fy, fz, E). */
+__device__ __forceinline__ float4 ref_nl_bead(const RigidModel& M, float px, float py, float pz, float qlig,
+		uint32_t tlig, uint32_t base, uint32_t num) {
+	const DevNL& nl = M.grid.nl;
+	const DevParams& P = M.par;
+	const uint32_t* lst = nl.typed_list ? nl.typed_list : nl.list;
+	const bool typed = nl.typed_list != nullptr;
+	const bool shape86 = P.potshape == GBA_POTSHAPE_8_6;
+	const bool cdiel = P.dielec == GBA_DIELEC_CONSTANT;
+	float ax = 0.f, ay = 0.f, az = 0.f, ae = 0.f;
+	for (uint32_t k = 0; k < num; ++k) {
+		const uint32_t ent = __ldg(&lst[base + k]);
+		const uint32_t j = typed ? ent & 0xffffffu : ent;
+		const float4 r = __ldg(&M.rec.xyzq[j]);
+		float dx = fsub(px, r.x), dy = fsub(py, r.y), dz = fsub(pz, r.z);
+		const float dr2 = fadd(fadd(fmul(dx, dx), fmul(dy, dy)), fmul(dz, dz));
+		if (dr2 > nl.dPlateau2) continue;
+		const uint32_t trec = typed ? ent >> 24 : __ldg(&M.rec.tm[j]) & 0xffffu;
+		if (trec == 0) continue;   /* no parameters (the reference would index before its table) */
+		/* (float)(1.0 / (double)dr2): double rounding is harmless here, so
+		 * this is the correctly rounded float reciprocal */
+		const float dr2_inv = __frcp_rn(dr2);
+		dx = fmul(dx, dr2_inv); dy = fmul(dy, dr2_inv); dz = fmul(dz, dr2_inv);
+		const size_t kp = (size_t)P.num_types * (trec - 1) + (tlig - 1);
+		const float4 p = __ldg(&P.lj[kp]);
+		const float ivor = __ldg(&P.ivor[kp]);
+		float fx, fy, fz, e;
+		ref_lj(dr2, dr2_inv, dx, dy, dz, p, ivor, shape86, fx, fy, fz, e);
+		ax = fadd(ax, fx); ay = fadd(ay, fy); az = fadd(az, fz); ae = fadd(ae, e);
+		const float ratio = __ldg(&nl.ratio[(int)fmul(dr2, 10000.0f)]);
+		const float rdx = fmul(ratio, dx), rdy = fmul(ratio, dy), rdz = fmul(ratio, dz);
+		ref_lj(nl.dPlateau2, nl.dPlateau2_inv, rdx, rdy, rdz, p, ivor, shape86, fx, fy, fz, e);
+		ax = fsub(ax, fx); ay = fsub(ay, fy); az = fsub(az, fz); ae = fsub(ae, e);
+		const float qq = fmul(fmul(qlig, r.w), P.ffelec);
+		if ((double)fabsf(qq) > 0.001) {
+			ref_coulomb(dr2_inv, dx, dy, dz, qq, cdiel, fx, fy, fz, e);
+			ax = fadd(ax, fx); ay = fadd(ay, fy); az = fadd(az, fz); ae = fadd(ae, e);
+			ref_coulomb(nl.dPlateau2_inv, rdx, rdy, rdz, qq, cdiel, fx, fy, fz, e);
+			ax = fsub(ax, fx); ay = fsub(ay, fy); az = fsub(az, fz); ae = fsub(ae, e);
+		}
+	}
+	return make_float4(ax, ay, az, ae);
+}
+
+/* One round in the reference's order: for each of the 64 staged beads its
+ * total (fx, fy, fz, E) -- grid term, plus the neighbour-list term for beads
+ * that looked it up -- parked in the slot's first four weight floats
+ * (W.cw[9 s .. 9 s + 3], free once the bead's grid term is done). */
+__device__ __forceinline__ void eval_round_ref(const RigidModel& M, uint32_t i0, int lane, WarpStage& W) {
+	float ttx, tty, ttz;
+	const PoseRot R = get_pose(W, ttx, tty, ttz);
+#pragma unroll
+	for (int h = 0; h < 2; ++h) {
+		const int s = lane + 32 * h;
+		const uint32_t i = i0 + s;
+		if (i >= M.lig.n) continue;
+		const float4 b = __ldg(&M.lig.xyzq[i]);
+		const uint32_t tm = __ldg(&M.lig.tm[i]);
+		const uint32_t type = tm & 0xffffu, mapped = tm >> 16;
+		float px, py, pz;
+		rot_apply(R.m, b.x, b.y, b.z, px, py, pz);
+		px = fadd(px, ttx); py = fadd(py, tty); pz = fadd(pz, ttz);
+		put_bead(W, s, b.x, b.y, b.z, px, py, pz, b.w, type);
+		BeadGrid bg{0u, 0u};
+		const uint32_t nlk = stage_grid(M.grid, px, py, pz, mapped, b.w, s, W, bg);
+		float* cw = W.cw + kCornerStride * s;
+		float4 pot = make_float4(0.f, 0.f, 0.f, 0.f);
+		if (nlk > 0) {
+			const DevIntrpl& g = (bg.t & 0x80000000u) ? M.grid.outer : M.grid.inner;
+			pot = ref_channel(g, bg.t & 0x7fffffffu, cw);
+			if (nlk > 1) {
+				float4 el = ref_channel(g, bg.q & 0x7fffffffu, cw);
+				el.x = fmul(el.x, b.w); el.y = fmul(el.y, b.w); el.z = fmul(el.z, b.w); el.w = fmul(el.w, b.w);
+				pot.x = fadd(pot.x, el.x); pot.y = fadd(pot.y, el.y); pot.z = fadd(pot.z, el.z);
+				pot.w = fadd(pot.w, el.w);
+			}
+		}
+		if (type != 0) {
+			bool in_nl = false;
+			const uint32_t num = stage_nl(M.grid.nl, px, py, pz, s, W, in_nl);
+			if (in_nl) {
+				const float4 a = ref_nl_bead(M, px, py, pz, b.w, type, W.lbase[s], num);
+				pot.x = fadd(pot.x, a.x); pot.y = fadd(pot.y, a.y); pot.z = fadd(pot.z, a.z);
+				pot.w = fadd(pot.w, a.w);
+			}
+		}
+		cw[0] = pot.x; cw[1] = pot.y; cw[2] = pot.z; cw[3] = pot.w;
+	}
+	__syncwarp();
+}
+
+/* Adds the bead totals of slots 0 .. nb-1 of W to the running sums, in bead
+ * order: lane c < 13 owns sum c (0 energy, 1..3 force, 4 + 3 a + b the
+ * torque entry x_b f_a).  Returns the lane's updated sum. */
+__device__ __forceinline__ float ref_accumulate(const WarpStage& W, uint32_t nb, int lane, float acc) {
+	if (lane < 13) {
+		const int a = (lane - 4) / 3, bb = (lane - 4) % 3;
+		for (uint32_t s = 0; s < nb; ++s) {
+			const float* f = W.cw + kCornerStride * s;
+			if (lane == 0) {
+				acc = fadd(acc, f[3]);
+			} else if (lane < 4) {
+				acc = fadd(acc, f[lane - 1]);
+			} else {
+				const float4 u = W.ut[s];
+				const float ub = bb == 0 ? u.x : (bb == 1 ? u.y : u.z);
+				acc = fadd(acc, fmul(ub, f[a]));
+			}
+		}
+	}
+	return acc;
+}
+
+/* The pose result from the running sums of lanes 0..12: ForceLim and the
+ * TorqueMat contraction, on every lane. */
+__device__ __forceinline__ void finish_ref(float acc, const WarpStage& W, float res[7]) {
+	float c[13];
+#pragma unroll
+	for (int k = 0; k < 13; ++k) c[k] = __shfl_sync(GBA_FULL_MASK, acc, k);
+	float sFx = c[1], sFy = c[2], sFz = c[3];
+	force_lim(sFx, sFy, sFz);
+	float ang[3];
+	float ttx, tty, ttz;
+	torque_reduce(get_pose(W, ttx, tty, ttz), c + 4, ang);
+	res[0] = c[0]; res[1] = sFx; res[2] = sFy; res[3] = sFz;
+	res[4] = ang[0]; res[5] = ang[1]; res[6] = ang[2];
+}
+
+/* A whole pose in the reference's order, one warp. */
+__device__ __forceinline__ void eval_pose_rigid_ref(const RigidModel& M, float tx, float ty, float tz,
+		float a0, float a1, float a2, int lane, WarpStage& W, float res[7]) {
+	put_pose(W, pose_rotation(a0, a1, a2, lane), tx, ty, tz, lane);
+	float acc = 0.f;
+	for (uint32_t i0 = 0; i0 < M.lig.n; i0 += kBeadsPerRound) {
+		eval_round_ref(M, i0, lane, W);
+		acc = ref_accumulate(W, min((uint32_t)kBeadsPerRound, M.lig.n - i0), lane, acc);
+		__syncwarp();
+	}
+	finish_ref(acc, W, res);
+}
+
 /* Barrier of the `nthreads` threads that use barrier `id` (a named barrier:
  * a subset of the block's warps). */
 __device__ __forceinline__ void group_sync(int id, int nthreads) {

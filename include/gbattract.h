@@ -181,13 +181,30 @@ int gba_set_pose_order(gba_ctx* ctx, int enable);
  *                            per list entry, kept with the grid until either
  *                            is released) instead of gathering the type per
  *                            pair.  Receptors with types above 255 or 2^24
- *                            beads or more keep the gather.
- * The default is all four.  Changing options drops the cached minimizer
- * graphs. */
+ *                            beads or more keep the gather;
+ *   GBA_KOPT_REFERENCE_ORDER every pose is summed in the reference CPU
+ *                            path's operation order (CPUEnergyService6D,
+ *                            src/service/CPUEnergyService6D.tpp:63-200): bead
+ *                            by bead, grid term then neighbour list in list
+ *                            order, the reference's float and double steps,
+ *                            then the bead sums in bead order -- so energies
+ *                            and minimizer trajectories equal the reference's
+ *                            bit for bit wherever its sin/cos are correctly
+ *                            rounded.  Reads the ratio table and the
+ *                            native lookups whatever the other options say.
+ *                            Slower (a lane walks a bead's list alone);
+ *                            applies to gba_energy_6d, the noalloc
+ *                            and batch scoring calls, both minimizer forms
+ *                            (one warp per pose: no teams), not to
+ *                            gba_census_6d or the normal-mode calls.  Off by
+ *                            default.
+ * The default is the first four.  Changing options drops the cached
+ * minimizer graphs. */
 #define GBA_KOPT_RATIO_COMPUTED 1u
 #define GBA_KOPT_COOP_LOOKUP    2u
 #define GBA_KOPT_FOUR_BLOCKS    4u
 #define GBA_KOPT_TYPED_LIST     8u
+#define GBA_KOPT_REFERENCE_ORDER 16u
 #define GBA_KOPT_DEFAULT        (GBA_KOPT_RATIO_COMPUTED | GBA_KOPT_COOP_LOOKUP | GBA_KOPT_FOUR_BLOCKS | \
                                  GBA_KOPT_TYPED_LIST)
 int gba_set_kernel_options(gba_ctx* ctx, uint32_t flags);

@@ -4,7 +4,9 @@ Run in a tree where the reference sources were compiled into
 oracle/_ref/libattract_ref.so (oracle/build_ref.sh).  Each fixture stores the
 inputs (pivotized beads, types, charges, modes, the parameter table, grid
 options, poses) and the reference's outputs for them, computed through its
-Server<Types_6D<float>> + CPUEnergyService6D<float> (or the modes variant).
+Server<Types_6D<float>> + CPUEnergyService6D<float> (or the modes variant);
+rigid fixtures also mark the poses whose sin/cos the generating host's libm
+rounded correctly (sincos_exact).
 Grids are not stored: tests rebuild them with the oracle's CPU grid builder,
 which is deterministic, and feed the identical grid to every path.
 
@@ -32,6 +34,14 @@ from oracle import pyoracle as po  # noqa: E402
 
 REF_TEST = po.ref_root() / "test" / "resources"
 OUT = Path(__file__).resolve().parent
+
+
+def sincos_mask(dofs):
+    """Per rigid pose: whether this host's sinf/cosf (the ones the reference
+    called) returned the correctly rounded value for all three angles -- the
+    poses on which a device summing in the reference's order must equal
+    ref_out bit for bit."""
+    return po.libm_sincos_rounds_exactly(np.asarray(dofs)[:, 3:6])
 
 
 def pack(name, rec, lig, params, opts, dofs, out, extra=None):
@@ -64,7 +74,7 @@ def rigid_synth():
     opts = pkg.GridOptions()
     grid = po.build_grid(wl.rec, wl.params, opts)
     out = po.ref_energy_6d(wl.rec, wl.lig, grid, wl.params, wl.dofs, nworkers=2, item_size=17)
-    pack("rigid_synth", wl.rec, wl.lig, wl.params, opts, wl.dofs, out)
+    pack("rigid_synth", wl.rec, wl.lig, wl.params, opts, wl.dofs, out, dict(sincos_exact=sincos_mask(wl.dofs)))
 
 
 def rigid_const():
@@ -75,7 +85,7 @@ def rigid_const():
     opts = pkg.GridOptions()
     grid = po.build_grid(wl.rec, wl.params, opts)
     out = po.ref_energy_6d(wl.rec, wl.lig, grid, wl.params, wl.dofs, nworkers=1, item_size=100)
-    pack("rigid_const", wl.rec, wl.lig, wl.params, opts, wl.dofs, out)
+    pack("rigid_const", wl.rec, wl.lig, wl.params, opts, wl.dofs, out, dict(sincos_exact=sincos_mask(wl.dofs)))
 
 
 def rigid_pdb():
@@ -96,7 +106,7 @@ def rigid_pdb():
     rng = np.random.default_rng(303)
     dofs = pkg.synth.random_poses(rng, 64, 22.0, 32.0)
     out = po.ref_energy_6d(rec, lig, grid, params, dofs, nworkers=2, item_size=100)
-    pack("rigid_pdb", rec, lig, params, opts, dofs, out)
+    pack("rigid_pdb", rec, lig, params, opts, dofs, out, dict(sincos_exact=sincos_mask(dofs)))
 
 
 def modes_synth():

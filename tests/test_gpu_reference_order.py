@@ -1,0 +1,159 @@
+"""GBA_KOPT_REFERENCE_ORDER: the kernels sum every pose in the reference CPU
+path's operation order (CPUEnergyService6D, src/service/CPUEnergyService6D.tpp:63-200:
+bead by bead, grid term then the neighbour list in list order with the
+reference's float and double steps, then the bead sums in bead order).
+
+The device then equals the reference bit for bit wherever the reference's
+sin/cos are correctly rounded:
+* against the reference's own outputs (the golden fixtures) on every pose
+  whose angles the generating host's sinf/cosf rounded correctly;
+* against the oracle with correctly rounded sin/cos on every pose, at the
+  sizes of config 0 and on a config-1 sample;
+* minimization: config 0 in full (1,000 poses, maxFunEval 100) -- the
+  device VA13 trajectories, evaluation counts and final results equal the
+  oracle's minfor driving the same arithmetic, bit for bit, in the
+  persistent kernel, the plain per-step form and a multi-pair batch.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from conftest import golden_inputs
+
+pytestmark = pytest.mark.gpu
+
+KOPT_DEFAULT = 15
+KOPT_REFERENCE_ORDER = 16
+RIGID = ["rigid_synth", "rigid_const", "rigid_pdb"]
+
+
+@pytest.fixture(scope="module")
+def ctx(pkg):
+    from gbattract.context import GbaContext
+    c = GbaContext(0)
+    c.set_kernel_options(KOPT_DEFAULT | KOPT_REFERENCE_ORDER)
+    yield c
+    c.close()
+
+
+def _upload(ctx, rec, lig, grid, params):
+    return (ctx.upload_protein(rec), ctx.upload_protein(lig), ctx.upload_grid(grid),
+            ctx.upload_params(params))
+
+
+@pytest.mark.parametrize("name", RIGID)
+def test_equals_reference_outputs(name, golden_cases, oracle, ctx):
+    d = golden_cases[name]
+    rec, lig, params, opts = golden_inputs(d)
+    grid = oracle.build_grid(rec, params, opts)
+    ids = _upload(ctx, rec, lig, grid, params)
+    got = ctx.energy_6d(*ids, d["dofs"])
+    exact = d["sincos_exact"].astype(bool)
+    with oracle.exact_sincos():
+        ref_x = oracle.energy_6d(rec, lig, grid, params, d["dofs"])
+    print(f"{name}: {int(exact.sum())}/{len(exact)} poses with correctly rounded libm sin/cos; "
+          f"bitwise equal to the reference on {int(np.all(got == d['ref_out'], axis=1).sum())}")
+    assert exact.mean() > 0.9
+    assert np.array_equal(got[exact], d["ref_out"][exact])
+    assert np.array_equal(got, ref_x)
+    for i in ids:
+        ctx.release(i)
+
+
+def test_option_combinations_agree(small_case, oracle, ctx):
+    """The order ignores the other options (it reads the ratio table and the
+    native corners): every combination, with and without the octet copy,
+    gives the same bits, equal to the exact-sincos oracle."""
+    wl, grid = small_case
+    ids = _upload(ctx, wl.rec, wl.lig, grid, wl.params)
+    with oracle.exact_sincos():
+        ref = oracle.energy_6d(wl.rec, wl.lig, grid, wl.params, wl.dofs)
+    try:
+        for flags, octets in ((16, False), (16 | 8, False), (31, True), (16 | 2, True)):
+            ctx.grid_octets(ids[2], octets)
+            ctx.set_kernel_options(flags)
+            assert np.array_equal(ctx.energy_6d(*ids, wl.dofs), ref), flags
+    finally:
+        ctx.set_kernel_options(KOPT_DEFAULT | KOPT_REFERENCE_ORDER)
+        ctx.grid_octets(ids[2], False)
+    for i in ids:
+        ctx.release(i)
+
+
+def test_noalloc_and_batch_follow_the_option(small_case, oracle, ctx):
+    import torch
+    wl, grid = small_case
+    ids = _upload(ctx, wl.rec, wl.lig, grid, wl.params)
+    ref = ctx.energy_6d(*ids, wl.dofs)
+    fn = ctx.lib.gba_energy_6d_noalloc
+    fn.argtypes = [C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_void_p, C.c_size_t,
+                   C.c_void_p, C.c_void_p]
+    fn.restype = C.c_int
+    d = torch.from_numpy(wl.dofs).cuda()
+    out = torch.empty((len(wl.dofs), 7), dtype=torch.float32, device="cuda")
+    assert fn(ctx.h, *ids, d.data_ptr(), len(wl.dofs), out.data_ptr(), None) == 0
+    torch.cuda.synchronize()
+    assert np.array_equal(out.cpu().numpy(), ref)
+    (be,) = ctx.batch_energy_6d([(*ids, wl.dofs)])
+    assert np.array_equal(be, ref)
+    for i in ids:
+        ctx.release(i)
+
+
+def test_config1_sample_bitwise(pkg, oracle, ctx):
+    """Receptor 2000 / ligand 700 beads, 2,048 of config 1's poses, on the
+    device-built grid with its octet copy."""
+    wl = pkg.synth.make_config(1)
+    dofs = np.ascontiguousarray(wl.dofs[:2048])
+    rec, lig, par = ctx.upload_protein(wl.rec), ctx.upload_protein(wl.lig), ctx.upload_params(wl.params)
+    gid = ctx.build_grid(rec, par, pkg.GridOptions())
+    ctx.grid_octets(gid, True)
+    host = ctx.download_grid(gid)
+    got = ctx.energy_6d(rec, lig, gid, par, dofs)
+    with oracle.exact_sincos():
+        ref = oracle.energy_6d(wl.rec, wl.lig, host, wl.params, dofs)
+    assert np.array_equal(got, ref)
+    for i in (gid, lig, rec, par):
+        ctx.release(i)
+
+
+def test_config0_minimization_bitwise(pkg, oracle, ctx):
+    wl = pkg.synth.make_config(0)
+    rec, lig, par = ctx.upload_protein(wl.rec), ctx.upload_protein(wl.lig), ctx.upload_params(wl.params)
+    gid = ctx.build_grid(rec, par, pkg.GridOptions())
+    ids = (rec, lig, gid, par)
+    grid = ctx.download_grid(gid)
+    steps = wl.steps
+    dev = ctx.minimize_6d(*ids, wl.dofs, max_evals=steps)
+    with oracle.exact_sincos():
+        ref = oracle.minimize_6d(wl.rec, wl.lig, grid, wl.params, wl.dofs, steps)
+    for a, b, what in zip(dev, ref, ("states", "results", "evaluations")):
+        assert np.array_equal(a, b), what
+    plain = ctx.minimize_6d_plain(*ids, wl.dofs[:200], max_evals=steps)
+    for a, b in zip(plain, ref):
+        assert np.array_equal(a, b[:200])
+    # against the oracle as the reference runs it (the C library's sin/cos)
+    _, r_libm, _ = oracle.minimize_6d(wl.rec, wl.lig, grid, wl.params, wl.dofs, steps)
+    st = oracle.minimization_stats(dev[1], r_libm)
+    same = float(np.mean(np.all(dev[1] == r_libm, axis=1)))
+    print(f"config 0 minimization in the reference order: bitwise equal to the exact-sincos oracle on "
+          f"all {len(wl.dofs)} poses; vs the libm oracle {st}, identical trajectories {same:.3f}")
+    for i in (gid, lig, rec, par):
+        ctx.release(i)
+
+
+def test_batch_minimize_bitwise(pkg, oracle, ctx):
+    """Three pairs of uneven sizes in one batch: each pose's trajectory equals
+    the oracle's."""
+    pairs, refs = [], []
+    for k, (nr, nl, npz) in enumerate([(120, 50, 40), (200, 90, 7), (90, 140, 65)]):
+        wl = pkg.synth.make_pair(4, nr, nl, npz, (18.0, 28.0), seed=3000 + k)
+        grid = oracle.build_grid(wl.rec, wl.params, pkg.GridOptions())
+        pairs.append((*_upload(ctx, wl.rec, wl.lig, grid, wl.params), wl.dofs))
+        with oracle.exact_sincos():
+            refs.append(oracle.minimize_6d(wl.rec, wl.lig, grid, wl.params, wl.dofs, 60))
+    got = ctx.batch_minimize_6d(pairs, max_evals=60)
+    for g, r in zip(got, refs):
+        for a, b in zip(g, r):
+            assert np.array_equal(a, b)

@@ -27,6 +27,22 @@ def test_rigid_oracle_matches_reference_fixture(name, golden_cases, oracle):
     assert st["n_grid"].min() > 0 and st["n_pairs"].sum() > 0
 
 
+@pytest.mark.parametrize("name", RIGID)
+def test_exact_sincos_oracle_bitwise_on_exact_poses(name, golden_cases, oracle):
+    """With correctly rounded sin/cos the restatement equals the reference's
+    outputs bit for bit on every pose whose angles the generating host's
+    sinf/cosf rounded correctly -- on any host, since it no longer depends on
+    the local libm."""
+    d = golden_cases[name]
+    rec, lig, params, opts = golden_inputs(d)
+    grid = oracle.build_grid(rec, params, opts)
+    with oracle.exact_sincos():
+        got = oracle.energy_6d(rec, lig, grid, params, d["dofs"])
+    exact = d["sincos_exact"].astype(bool)
+    assert exact.mean() > 0.9
+    assert np.array_equal(got[exact], d["ref_out"][exact])
+
+
 def test_modes_oracle_matches_reference_fixture(golden_cases, oracle):
     d = golden_cases["modes_synth"]
     rec, lig, params, opts = golden_inputs(d)

@@ -52,6 +52,7 @@ sys.path.insert(0, str(ROOT))
 METRIC = "E+grad evals/s"
 UNIT = "evals/s"
 WORKLOAD = "rigid scoring, receptor 2000 / ligand 700 beads, 100000 poses (config 1)"
+KOPT_REFERENCE_ORDER = 16    # GBA_KOPT_REFERENCE_ORDER: the reference CPU path's summation order
 
 
 def log(*a):
@@ -278,12 +279,14 @@ def run_reference(args):
     return 0
 
 
-def bench_minimization(ctx, pkg, nthreads: int, with_cpu: bool):
+def bench_minimization(ctx, pkg, nthreads: int, with_cpu: bool, kopts: int = 15):
     """Config 0 (receptor 500 / ligand 200 beads, 1000 poses, 100-evaluation VA13):
     minimized poses/s of the device-resident batched form, of the plain per-step
     forms (one launch per round; the reference's 100-pose work items) and of the
     CPU oracle's VA13 on all host threads, with the agreement of the minimized
-    energies."""
+    energies; and the batched form in the reference's summation order
+    (GBA_KOPT_REFERENCE_ORDER), its cost and its bitwise equality with the
+    oracle taking correctly rounded sin/cos."""
     import torch
     wl = pkg.synth.make_config(0)
     rec, lig, par = ctx.upload_protein(wl.rec), ctx.upload_protein(wl.lig), ctx.upload_params(wl.params)
@@ -307,6 +310,15 @@ def bench_minimization(ctx, pkg, nthreads: int, with_cpu: bool):
         dt = time.perf_counter() - t0
         out[key + "_poses_per_s"] = n / dt
         out[key + "_identical_to_batched"] = bool(np.array_equal(r_p, r_dev))
+    ctx.set_kernel_options(kopts | KOPT_REFERENCE_ORDER)
+    ctx.minimize_6d(*ids, wl.dofs[:128], max_evals=steps)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    ro = ctx.minimize_6d(*ids, wl.dofs, max_evals=steps)
+    dt_ro = time.perf_counter() - t0
+    ctx.set_kernel_options(kopts)
+    out["reference_order_poses_per_s"] = n / dt_ro
+    out["reference_order_time_ratio"] = dt_ro / dt_dev
     out["speedup_vs_plain_one_launch"] = out["batched_device_poses_per_s"] / out["plain_one_launch_per_round_poses_per_s"]
     out["speedup_vs_plain_100_pose_items"] = out["batched_device_poses_per_s"] / out["plain_100_pose_items_poses_per_s"]
     if with_cpu:
@@ -326,6 +338,12 @@ def bench_minimization(ctx, pkg, nthreads: int, with_cpu: bool):
         _, r_ulp, _ = po.minimize_6d(wl.rec, wl.lig, gh, wl.params, d1, steps, nthreads=nthreads)
         rel = np.abs(r_ulp[:, 0].astype(np.float64) - r_cpu[:, 0]) / np.maximum(np.abs(r_cpu[:, 0]), 1e-3)
         out["oracle_self_agreement_one_ulp_start"] = float(np.mean(rel <= 1e-3))
+        rel = np.abs(ro[1][:, 0].astype(np.float64) - r_cpu[:, 0]) / np.maximum(np.abs(r_cpu[:, 0]), 1e-3)
+        out["reference_order_agreement_within_1e-3"] = float(np.mean(rel <= 1e-3))
+        with po.exact_sincos():
+            x = po.minimize_6d(wl.rec, wl.lig, gh, wl.params, wl.dofs, steps, nthreads=nthreads)
+        out["reference_order_bitwise_equal_exact_sincos_oracle"] = bool(
+            all(np.array_equal(a, b) for a, b in zip(ro, x)))
     for i in (grid, lig, rec, par):
         ctx.release(i)
     return out
@@ -814,6 +832,20 @@ def main():
     # parity spot check of the timed result (device path) against the host path
     ok = bool(np.array_equal(out.cpu().numpy(), ho.numpy()))
 
+    # the same batch summed in the reference CPU path's order (outside the
+    # timed region; the timed result is kept in `out` for the parity check)
+    reference_order = None
+    if not args.kopts & KOPT_REFERENCE_ORDER:
+        keep = out.clone()
+        ctx.set_kernel_options(args.kopts | KOPT_REFERENCE_ORDER)
+        step()
+        torch.cuda.synchronize()
+        ro_ms = timed_ms(2)
+        ctx.set_kernel_options(args.kopts)
+        reference_order = {"evals_per_s": n / (ro_ms / 1000.0), "ms_per_step": ro_ms,
+                           "time_ratio": ro_ms / (1000.0 * kavg)}
+        out.copy_(keep)
+
     cpu = None
     parity = None
     if rank == 0 and not args.no_cpu:
@@ -828,7 +860,7 @@ def main():
     l2_peak = measured_l2_peak() if rank == 0 else None
     minim = None
     if rank == 0 and not args.no_min:
-        minim = bench_minimization(ctx, pkg, os.cpu_count() or 1, with_cpu=not args.no_cpu)
+        minim = bench_minimization(ctx, pkg, os.cpu_count() or 1, with_cpu=not args.no_cpu, kopts=args.kopts)
     batched = None
     if rank == 0 and not args.no_min and not args.no_batch:
         ctx.grid_octets(grid, False)
@@ -867,6 +899,7 @@ def main():
             # per step: the fused energy kernel (+ the three visiting-order kernels --
             # cell counts, their prefix sum, the scatter -- when the order is on)
             "gpu_launches": args.steps * (4 if best.startswith("order=1") else 1),
+            "reference_order": reference_order,
             "minimization": minim,
             "batched_uneven": batched,
             "variants_ms": variants, "variant_timed": best, "kernel_options": args.kopts,

@@ -41,6 +41,8 @@
 #ifndef GBA_RIGID_POSE_CUH_
 #define GBA_RIGID_POSE_CUH_
 
+#include <cstddef>
+
 #include "energy_dev.cuh"
 
 namespace gba {
@@ -792,62 +794,109 @@ __device__ __forceinline__ void ref_coulomb(float dr2_inv, float dx, float dy, f
 	}
 }
 
-/* The neighbour-list term of one bead in list order (NLPotForce's loop):
- * returns the bead's accumulated (fx, fy, fz, E). */
-__device__ __forceinline__ float4 ref_nl_bead(const RigidModel& M, float px, float py, float pz, float qlig,
-		uint32_t tlig, uint32_t base, uint32_t num) {
+/* The four sub-terms NLPotForce adds for one pair -- LJPotForce at r, at the
+ * plateau, ChargePotForce at r, at the plateau -- each (fx, fy, fz, E), for
+ * the 32 pairs of a window; flags bit 0: the pair is within the plateau,
+ * bit 1: its charge product passes the Coulomb test.  Overlaid on the
+ * staging area's corner weights and lookup queue, which the reference order
+ * does not use once the round's grid terms are taken. */
+struct RefTerms {
+	float4 t[32][4];
+	uint32_t flags[32];
+};
+static_assert(sizeof(RefTerms) <= sizeof(WarpStage::cw) + sizeof(WarpStage::look), "RefTerms overlay");
+static_assert(offsetof(WarpStage, look) == offsetof(WarpStage, cw) + sizeof(WarpStage::cw), "RefTerms overlay");
+static_assert(offsetof(WarpStage, cw) % 16 == 0, "RefTerms overlay");
+
+__device__ __forceinline__ RefTerms& ref_terms(WarpStage& W) { return *reinterpret_cast<RefTerms*>(W.cw); }
+
+/* The sub-terms of one pair -- ligand bead staged in slot sl, list entry ent
+ * -- into window position b (the loop body of NLPotForce,
+ * src/model/neighborlist.h:70-158). */
+__device__ __forceinline__ void ref_pair_terms(const RigidModel& M, WarpStage& W, uint32_t sl, uint32_t ent,
+		int b) {
 	const DevNL& nl = M.grid.nl;
 	const DevParams& P = M.par;
-	const uint32_t* lst = nl.typed_list ? nl.typed_list : nl.list;
 	const bool typed = nl.typed_list != nullptr;
+	const uint32_t j = typed ? ent & 0xffffffu : ent;
+	const float4 r = __ldg(&M.rec.xyzq[j]);
+	const uint32_t trec = typed ? ent >> 24 : __ldg(&M.rec.tm[j]) & 0xffffu;
+	const float4 bq = W.pq[sl];
+	const uint32_t tlig = __float_as_uint(W.ut[sl].w);
+	float dx = fsub(bq.x, r.x), dy = fsub(bq.y, r.y), dz = fsub(bq.z, r.z);
+	const float dr2 = fadd(fadd(fmul(dx, dx), fmul(dy, dy)), fmul(dz, dz));
+	RefTerms& T = ref_terms(W);
+	/* trec 0: no parameters (the reference would index before its table) */
+	if (dr2 > nl.dPlateau2 || trec == 0) {
+		T.flags[b] = 0;
+		return;
+	}
 	const bool shape86 = P.potshape == GBA_POTSHAPE_8_6;
 	const bool cdiel = P.dielec == GBA_DIELEC_CONSTANT;
-	float ax = 0.f, ay = 0.f, az = 0.f, ae = 0.f;
-	for (uint32_t k = 0; k < num; ++k) {
-		const uint32_t ent = __ldg(&lst[base + k]);
-		const uint32_t j = typed ? ent & 0xffffffu : ent;
-		const float4 r = __ldg(&M.rec.xyzq[j]);
-		float dx = fsub(px, r.x), dy = fsub(py, r.y), dz = fsub(pz, r.z);
-		const float dr2 = fadd(fadd(fmul(dx, dx), fmul(dy, dy)), fmul(dz, dz));
-		if (dr2 > nl.dPlateau2) continue;
-		const uint32_t trec = typed ? ent >> 24 : __ldg(&M.rec.tm[j]) & 0xffffu;
-		if (trec == 0) continue;   /* no parameters (the reference would index before its table) */
-		/* (float)(1.0 / (double)dr2): double rounding is harmless here, so
-		 * this is the correctly rounded float reciprocal */
-		const float dr2_inv = __frcp_rn(dr2);
-		dx = fmul(dx, dr2_inv); dy = fmul(dy, dr2_inv); dz = fmul(dz, dr2_inv);
-		const size_t kp = (size_t)P.num_types * (trec - 1) + (tlig - 1);
-		const float4 p = __ldg(&P.lj[kp]);
-		const float ivor = __ldg(&P.ivor[kp]);
-		float fx, fy, fz, e;
-		ref_lj(dr2, dr2_inv, dx, dy, dz, p, ivor, shape86, fx, fy, fz, e);
-		ax = fadd(ax, fx); ay = fadd(ay, fy); az = fadd(az, fz); ae = fadd(ae, e);
-		const float ratio = __ldg(&nl.ratio[(int)fmul(dr2, 10000.0f)]);
-		const float rdx = fmul(ratio, dx), rdy = fmul(ratio, dy), rdz = fmul(ratio, dz);
-		ref_lj(nl.dPlateau2, nl.dPlateau2_inv, rdx, rdy, rdz, p, ivor, shape86, fx, fy, fz, e);
-		ax = fsub(ax, fx); ay = fsub(ay, fy); az = fsub(az, fz); ae = fsub(ae, e);
-		const float qq = fmul(fmul(qlig, r.w), P.ffelec);
-		if ((double)fabsf(qq) > 0.001) {
-			ref_coulomb(dr2_inv, dx, dy, dz, qq, cdiel, fx, fy, fz, e);
-			ax = fadd(ax, fx); ay = fadd(ay, fy); az = fadd(az, fz); ae = fadd(ae, e);
-			ref_coulomb(nl.dPlateau2_inv, rdx, rdy, rdz, qq, cdiel, fx, fy, fz, e);
-			ax = fsub(ax, fx); ay = fsub(ay, fy); az = fsub(az, fz); ae = fsub(ae, e);
+	/* (float)(1.0 / (double)dr2): double rounding is harmless here, so this
+	 * is the correctly rounded float reciprocal */
+	const float inv = __frcp_rn(dr2);
+	dx = fmul(dx, inv); dy = fmul(dy, inv); dz = fmul(dz, inv);
+	const size_t kp = (size_t)P.num_types * (trec - 1) + (tlig - 1);
+	const float4 p = __ldg(&P.lj[kp]);
+	const float ivor = __ldg(&P.ivor[kp]);
+	const float ratio = __ldg(&nl.ratio[(int)fmul(dr2, 10000.0f)]);
+	float4 t;
+	ref_lj(dr2, inv, dx, dy, dz, p, ivor, shape86, t.x, t.y, t.z, t.w);
+	T.t[b][0] = t;
+	const float rdx = fmul(ratio, dx), rdy = fmul(ratio, dy), rdz = fmul(ratio, dz);
+	ref_lj(nl.dPlateau2, nl.dPlateau2_inv, rdx, rdy, rdz, p, ivor, shape86, t.x, t.y, t.z, t.w);
+	T.t[b][1] = t;
+	const float qq = fmul(fmul(bq.w, r.w), P.ffelec);
+	/* fabs(qq) > 0.001 in double: 0.001f is the first float above 0.001 */
+	const bool charged = fabsf(qq) >= 0.001f;
+	if (charged) {
+		ref_coulomb(inv, dx, dy, dz, qq, cdiel, t.x, t.y, t.z, t.w);
+		T.t[b][2] = t;
+		ref_coulomb(nl.dPlateau2_inv, rdx, rdy, rdz, qq, cdiel, t.x, t.y, t.z, t.w);
+		T.t[b][3] = t;
+	}
+	T.flags[b] = charged ? 3u : 1u;
+}
+
+/* Folds the window's pairs [lo, hi) (positions from the window start wb)
+ * into a bead's neighbour-list accumulator in list order. */
+__device__ __forceinline__ void ref_fold(const RefTerms& T, uint32_t lo, uint32_t hi, float4& a) {
+	for (uint32_t k = lo; k < hi; ++k) {
+		const uint32_t f = T.flags[k];
+		if (!(f & 1u)) continue;
+		const float4 t0 = T.t[k][0], t1 = T.t[k][1];
+		a.x = fadd(a.x, t0.x); a.y = fadd(a.y, t0.y); a.z = fadd(a.z, t0.z); a.w = fadd(a.w, t0.w);
+		a.x = fsub(a.x, t1.x); a.y = fsub(a.y, t1.y); a.z = fsub(a.z, t1.z); a.w = fsub(a.w, t1.w);
+		if (f & 2u) {
+			const float4 t2 = T.t[k][2], t3 = T.t[k][3];
+			a.x = fadd(a.x, t2.x); a.y = fadd(a.y, t2.y); a.z = fadd(a.z, t2.z); a.w = fadd(a.w, t2.w);
+			a.x = fsub(a.x, t3.x); a.y = fsub(a.y, t3.y); a.z = fsub(a.z, t3.z); a.w = fsub(a.w, t3.w);
 		}
 	}
-	return make_float4(ax, ay, az, ae);
 }
 
 /* One round in the reference's order: for each of the 64 staged beads its
  * total (fx, fy, fz, E) -- grid term, plus the neighbour-list term for beads
  * that looked it up -- parked in the slot's first four weight floats
- * (W.cw[9 s .. 9 s + 3], free once the bead's grid term is done). */
+ * (W.cw[9 s .. 9 s + 3]).  The pair sub-terms are computed by the whole warp
+ * over the round's flattened pair list, 32 pairs at a time (every lane busy,
+ * which matters for the double-precision steps on GB300's narrow FP64 pipe),
+ * and each bead's lane then adds its pairs' sub-terms in list order. */
 __device__ __forceinline__ void eval_round_ref(const RigidModel& M, uint32_t i0, int lane, WarpStage& W) {
 	float ttx, tty, ttz;
 	const PoseRot R = get_pose(W, ttx, tty, ttz);
+	float4 pot[2], acc[2];
+	uint32_t nln[2];
+	bool in_nl[2];
 #pragma unroll
 	for (int h = 0; h < 2; ++h) {
 		const int s = lane + 32 * h;
 		const uint32_t i = i0 + s;
+		pot[h] = make_float4(0.f, 0.f, 0.f, 0.f);
+		acc[h] = make_float4(0.f, 0.f, 0.f, 0.f);
+		nln[h] = 0;
+		in_nl[h] = false;
 		if (i >= M.lig.n) continue;
 		const float4 b = __ldg(&M.lig.xyzq[i]);
 		const uint32_t tm = __ldg(&M.lig.tm[i]);
@@ -858,28 +907,56 @@ __device__ __forceinline__ void eval_round_ref(const RigidModel& M, uint32_t i0,
 		put_bead(W, s, b.x, b.y, b.z, px, py, pz, b.w, type);
 		BeadGrid bg{0u, 0u};
 		const uint32_t nlk = stage_grid(M.grid, px, py, pz, mapped, b.w, s, W, bg);
-		float* cw = W.cw + kCornerStride * s;
-		float4 pot = make_float4(0.f, 0.f, 0.f, 0.f);
+		const float* cw = W.cw + kCornerStride * s;
 		if (nlk > 0) {
 			const DevIntrpl& g = (bg.t & 0x80000000u) ? M.grid.outer : M.grid.inner;
-			pot = ref_channel(g, bg.t & 0x7fffffffu, cw);
+			pot[h] = ref_channel(g, bg.t & 0x7fffffffu, cw);
 			if (nlk > 1) {
 				float4 el = ref_channel(g, bg.q & 0x7fffffffu, cw);
 				el.x = fmul(el.x, b.w); el.y = fmul(el.y, b.w); el.z = fmul(el.z, b.w); el.w = fmul(el.w, b.w);
-				pot.x = fadd(pot.x, el.x); pot.y = fadd(pot.y, el.y); pot.z = fadd(pot.z, el.z);
-				pot.w = fadd(pot.w, el.w);
+				pot[h].x = fadd(pot[h].x, el.x); pot[h].y = fadd(pot[h].y, el.y);
+				pot[h].z = fadd(pot[h].z, el.z); pot[h].w = fadd(pot[h].w, el.w);
 			}
 		}
-		if (type != 0) {
-			bool in_nl = false;
-			const uint32_t num = stage_nl(M.grid.nl, px, py, pz, s, W, in_nl);
-			if (in_nl) {
-				const float4 a = ref_nl_bead(M, px, py, pz, b.w, type, W.lbase[s], num);
-				pot.x = fadd(pot.x, a.x); pot.y = fadd(pot.y, a.y); pot.z = fadd(pot.z, a.z);
-				pot.w = fadd(pot.w, a.w);
+		if (type != 0) nln[h] = stage_nl(M.grid.nl, px, py, pz, s, W, in_nl[h]);
+	}
+	uint32_t start[2];
+	const uint32_t n_pair = queue_pairs(W, nln, lane, start);
+	__syncwarp();   /* weights read, list bases final: the overlay may be written */
+
+	const uint32_t* lst = M.grid.nl.typed_list ? M.grid.nl.typed_list : M.grid.nl.list;
+	PairWindow win;
+	for (uint32_t w = 0; w < n_pair; w += 64) {
+		uint32_t sa, sb, ea = 0, eb = 0;
+		win.owners(W, w, start, nln, lane, sa, sb);
+		if (w + lane < n_pair) ea = __ldg(&lst[W.lbase[sa] + w + lane]);
+		if (w + 32 + lane < n_pair) eb = __ldg(&lst[W.lbase[sb] + w + 32 + lane]);
+#pragma unroll
+		for (int half = 0; half < 2; ++half) {
+			const uint32_t wb = w + 32 * half;
+			if (wb >= n_pair) break;
+			if (wb + lane < n_pair) ref_pair_terms(M, W, half ? sb : sa, half ? eb : ea, lane);
+			__syncwarp();
+			const uint32_t we = min(wb + 32, n_pair);
+#pragma unroll
+			for (int h = 0; h < 2; ++h) {
+				const uint32_t lo = max(start[h], wb), hi = min(start[h] + nln[h], we);
+				if (lo < hi) ref_fold(ref_terms(W), lo - wb, hi - wb, acc[h]);
 			}
+			__syncwarp();
 		}
-		cw[0] = pot.x; cw[1] = pot.y; cw[2] = pot.z; cw[3] = pot.w;
+	}
+#pragma unroll
+	for (int h = 0; h < 2; ++h) {
+		const int s = lane + 32 * h;
+		if (i0 + s >= M.lig.n) continue;
+		float4 v = pot[h];
+		if (in_nl[h]) {
+			v.x = fadd(v.x, acc[h].x); v.y = fadd(v.y, acc[h].y); v.z = fadd(v.z, acc[h].z);
+			v.w = fadd(v.w, acc[h].w);
+		}
+		float* cw = W.cw + kCornerStride * s;
+		cw[0] = v.x; cw[1] = v.y; cw[2] = v.z; cw[3] = v.w;
 	}
 	__syncwarp();
 }

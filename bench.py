@@ -286,7 +286,9 @@ def bench_minimization(ctx, pkg, nthreads: int, with_cpu: bool, kopts: int = 15)
     CPU oracle's VA13 on all host threads, with the agreement of the minimized
     energies; and the batched form in the reference's summation order
     (GBA_KOPT_REFERENCE_ORDER), its cost and its bitwise equality with the
-    oracle taking correctly rounded sin/cos."""
+    oracle taking correctly rounded sin/cos -- and, with the host C library's
+    sin/cos tabulated (gba_set_host_sincos), with the oracle as the reference
+    runs it."""
     import torch
     wl = pkg.synth.make_config(0)
     rec, lig, par = ctx.upload_protein(wl.rec), ctx.upload_protein(wl.lig), ctx.upload_params(wl.params)
@@ -316,7 +318,18 @@ def bench_minimization(ctx, pkg, nthreads: int, with_cpu: bool, kopts: int = 15)
     t0 = time.perf_counter()
     ro = ctx.minimize_6d(*ids, wl.dofs, max_evals=steps)
     dt_ro = time.perf_counter() - t0
+    # and with the host C library's sin/cos: the reference's values on this host
+    t0 = time.perf_counter()
+    ctx.set_host_sincos(4096.0)
+    out["host_sincos_table_s"] = time.perf_counter() - t0
+    ctx.minimize_6d(*ids, wl.dofs[:128], max_evals=steps)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    rh = ctx.minimize_6d(*ids, wl.dofs, max_evals=steps)
+    dt_rh = time.perf_counter() - t0
+    ctx.set_host_sincos(0)
     ctx.set_kernel_options(kopts)
+    out["reference_order_host_sincos_poses_per_s"] = n / dt_rh
     out["reference_order_poses_per_s"] = n / dt_ro
     out["reference_order_time_ratio"] = dt_ro / dt_dev
     out["speedup_vs_plain_one_launch"] = out["batched_device_poses_per_s"] / out["plain_one_launch_per_round_poses_per_s"]
@@ -325,7 +338,7 @@ def bench_minimization(ctx, pkg, nthreads: int, with_cpu: bool, kopts: int = 15)
         from oracle import pyoracle as po
         gh = ctx.download_grid(grid)
         t0 = time.perf_counter()
-        _, r_cpu, _ = po.minimize_6d(wl.rec, wl.lig, gh, wl.params, wl.dofs, steps, nthreads=nthreads)
+        s_cpu, r_cpu, n_cpu = po.minimize_6d(wl.rec, wl.lig, gh, wl.params, wl.dofs, steps, nthreads=nthreads)
         dt = time.perf_counter() - t0
         rel = np.abs(r_dev[:, 0].astype(np.float64) - r_cpu[:, 0]) / np.maximum(np.abs(r_cpu[:, 0]), 1e-3)
         out["cpu_oracle_poses_per_s"] = n / dt
@@ -340,6 +353,10 @@ def bench_minimization(ctx, pkg, nthreads: int, with_cpu: bool, kopts: int = 15)
         out["oracle_self_agreement_one_ulp_start"] = float(np.mean(rel <= 1e-3))
         rel = np.abs(ro[1][:, 0].astype(np.float64) - r_cpu[:, 0]) / np.maximum(np.abs(r_cpu[:, 0]), 1e-3)
         out["reference_order_agreement_within_1e-3"] = float(np.mean(rel <= 1e-3))
+        rel = np.abs(rh[1][:, 0].astype(np.float64) - r_cpu[:, 0]) / np.maximum(np.abs(r_cpu[:, 0]), 1e-3)
+        out["reference_order_host_sincos_agreement_within_1e-3"] = float(np.mean(rel <= 1e-3))
+        out["reference_order_host_sincos_bitwise_equal_oracle"] = bool(
+            np.array_equal(rh[0], s_cpu) and np.array_equal(rh[1], r_cpu) and np.array_equal(rh[2], n_cpu))
         with po.exact_sincos():
             x = po.minimize_6d(wl.rec, wl.lig, gh, wl.params, wl.dofs, steps, nthreads=nthreads)
         out["reference_order_bitwise_equal_exact_sincos_oracle"] = bool(

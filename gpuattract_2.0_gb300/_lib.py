@@ -96,6 +96,7 @@ def load() -> C.CDLL:
         "gba_set_pose_order": ([P, I], I),
         "gba_kernel_timing": ([P, C.c_int32], I),
         "gba_set_kernel_options": ([P, C.c_uint32], I),
+        "gba_set_host_sincos": ([P, C.c_float], I),
         "gba_energy_6d_noalloc": ([P, U32, U32, U32, U32, P, SZ, P, P], I),
         "gba_allocation_count": ([C.POINTER(C.c_uint64)], I),
         "gba_kernel_time": ([P, C.POINTER(C.c_double), C.POINTER(C.c_uint64), C.c_int32], I),

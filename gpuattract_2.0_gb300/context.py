@@ -327,6 +327,11 @@ class GbaContext:
         bit the reference's results, slower); the default is 15."""
         self._check(self.lib.gba_set_kernel_options(self.h, int(flags)))
 
+    def set_host_sincos(self, max_abs: float = 4096.0):
+        """Take each angle's sin/cos from this process's C library (sinf/cosf),
+        tabulated on the device for |angle| in [2^-12, max_abs); 0 turns it off."""
+        self._check(self.lib.gba_set_host_sincos(self.h, float(max_abs)))
+
     def kernel_timing(self, enable: bool):
         """Record CUDA events around every fused rigid energy kernel launch."""
         self._check(self.lib.gba_kernel_timing(self.h, int(bool(enable))))

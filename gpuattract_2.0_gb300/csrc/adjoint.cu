@@ -190,7 +190,7 @@ __global__ void __launch_bounds__(kPairwiseThreads) pairwise_kernel(const Pairwi
 		float c[6];
 #pragma unroll
 		for (int k = 0; k < 6; ++k) c[k] = __shfl_sync(GBA_FULL_MASK, dv, k);
-		const PoseRot R = pose_rotation(c[3], c[4], c[5], lane);
+		const PoseRot R = pose_rotation(c[3], c[4], c[5], lane, DevTrig{nullptr, 0u, 0u});
 		const float w = BACKWARD ? __ldg(&L.gE[p]) : 0.f;
 		float sE = 0.f, sFx = 0.f, sFy = 0.f, sFz = 0.f;
 		float Tq[9] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};

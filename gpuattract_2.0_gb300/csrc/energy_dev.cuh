@@ -9,7 +9,8 @@
  * sets are bit-identical to the reference CPU path.  The rotation angles go
  * through double-precision sincos rounded to float: the correctly rounded
  * value, which glibc's sinf/cosf return for all but about 1% of arguments
- * (where they are off by one ulp).  The smooth arithmetic after those
+ * (where they are off by one ulp) -- or, with gba_set_host_sincos, the host
+ * C library's own sinf/cosf values read from a table.  The smooth arithmetic after those
  * decisions (trilinear sums, pair terms, reductions) may fuse.
  */
 #ifndef GBA_ENERGY_DEV_CUH_
@@ -45,14 +46,26 @@ struct PoseRot {
 	float cphi, sphi, cssi, sssi, crot, srot;
 };
 
-/* Lanes 0..2 each take one Euler angle (phi, ssi, rot) through double sincos;
- * the 6 values are broadcast and combined as euler2rotmat does
+/* Lanes 0..2 each take one Euler angle (phi, ssi, rot) through double sincos
+ * -- or, for angles the host table T covers, the host C library's sinf/cosf
+ * read from it; the 6 values are broadcast and combined as euler2rotmat does
  * (src/model/matrixFunctions.h:40-77), unfused. */
-__device__ __forceinline__ PoseRot pose_rotation(float phi, float ssi, float rot, int lane) {
+__device__ __forceinline__ PoseRot pose_rotation(float phi, float ssi, float rot, int lane, const DevTrig& T) {
 	float a = lane == 0 ? phi : (lane == 1 ? ssi : rot);
-	double sd = 0.0, cd = 1.0;
-	if (lane < 3) sincos((double)a, &sd, &cd);
-	float s = (float)sd, c = (float)cd;
+	float s = 0.f, c = 1.f;
+	if (lane < 3) {
+		const uint32_t b = __float_as_uint(a), mag = b & 0x7fffffffu;
+		if (T.sc && mag >= T.lo && mag < T.hi) {
+			const float2 v = __ldg(&T.sc[(size_t)(b >> 31) * (T.hi - T.lo) + (mag - T.lo)]);
+			s = v.x;
+			c = v.y;
+		} else {
+			double sd, cd;
+			sincos((double)a, &sd, &cd);
+			s = (float)sd;
+			c = (float)cd;
+		}
+	}
 	PoseRot R;
 	R.cphi = __shfl_sync(GBA_FULL_MASK, c, 0);
 	R.sphi = __shfl_sync(GBA_FULL_MASK, s, 0);

@@ -129,7 +129,8 @@ struct ModesFrame {
 /* Lane k (k < 26) brings the k-th float of the DOF_6D_Modes record; every
  * lane gets the frame and the amplitudes. */
 template <int MM>
-__device__ __forceinline__ ModesFrame modes_frame(const float dv, const int lane, float ampR[MM], float ampL[MM]) {
+__device__ __forceinline__ ModesFrame modes_frame(const float dv, const int lane, float ampR[MM], float ampL[MM],
+		const DevTrig& T) {
 	ModesFrame F;
 	F.t[0] = __shfl_sync(GBA_FULL_MASK, dv, 0);
 	F.t[1] = __shfl_sync(GBA_FULL_MASK, dv, 1);
@@ -142,7 +143,7 @@ __device__ __forceinline__ ModesFrame modes_frame(const float dv, const int lane
 		ampR[m] = __shfl_sync(GBA_FULL_MASK, dv, 6 + m);
 		ampL[m] = __shfl_sync(GBA_FULL_MASK, dv, 16 + m);
 	}
-	F.R = pose_rotation(a0, a1, a2, lane);
+	F.R = pose_rotation(a0, a1, a2, lane, T);
 	const PoseRot& R = F.R;
 	/* R(-ang): same sin/cos with the sines negated (exact sign flips) */
 	{
@@ -412,7 +413,7 @@ template <int MM>
 __device__ __forceinline__ float eval_pose_modes(const ModesLaunch& L, const float dv, const int lane,
 		WarpStage& W, ModeStage<MM>& MS) {
 	float ampR[MM], ampL[MM];
-	const ModesFrame F = modes_frame<MM>(dv, lane, ampR, ampL);
+	const ModesFrame F = modes_frame<MM>(dv, lane, ampR, ampL, L.trig);
 	float gRr[MM], gRn[MM], gL[MM];
 #pragma unroll
 	for (int m = 0; m < MM; ++m) { gRr[m] = 0.f; gRn[m] = 0.f; gL[m] = 0.f; }
@@ -456,7 +457,7 @@ __global__ void __launch_bounds__(kModesRecThreads, kModesRecBlocks) modes_rec_k
 		const float* d = reinterpret_cast<const float*>(L.dofs + p);
 		const float dv = lane < 26 ? __ldg(d + lane) : 0.f;
 		float ampR[MM], ampL[MM];
-		const ModesFrame F = modes_frame<MM>(dv, lane, ampR, ampL);
+		const ModesFrame F = modes_frame<MM>(dv, lane, ampR, ampL, L.trig);
 		float gR[MM];
 #pragma unroll
 		for (int m = 0; m < MM; ++m) gR[m] = 0.f;
@@ -481,7 +482,7 @@ __global__ void __launch_bounds__(kModesThreads, 2) modes_lig_kernel(const Modes
 		const float* d = reinterpret_cast<const float*>(L.dofs + p);
 		const float dv = lane < 26 ? __ldg(d + lane) : 0.f;
 		float ampR[MM], ampL[MM];
-		const ModesFrame F = modes_frame<MM>(dv, lane, ampR, ampL);
+		const ModesFrame F = modes_frame<MM>(dv, lane, ampR, ampL, L.trig);
 		float gRr[MM], gRn[MM], gL[MM];
 		const float* o = reinterpret_cast<const float*>(L.out + p);
 #pragma unroll

@@ -663,6 +663,7 @@ RigidLaunch Context::rigid_launch(gba_id rec, gba_id lig, gba_id grid, gba_id pa
 	L.m.grid = apply_kernel_options(G->dev);
 	L.m.par = P->dev;
 	L.m.par.pair = P->pair_table(G->dev.nl.dPlateau2, may_allocate);
+	L.m.trig = trig;
 	L.bound4 = (kernel_opts & GBA_KOPT_FOUR_BLOCKS) ? 1 : 0;
 	L.ref_order = (kernel_opts & GBA_KOPT_REFERENCE_ORDER) ? 1 : 0;
 	if (kernel_opts & GBA_KOPT_TYPED_LIST)
@@ -745,6 +746,7 @@ ModesLaunch Context::modes_launch(gba_id rec, gba_id lig, gba_id grid_rec, gba_i
 	L.grid_lig = apply_kernel_options(GL->dev);
 	L.par = P->dev;
 	L.par.pair = P->pair_table(GR->dev.nl.dPlateau2);
+	L.trig = trig;
 	L.rec_modes = R->dev.modes;
 	L.rec_ms = 3 * R->dev.n_modes;
 	L.lig_modes = Lg->dev.modes;

@@ -267,6 +267,11 @@ struct Context {
 	ModesLaunch modes_launch(gba_id rec, gba_id lig, gba_id grid_rec, gba_id grid_lig, gba_id params);
 	void run_modes(ModesLaunch& L, cudaStream_t s);
 
+	/* the host C library's sin/cos table (gba_set_host_sincos); trig.sc ==
+	 * nullptr: off */
+	DevBuffer trig_table;
+	DevTrig trig{nullptr, 0u, 0u};
+
 	/* GBA_KOPT_* flags (gba_set_kernel_options) and their effect on a grid */
 	uint32_t kernel_opts = GBA_KOPT_DEFAULT;
 	DevGrid apply_kernel_options(DevGrid g) const;

@@ -95,6 +95,14 @@ struct PoseCensus {
 	uint32_t n_grid, n_grid_charged, n_nl, n_nl_entries;
 };
 
+/* The host C library's sinf/cosf, tabulated (gba_set_host_sincos): entry
+ * (sign(a) ? hi - lo : 0) + (|a| bits - lo) holds (sinf(a), cosf(a)) for
+ * every float angle a with |a| bits in [lo, hi).  sc == nullptr: off. */
+struct DevTrig {
+	const float2* sc;
+	uint32_t lo, hi;
+};
+
 /* ---- launch wrappers (energy_rigid.cu) ----------------------------------- */
 
 /* Everything one rigid receptor-ligand pair's evaluation reads. */
@@ -102,6 +110,7 @@ struct RigidModel {
 	DevProtein rec, lig;
 	DevGrid grid;
 	DevParams par;
+	DevTrig trig;
 };
 
 struct RigidLaunch {
@@ -175,6 +184,7 @@ struct ModesLaunch {
 	DevGrid grid_rec;         /* receptor grid: ligand beads + NL */
 	DevGrid grid_lig;         /* ligand grid: receptor beads */
 	DevParams par;
+	DevTrig trig;
 	const float* rec_modes;   /* [i][m][axis] */
 	uint32_t rec_ms;          /* floats per receptor bead record (3*Mr) */
 	const float* lig_modes;

@@ -665,7 +665,7 @@ __device__ __forceinline__ void finish_pose(const WarpStage& W, float res[7]) {
 template <bool CENSUS, bool ROUNDWISE = false>
 __device__ __forceinline__ void eval_pose_rigid(const RigidModel& M, float tx, float ty, float tz,
 		float a0, float a1, float a2, int lane, WarpStage& W, float res[7], PoseCensus* census) {
-	put_pose(W, pose_rotation(a0, a1, a2, lane), tx, ty, tz, lane);
+	put_pose(W, pose_rotation(a0, a1, a2, lane, M.trig), tx, ty, tz, lane);
 	RoundCensus cen;
 	if (ROUNDWISE) {
 		clear_totals(W, lane);
@@ -1001,7 +1001,7 @@ __device__ __forceinline__ void finish_ref(float acc, const WarpStage& W, float 
 /* A whole pose in the reference's order, one warp. */
 __device__ __forceinline__ void eval_pose_rigid_ref(const RigidModel& M, float tx, float ty, float tz,
 		float a0, float a1, float a2, int lane, WarpStage& W, float res[7]) {
-	put_pose(W, pose_rotation(a0, a1, a2, lane), tx, ty, tz, lane);
+	put_pose(W, pose_rotation(a0, a1, a2, lane, M.trig), tx, ty, tz, lane);
 	float acc = 0.f;
 	for (uint32_t i0 = 0; i0 < M.lig.n; i0 += kBeadsPerRound) {
 		eval_round_ref(M, i0, lane, W);
@@ -1030,7 +1030,7 @@ __device__ __forceinline__ void eval_pose_rigid_team(const RigidModel& M, float 
 		int bar_id) {
 	const int nthreads = 32 * G;
 	WarpStage& W = stages[t];
-	if (t == 0) put_pose(W, pose_rotation(a0, a1, a2, lane), tx, ty, tz, lane);
+	if (t == 0) put_pose(W, pose_rotation(a0, a1, a2, lane, M.trig), tx, ty, tz, lane);
 	group_sync(bar_id, nthreads);
 	if (t != 0) {
 		if (lane < 18) W.pose[lane] = stages[0].pose[lane];

@@ -209,6 +209,22 @@ int gba_set_pose_order(gba_ctx* ctx, int enable);
                                  GBA_KOPT_TYPED_LIST)
 int gba_set_kernel_options(gba_ctx* ctx, uint32_t flags);
 
+/* Takes each Euler angle's sine and cosine from this process's C library
+ * (sinf, cosf) -- the values the reference's euler2rotmat / euler2torquemat
+ * receive on this host (src/model/matrixFunctions.h:40-127) -- instead of
+ * computing them correctly rounded on the device.  The library is evaluated
+ * once, on all host threads, for every float angle with magnitude in
+ * [2^-12, max_abs), and the values are kept on the device: 8 bytes per
+ * angle, 3.2 GB for max_abs = 4096 (minimization trajectories reach angles
+ * beyond 100 rad).  Below 2^-12
+ * the correctly rounded values (sin a = a, cos a = 1) are used, as any
+ * faithful library returns; at or beyond max_abs the computed ones.  With
+ * GBA_KOPT_REFERENCE_ORDER the rigid results then equal the reference's on
+ * this host bit for bit.  Applies to every rigid and normal-mode call of the
+ * context.  max_abs = 0 turns it off and frees the table; max_abs above 4096
+ * is rejected.  No reference counterpart. */
+int gba_set_host_sincos(gba_ctx* ctx, float max_abs);
+
 /* While enabled, CUDA events are recorded on the launching stream around
  * every fused rigid energy kernel launch (gba_energy_6d and friends);
  * gba_kernel_time synchronizes on them and returns the summed kernel time

@@ -13,6 +13,9 @@ sin/cos are correctly rounded:
   device VA13 trajectories, evaluation counts and final results equal the
   oracle's minfor driving the same arithmetic, bit for bit, in the
   persistent kernel, the plain per-step form and a multi-pair batch.
+With the host C library's sin/cos tabulated on the device as well
+(gba_set_host_sincos) the device equals the oracle as the reference runs it
+on this host -- libm sin/cos -- on every pose, minimizations included.
 """
 import ctypes as C
 
@@ -157,3 +160,45 @@ def test_batch_minimize_bitwise(pkg, oracle, ctx):
     for g, r in zip(got, refs):
         for a, b in zip(g, r):
             assert np.array_equal(a, b)
+
+
+def test_host_sincos_reproduces_the_reference_on_this_host(pkg, oracle, ctx):
+    """With the host C library's sin/cos tabulated (gba_set_host_sincos), the
+    device takes the very values the reference takes on this host, so the
+    reference order equals the oracle as the reference runs it -- libm
+    sin/cos, no correction -- on every pose: a config-1 sample's energies
+    and config 0's minimizations in full (all three outputs)."""
+    import time
+    t0 = time.perf_counter()
+    # minimization trajectories reach angles beyond 100 rad: the whole
+    # supported range
+    ctx.set_host_sincos(4096.0)
+    print(f"host sin/cos table: {time.perf_counter() - t0:.2f} s")
+    try:
+        wl = pkg.synth.make_config(1)
+        dofs = np.ascontiguousarray(wl.dofs[:2048])
+        rec, lig, par = ctx.upload_protein(wl.rec), ctx.upload_protein(wl.lig), ctx.upload_params(wl.params)
+        gid = ctx.build_grid(rec, par, pkg.GridOptions())
+        host = ctx.download_grid(gid)
+        exact = oracle.libm_sincos_rounds_exactly(dofs[:, 3:6])
+        assert not exact.all()        # the sample does meet misrounded angles
+        assert np.array_equal(ctx.energy_6d(rec, lig, gid, par, dofs),
+                              oracle.energy_6d(wl.rec, wl.lig, host, wl.params, dofs))
+        for i in (gid, lig, rec, par):
+            ctx.release(i)
+
+        wl = pkg.synth.make_config(0)
+        rec, lig, par = ctx.upload_protein(wl.rec), ctx.upload_protein(wl.lig), ctx.upload_params(wl.params)
+        gid = ctx.build_grid(rec, par, pkg.GridOptions())
+        host = ctx.download_grid(gid)
+        dev = ctx.minimize_6d(rec, lig, gid, par, wl.dofs, max_evals=wl.steps)
+        ref = oracle.minimize_6d(wl.rec, wl.lig, host, wl.params, wl.dofs, wl.steps)
+        for a, b, what in zip(dev, ref, ("states", "results", "evaluations")):
+            assert np.array_equal(a, b), what
+        st = oracle.minimization_stats(dev[1], ref[1])
+        print(f"config 0 minimization, reference order + host sin/cos vs the oracle (libm): {st}")
+        assert st["within_tol"] == 1.0
+        for i in (gid, lig, rec, par):
+            ctx.release(i)
+    finally:
+        ctx.set_host_sincos(0)

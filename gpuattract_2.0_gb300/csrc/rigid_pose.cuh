@@ -796,13 +796,19 @@ __device__ __forceinline__ void ref_coulomb(float dr2_inv, float dx, float dy, f
 
 /* The four sub-terms NLPotForce adds for one pair -- LJPotForce at r, at the
  * plateau, ChargePotForce at r, at the plateau -- each (fx, fy, fz, E), for
- * the 32 pairs of a window; flags bit 0: the pair is within the plateau,
- * bit 1: its charge product passes the Coulomb test.  Overlaid on the
- * staging area's corner weights and lookup queue, which the reference order
- * does not use once the round's grid terms are taken. */
+ * the 32 pairs of a window (flags bit 0: the pair is within the plateau,
+ * bit 1: its charge product passes the Coulomb test); the neighbour-list
+ * accumulator of each of the round's 64 beads, component c in acc[s][c];
+ * and the window's segments (runs of pairs of one bead): first position and
+ * bead slot of segment j.  Overlaid on the staging area's corner weights and
+ * lookup queue, which the reference order does not use once the round's grid
+ * terms are taken. */
 struct RefTerms {
 	float4 t[32][4];
 	uint32_t flags[32];
+	float acc[64][4];
+	uint8_t seg_pos[33];
+	uint8_t seg_slot[32];
 };
 static_assert(sizeof(RefTerms) <= sizeof(WarpStage::cw) + sizeof(WarpStage::look), "RefTerms overlay");
 static_assert(offsetof(WarpStage, look) == offsetof(WarpStage, cw) + sizeof(WarpStage::cw), "RefTerms overlay");
@@ -859,20 +865,38 @@ __device__ __forceinline__ void ref_pair_terms(const RigidModel& M, WarpStage& W
 	T.flags[b] = charged ? 3u : 1u;
 }
 
-/* Folds the window's pairs [lo, hi) (positions from the window start wb)
- * into a bead's neighbour-list accumulator in list order. */
-__device__ __forceinline__ void ref_fold(const RefTerms& T, uint32_t lo, uint32_t hi, float4& a) {
-	for (uint32_t k = lo; k < hi; ++k) {
-		const uint32_t f = T.flags[k];
-		if (!(f & 1u)) continue;
-		const float4 t0 = T.t[k][0], t1 = T.t[k][1];
-		a.x = fadd(a.x, t0.x); a.y = fadd(a.y, t0.y); a.z = fadd(a.z, t0.z); a.w = fadd(a.w, t0.w);
-		a.x = fsub(a.x, t1.x); a.y = fsub(a.y, t1.y); a.z = fsub(a.z, t1.z); a.w = fsub(a.w, t1.w);
-		if (f & 2u) {
-			const float4 t2 = T.t[k][2], t3 = T.t[k][3];
-			a.x = fadd(a.x, t2.x); a.y = fadd(a.y, t2.y); a.z = fadd(a.z, t2.z); a.w = fadd(a.w, t2.w);
-			a.x = fsub(a.x, t3.x); a.y = fsub(a.y, t3.y); a.z = fsub(a.z, t3.z); a.w = fsub(a.w, t3.w);
+/* Folds the n pairs of a window into their beads' accumulators in list
+ * order.  Lane p (p < n) holds the slot of the bead owning pair p.  The
+ * window's segments are numbered; four lanes take a segment, one component
+ * each (the components' sums are independent), eight segments at a time. */
+__device__ __forceinline__ void ref_fold(RefTerms& T, uint32_t n, uint32_t owner, int lane) {
+	const uint32_t prev = __shfl_up_sync(GBA_FULL_MASK, owner, 1);
+	const bool start = (uint32_t)lane < n && (lane == 0 || owner != prev);
+	const uint32_t starts = __ballot_sync(GBA_FULL_MASK, start);
+	const uint32_t nseg = __popc(starts);
+	if (start) {
+		const uint32_t j = __popc(starts & ((1u << lane) - 1u));
+		T.seg_pos[j] = (uint8_t)lane;
+		T.seg_slot[j] = (uint8_t)owner;
+	}
+	if (lane == 0) T.seg_pos[nseg] = (uint8_t)n;
+	__syncwarp();
+	const int c = lane & 3;
+	for (uint32_t j = lane >> 2; j < nseg; j += 8) {
+		const uint32_t lo = T.seg_pos[j], hi = T.seg_pos[j + 1], sl = T.seg_slot[j];
+		float a = T.acc[sl][c];
+		for (uint32_t k = lo; k < hi; ++k) {
+			const uint32_t f = T.flags[k];
+			if (!(f & 1u)) continue;
+			const float* t = reinterpret_cast<const float*>(T.t[k]);
+			a = fadd(a, t[c]);
+			a = fsub(a, t[4 + c]);
+			if (f & 2u) {
+				a = fadd(a, t[8 + c]);
+				a = fsub(a, t[12 + c]);
+			}
 		}
+		T.acc[sl][c] = a;
 	}
 }
 
@@ -882,11 +906,12 @@ __device__ __forceinline__ void ref_fold(const RefTerms& T, uint32_t lo, uint32_
  * (W.cw[9 s .. 9 s + 3]).  The pair sub-terms are computed by the whole warp
  * over the round's flattened pair list, 32 pairs at a time (every lane busy,
  * which matters for the double-precision steps on GB300's narrow FP64 pipe),
- * and each bead's lane then adds its pairs' sub-terms in list order. */
+ * and the sub-terms are then added to each bead's accumulator in list order,
+ * four lanes per bead, one per component (ref_fold). */
 __device__ __forceinline__ void eval_round_ref(const RigidModel& M, uint32_t i0, int lane, WarpStage& W) {
 	float ttx, tty, ttz;
 	const PoseRot R = get_pose(W, ttx, tty, ttz);
-	float4 pot[2], acc[2];
+	float4 pot[2];
 	uint32_t nln[2];
 	bool in_nl[2];
 #pragma unroll
@@ -894,7 +919,6 @@ __device__ __forceinline__ void eval_round_ref(const RigidModel& M, uint32_t i0,
 		const int s = lane + 32 * h;
 		const uint32_t i = i0 + s;
 		pot[h] = make_float4(0.f, 0.f, 0.f, 0.f);
-		acc[h] = make_float4(0.f, 0.f, 0.f, 0.f);
 		nln[h] = 0;
 		in_nl[h] = false;
 		if (i >= M.lig.n) continue;
@@ -923,6 +947,11 @@ __device__ __forceinline__ void eval_round_ref(const RigidModel& M, uint32_t i0,
 	uint32_t start[2];
 	const uint32_t n_pair = queue_pairs(W, nln, lane, start);
 	__syncwarp();   /* weights read, list bases final: the overlay may be written */
+	RefTerms& T = ref_terms(W);
+	if (n_pair > 0) {
+#pragma unroll
+		for (int k = 0; k < 8; ++k) (&T.acc[0][0])[lane + 32 * k] = 0.f;
+	}
 
 	const uint32_t* lst = M.grid.nl.typed_list ? M.grid.nl.typed_list : M.grid.nl.list;
 	PairWindow win;
@@ -937,15 +966,18 @@ __device__ __forceinline__ void eval_round_ref(const RigidModel& M, uint32_t i0,
 			if (wb >= n_pair) break;
 			if (wb + lane < n_pair) ref_pair_terms(M, W, half ? sb : sa, half ? eb : ea, lane);
 			__syncwarp();
-			const uint32_t we = min(wb + 32, n_pair);
-#pragma unroll
-			for (int h = 0; h < 2; ++h) {
-				const uint32_t lo = max(start[h], wb), hi = min(start[h] + nln[h], we);
-				if (lo < hi) ref_fold(ref_terms(W), lo - wb, hi - wb, acc[h]);
-			}
+			ref_fold(T, min(n_pair - wb, 32u), half ? sb : sa, lane);
 			__syncwarp();
 		}
 	}
+	float4 acc[2];
+#pragma unroll
+	for (int h = 0; h < 2; ++h) {
+		const int s = lane + 32 * h;
+		acc[h] = n_pair > 0 ? make_float4(T.acc[s][0], T.acc[s][1], T.acc[s][2], T.acc[s][3])
+		                    : make_float4(0.f, 0.f, 0.f, 0.f);
+	}
+	__syncwarp();   /* accumulators read: the totals may overwrite them */
 #pragma unroll
 	for (int h = 0; h < 2; ++h) {
 		const int s = lane + 32 * h;

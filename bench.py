@@ -391,9 +391,12 @@ def modes_roofline(ctx, wl, gr, gl, n: int, launch_s: float):
 
 
 def bench_modes(ctx, pkg, n_poses: int, steps: int, minimize: bool = True, with_cpu: bool = True,
-                small: bool = False):
+                small: bool = False, kopts: int = 15):
     """Config 2: receptor 1500 / ligand 600 beads with 5 modes each: modes
-    energy+gradient evals/s, and (minimize) device vs plain minimization."""
+    energy+gradient evals/s, and (minimize) device vs plain minimization; the
+    scoring in the reference's summation order, and (minimize, with_cpu) a
+    64-pose minimization in that order with the host's sin/cos against the
+    oracle."""
     import torch
     if small:
         c = pkg.synth.CONFIGS[2]
@@ -418,6 +421,17 @@ def bench_modes(ctx, pkg, n_poses: int, steps: int, minimize: bool = True, with_
     torch.cuda.synchronize()
     launch_s = e0.elapsed_time(e1) / 1000.0 / 3
     evals = len(wl.dofs) / launch_s
+    ctx.set_kernel_options(kopts | KOPT_REFERENCE_ORDER)
+    ro_out = ctx.energy_6d_modes(*ids, d)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    ctx.energy_6d_modes(*ids, d, out=ro_out, stream=stream.cuda_stream)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ctx.set_kernel_options(kopts)
+    reference_order = {"evals_per_s": len(wl.dofs) / (e0.elapsed_time(e1) / 1000.0),
+                       "time_ratio": e0.elapsed_time(e1) / 1000.0 / launch_s}
+    del ro_out
     roof = None
     if with_cpu:
         roof = modes_roofline(ctx, wl, gr, gl, len(wl.dofs), launch_s)
@@ -426,7 +440,7 @@ def bench_modes(ctx, pkg, n_poses: int, steps: int, minimize: bool = True, with_
             ctx.release(i)
         return {"workload": f"config 2{' distributions' if small else ''}: receptor {wl.rec.n} / ligand "
                             f"{wl.lig.n} beads, 5+5 modes; {len(wl.dofs)} poses scored", "energy_evals_per_s": evals,
-                "roofline": roof}
+                "roofline": roof, "reference_order": reference_order}
     sub = wl.dofs
     ctx.minimize_6d_modes(*ids, sub[:64], max_evals=10)
     t0 = time.perf_counter()
@@ -462,7 +476,29 @@ def bench_modes(ctx, pkg, n_poses: int, steps: int, minimize: bool = True, with_
            # FP32 resolution of the DOFs (the reference minimizer stalls the same way)
            "ended_at_start_energy_fraction": float(np.mean(r1[:, 0] == e0)),
            "final_nan_fraction": float(np.mean(~np.isfinite(r1[:, 0]))),
-           "start_no_contact_fraction": float(np.mean(e0 == 0))}
+           "start_no_contact_fraction": float(np.mean(e0 == 0)),
+           "reference_order": reference_order}
+    if with_cpu:
+        # the reference's order with the host's sin/cos against the oracle as
+        # the reference runs it (libm sin/cos), 64 poses
+        from oracle import pyoracle as po
+        few = np.ascontiguousarray(sub[:64])
+        ctx.set_kernel_options(kopts | KOPT_REFERENCE_ORDER)
+        ctx.set_host_sincos(4096.0)
+        ctx.minimize_6d_modes(*ids, few[:8], max_evals=10)
+        t0 = time.perf_counter()
+        dev = ctx.minimize_6d_modes(*ids, few, max_evals=steps)
+        dt = time.perf_counter() - t0
+        ctx.set_host_sincos(0)
+        ctx.set_kernel_options(kopts)
+        hr, hl = ctx.download_grid(gr), ctx.download_grid(gl)
+        ref = po.minimize_6d_modes(wl.rec, wl.lig, hr, hl, wl.params, few, steps)
+        reference_order.update({
+            "minimize_sample_poses": len(few), "minimize_poses_per_s": len(few) / dt,
+            "minimize_bitwise_equal_oracle": bool(all(np.array_equal(a, b, equal_nan=True)
+                                                      for a, b in zip(dev, ref))),
+            "minimize_agreement_within_1e-3": po.minimization_stats(dev[1], ref[1])["within_tol"],
+            "minimize_default_order_agreement_within_1e-3": po.minimization_stats(r1[:64], ref[1])["within_tol"]})
     for i in (gr, gl, lig, rec, par):
         ctx.release(i)
     return res
@@ -658,8 +694,9 @@ def run_modes_only(args):
     pkg = __graft_entry__.load_package()
     from gbattract.context import GbaContext
     ctx = GbaContext(0)
+    ctx.set_kernel_options(args.kopts)
     res = bench_modes(ctx, pkg, n_poses=args.modes_poses, steps=200, minimize=not args.no_min,
-                      with_cpu=not args.no_cpu, small=args.modes_small)
+                      with_cpu=not args.no_cpu, small=args.modes_small, kopts=args.kopts)
     ctx.close()
     print(json.dumps({"suite": {"modes": res}}))
     return 0
@@ -887,7 +924,8 @@ def main():
     suite = {}
     if rank == 0 and not args.no_suite:
         ctx.grid_octets(grid, False)
-        suite["modes"] = bench_modes(ctx, pkg, n_poses=args.modes_poses, steps=200, with_cpu=not args.no_cpu)
+        suite["modes"] = bench_modes(ctx, pkg, n_poses=args.modes_poses, steps=200, with_cpu=not args.no_cpu,
+                                     kopts=args.kopts)
         suite["adjoint"] = bench_adjoint(ctx, pkg, n_poses=10000)
 
     if rank == 0:

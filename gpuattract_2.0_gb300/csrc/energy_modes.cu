@@ -425,12 +425,261 @@ __device__ __forceinline__ float eval_pose_modes(const ModesLaunch& L, const flo
 	return modes_epilogue<MM>(L, F, S, C, gL, gRr, gRn, lane);
 }
 
+/* ---- the reference CPU path's order (GBA_KOPT_REFERENCE_ORDER) ----------
+ *
+ * CPUEnergyService6DModes evaluates a pose array by array
+ * (src/service/CPUEnergyService6DModes.tpp:121-327): the receptor deformed
+ * and moved into the ligand frame, its grid forces (ligand grid) rotated back
+ * per bead; the ligand deformed and moved, its grid forces (receptor grid);
+ * the NL term bead by bead in list order, adding each pair's four sub-terms
+ * to the ligand bead and their reaction to the receptor bead; then sums in
+ * bead order: energy and force, the ligand mode projections of R^T f, the
+ * receptor mode projections, correctModeForce, the torque.  The rigid
+ * reference order's pieces (ref_grid_term, ref_pair_terms, ref_fold,
+ * ref_accumulate) follow it operation for operation; the receptor bead
+ * forces need a per-pose array (scratch in global memory, one per warp,
+ * float4 per receptor bead), and each receptor reaction is added to it in
+ * the reference's pair order by three lanes, one per component. */
+
+/* Receptor bead index of each window position (the reactions' scatter). */
+struct RefModesExtra {
+	uint32_t j[32];
+};
+
+/* x^4 correctly rounded, standing in for std::pow(x, 4) of
+ * correctModeForce: x^2 = p + e and p^2 = hi + lo exactly (Dekker's
+ * products through fma), x^4 = hi + (lo + 2 p e + e^2). */
+__device__ __forceinline__ double pow4_rn(double x) {
+	const double p = __dmul_rn(x, x);
+	const double e = __fma_rn(x, x, -p);
+	const double hi = __dmul_rn(p, p);
+	const double lo = __fma_rn(p, p, -hi);
+	return __dadd_rn(hi, __fma_rn(__dmul_rn(2.0, p), e, __fma_rn(e, e, lo)));
+}
+
+/* One pose in the reference's order; rf: this warp's receptor array.  Lane
+ * k (k < 26) brings the k-th float of the DOF_6D_Modes record; returns on
+ * lane k (k < 27) the k-th float of the Result_6D_Modes record. */
+template <int MM>
+__device__ __forceinline__ float eval_pose_modes_ref(const ModesLaunch& L, const float dv, const int lane,
+		WarpStage& W, RefModesExtra& X, float4* __restrict__ rf) {
+	const uint32_t Mr = L.rec.n_modes, Ml = L.lig.n_modes;
+	const float tx = __shfl_sync(GBA_FULL_MASK, dv, 0);
+	const float ty = __shfl_sync(GBA_FULL_MASK, dv, 1);
+	const float tz = __shfl_sync(GBA_FULL_MASK, dv, 2);
+	const float a0 = __shfl_sync(GBA_FULL_MASK, dv, 3);
+	const float a1 = __shfl_sync(GBA_FULL_MASK, dv, 4);
+	const float a2 = __shfl_sync(GBA_FULL_MASK, dv, 5);
+	float ampR[MM], ampL[MM];
+#pragma unroll
+	for (int m = 0; m < MM; ++m) {
+		ampR[m] = __shfl_sync(GBA_FULL_MASK, dv, 6 + m);
+		ampL[m] = __shfl_sync(GBA_FULL_MASK, dv, 16 + m);
+	}
+	const PoseRot R0 = pose_rotation(a0, a1, a2, lane, L.trig);
+
+	/* receptor: invertDOF (src/model/transform_modes.h:27-41) -- R(-ang)
+	 * from the sin/cos of the negated angles, t' = R^T (-t) -- then per bead
+	 * the ligand-grid force rotated back by R */
+	{
+		const PoseRot Rn = pose_rotation(-a0, -a1, -a2, lane, L.trig);
+		const float ipx = fadd(fadd(fmul(R0.m[0], -tx), fmul(R0.m[3], -ty)), fmul(R0.m[6], -tz));
+		const float ipy = fadd(fadd(fmul(R0.m[1], -tx), fmul(R0.m[4], -ty)), fmul(R0.m[7], -tz));
+		const float ipz = fadd(fadd(fmul(R0.m[2], -tx), fmul(R0.m[5], -ty)), fmul(R0.m[8], -tz));
+		for (uint32_t j0 = 0; j0 < L.rec.n; j0 += kBeadsPerRound) {
+#pragma unroll
+			for (int h = 0; h < 2; ++h) {
+				const int s = lane + 32 * h;
+				const uint32_t j = j0 + s;
+				if (j >= L.rec.n) continue;
+				const float4 r = __ldg(&L.rec.xyzq[j]);
+				const uint32_t mapped = __ldg(&L.rec.tm[j]) >> 16;
+				float x = r.x, y = r.y, z = r.z;
+				deform<MM>(L.rec_modes + (size_t)j * L.rec_ms, Mr, ampR, x, y, z);
+				float px, py, pz;
+				rot_apply(Rn.m, x, y, z, px, py, pz);
+				px = fadd(px, ipx); py = fadd(py, ipy); pz = fadd(pz, ipz);
+				const float4 pot = ref_grid_term(L.grid_lig, px, py, pz, mapped, r.w, s, W);
+				float fx, fy, fz;
+				rot_apply(R0.m, pot.x, pot.y, pot.z, fx, fy, fz);
+				rf[j] = make_float4(fx, fy, fz, 0.f);
+			}
+		}
+	}
+	__syncwarp();
+
+	/* ligand: grid term, NL term with the receptor reactions, sums in bead
+	 * order -- lanes 0..12 energy, force, torque; lanes 16 + m the ligand
+	 * mode projections */
+	const uint32_t* lst = L.grid_rec.nl.typed_list ? L.grid_rec.nl.typed_list : L.grid_rec.nl.list;
+	const bool typed = L.grid_rec.nl.typed_list != nullptr;
+	float acc = 0.f;
+	for (uint32_t i0 = 0; i0 < L.lig.n; i0 += kBeadsPerRound) {
+		float4 pot[2];
+		uint32_t nln[2];
+		bool in_nl[2];
+#pragma unroll
+		for (int h = 0; h < 2; ++h) {
+			const int s = lane + 32 * h;
+			const uint32_t i = i0 + s;
+			pot[h] = make_float4(0.f, 0.f, 0.f, 0.f);
+			nln[h] = 0;
+			in_nl[h] = false;
+			if (i >= L.lig.n) continue;
+			const float4 b = __ldg(&L.lig.xyzq[i]);
+			const uint32_t tm = __ldg(&L.lig.tm[i]);
+			const uint32_t type = tm & 0xffffu, mapped = tm >> 16;
+			float x = b.x, y = b.y, z = b.z;
+			deform<MM>(L.lig_modes + (size_t)i * L.lig_ms, Ml, ampL, x, y, z);
+			float px, py, pz;
+			rot_apply(R0.m, x, y, z, px, py, pz);
+			px = fadd(px, tx); py = fadd(py, ty); pz = fadd(pz, tz);
+			put_bead(W, s, b.x, b.y, b.z, px, py, pz, b.w, type);
+			pot[h] = ref_grid_term(L.grid_rec, px, py, pz, mapped, b.w, s, W);
+			if (type != 0) nln[h] = stage_nl(L.grid_rec.nl, px, py, pz, s, W, in_nl[h]);
+		}
+		uint32_t start[2];
+		const uint32_t n_pair = queue_pairs(W, nln, lane, start);
+		__syncwarp();   /* weights read, list bases final: the overlay may be written */
+		RefTerms& T = ref_terms(W);
+		if (n_pair > 0) {
+#pragma unroll
+			for (int k = 0; k < 8; ++k) (&T.acc[0][0])[lane + 32 * k] = 0.f;
+		}
+		PairWindow win;
+		for (uint32_t w = 0; w < n_pair; w += 64) {
+			uint32_t sa, sb, ea = 0, eb = 0;
+			win.owners(W, w, start, nln, lane, sa, sb);
+			if (w + lane < n_pair) ea = __ldg(&lst[W.lbase[sa] + w + lane]);
+			if (w + 32 + lane < n_pair) eb = __ldg(&lst[W.lbase[sb] + w + 32 + lane]);
+#pragma unroll
+			for (int half = 0; half < 2; ++half) {
+				const uint32_t wb = w + 32 * half;
+				if (wb >= n_pair) break;
+				if (wb + lane < n_pair) {
+					const uint32_t ent = half ? eb : ea;
+					const uint32_t j = typed ? ent & 0xffffffu : ent;
+					const uint32_t trec = typed ? ent >> 24 : __ldg(&L.rec.tm[j]) & 0xffffu;
+					const float4 r = __ldg(&L.rec.xyzq[j]);
+					float rx = r.x, ry = r.y, rz = r.z;
+					deform<MM>(L.rec_modes + (size_t)j * L.rec_ms, Mr, ampR, rx, ry, rz);
+					ref_pair_terms(L.grid_rec.nl, L.par, W, half ? sb : sa, make_float4(rx, ry, rz, r.w), trec,
+							lane);
+					X.j[lane] = j;
+				}
+				__syncwarp();
+				const uint32_t n = min(n_pair - wb, 32u);
+				ref_fold(T, n, half ? sb : sa, lane);
+				/* each pair's reaction on its receptor bead (0 - LJ(r) + LJ(plateau)
+				 * [- Coulomb(r) + Coulomb(plateau)]), added pair by pair */
+				if (lane < 3) {
+					for (uint32_t k = 0; k < n; ++k) {
+						const uint32_t f = T.flags[k];
+						if (!(f & 1u)) continue;
+						const float* t = reinterpret_cast<const float*>(T.t[k]);
+						float v = fsub(0.f, t[lane]);
+						v = fadd(v, t[4 + lane]);
+						if (f & 2u) {
+							v = fsub(v, t[8 + lane]);
+							v = fadd(v, t[12 + lane]);
+						}
+						float* d = reinterpret_cast<float*>(rf + X.j[k]) + lane;
+						*d = fadd(*d, v);
+					}
+				}
+				__syncwarp();
+			}
+		}
+		float4 a[2];
+#pragma unroll
+		for (int h = 0; h < 2; ++h) {
+			const int s = lane + 32 * h;
+			a[h] = n_pair > 0 ? make_float4(T.acc[s][0], T.acc[s][1], T.acc[s][2], T.acc[s][3])
+			                  : make_float4(0.f, 0.f, 0.f, 0.f);
+		}
+		__syncwarp();   /* accumulators read: the totals may overwrite them */
+#pragma unroll
+		for (int h = 0; h < 2; ++h) {
+			const int s = lane + 32 * h;
+			if (i0 + s >= L.lig.n) continue;
+			float4 v = pot[h];
+			if (in_nl[h]) {
+				v.x = fadd(v.x, a[h].x); v.y = fadd(v.y, a[h].y); v.z = fadd(v.z, a[h].z); v.w = fadd(v.w, a[h].w);
+			}
+			float* cw = W.cw + kCornerStride * s;
+			cw[0] = v.x; cw[1] = v.y; cw[2] = v.z; cw[3] = v.w;
+		}
+		__syncwarp();
+		const uint32_t nb = min((uint32_t)kBeadsPerRound, L.lig.n - i0);
+		acc = ref_accumulate(W, nb, lane, acc);
+		if (lane >= 16 && (uint32_t)(lane - 16) < Ml) {
+			/* reduceModeForce with rotation (src/model/reduction_modes.h:29-57):
+			 * -= (R^T f) . v */
+			const int m = lane - 16;
+			for (uint32_t s = 0; s < nb; ++s) {
+				const float* f = W.cw + kCornerStride * s;
+				float ox, oy, oz;
+				rot_apply_t(R0.m, f[0], f[1], f[2], ox, oy, oz);
+				const float* v = L.lig_modes + (size_t)(i0 + s) * L.lig_ms + 3 * m;
+				acc = fsub(acc, fadd(fadd(fmul(ox, __ldg(v)), fmul(oy, __ldg(v + 1))), fmul(oz, __ldg(v + 2))));
+			}
+		}
+		__syncwarp();
+	}
+	float c[13];
+#pragma unroll
+	for (int k = 0; k < 13; ++k) c[k] = __shfl_sync(GBA_FULL_MASK, acc, k);
+	float gL[MM], gR[MM];
+#pragma unroll
+	for (int m = 0; m < MM; ++m) gL[m] = __shfl_sync(GBA_FULL_MASK, acc, 16 + m);
+	/* reduceModeForce without rotation over the receptor forces, bead order */
+	float g = 0.f;
+	if ((uint32_t)lane < Mr) {
+		for (uint32_t j = 0; j < L.rec.n; ++j) {
+			const float4 f = rf[j];
+			const float* v = L.rec_modes + (size_t)j * L.rec_ms + 3 * lane;
+			g = fsub(g, fadd(fadd(fmul(f.x, __ldg(v)), fmul(f.y, __ldg(v + 1))), fmul(f.z, __ldg(v + 2))));
+		}
+	}
+#pragma unroll
+	for (int m = 0; m < MM; ++m) gR[m] = __shfl_sync(GBA_FULL_MASK, g, m);
+	__syncwarp();   /* rf read: the next pose may overwrite it */
+	float sFx = c[1], sFy = c[2], sFz = c[3];
+	force_lim(sFx, sFy, sFz);
+	float ang[3];
+	torque_reduce(R0, c + 4, ang);
+	/* correctModeForce (src/model/reduction_modes.h:101-115):
+	 * delta + (float)((double)(4 k) * pow(delta, 4)) */
+#pragma unroll
+	for (int m = 0; m < MM; ++m) {
+		if (m < (int)Mr)
+			gR[m] = fadd(gR[m], (float)__dmul_rn((double)fmul(4.0f, L.rec.mode_force[m]), pow4_rn((double)gR[m])));
+		if (m < (int)Ml)
+			gL[m] = fadd(gL[m], (float)__dmul_rn((double)fmul(4.0f, L.lig.mode_force[m]), pow4_rn((double)gL[m])));
+	}
+	float v = 0.f;
+	if (lane == 0) v = c[0];
+	else if (lane == 1) v = sFx;
+	else if (lane == 2) v = sFy;
+	else if (lane == 3) v = sFz;
+	else if (lane == 4) v = ang[0];
+	else if (lane == 5) v = ang[1];
+	else if (lane == 6) v = ang[2];
+#pragma unroll
+	for (int m = 0; m < MM; ++m) {
+		if (lane == 7 + m) v = m < (int)Mr ? gR[m] : 0.f;
+		if (lane == 17 + m) v = m < (int)Ml ? gL[m] : 0.f;
+	}
+	return v;
+}
+
 namespace {
 
 constexpr int kModesThreads = 256;       /* ligand-pass scoring kernel's block */
 constexpr int kModesRecThreads = 128;    /* receptor-pass kernel: block, */
 constexpr int kModesRecBlocks = 5;       /* resident blocks per SM (shared memory allows five) */
 constexpr int kModesMinThreads = 128;    /* minimizer kernel block */
+constexpr int kModesRefThreads = 128;    /* reference-order scoring kernel block */
 
 /* mode capacity compiled for a launch: 5 or GBA_MODES_MAX */
 int mode_capacity(const ModesLaunch& L) {
@@ -500,6 +749,24 @@ __global__ void __launch_bounds__(kModesThreads, 2) modes_lig_kernel(const Modes
 	}
 }
 
+/* GBA_KOPT_REFERENCE_ORDER scoring: a warp takes whole poses
+ * (eval_pose_modes_ref) with its own receptor array in L.ref_rf. */
+template <int MM>
+__global__ void __launch_bounds__(kModesRefThreads) modes_ref_kernel(const ModesLaunch L) {
+	__shared__ WarpStage stage[kModesRefThreads / 32];
+	__shared__ RefModesExtra extra[kModesRefThreads / 32];
+	const int lane = threadIdx.x & 31;
+	const int wib = threadIdx.x >> 5;
+	float4* rf = L.ref_rf + (((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * L.rec.n;
+	PoseFeed feed(L.next);
+	for (size_t p = feed.take(lane); p < L.n; p = feed.take(lane)) {
+		const float* d = reinterpret_cast<const float*>(L.dofs + p);
+		const float dv = lane < 26 ? __ldg(d + lane) : 0.f;
+		const float v = eval_pose_modes_ref<MM>(L, dv, lane, stage[wib], extra[wib], rf);
+		if (lane < 27) reinterpret_cast<float*>(L.out + p)[lane] = v;
+	}
+}
+
 /* Persistent VA13 over (ang xyz, pos xyz, modesRec[0..Mr), modesLig[0..Ml)):
  * the minimizer of minimize.cu generalised to 6 + Mr + Ml DOF (minfor.f is
  * fixed at 6, src/apps/em/minfor.f:16,33). */
@@ -509,7 +776,7 @@ __device__ __forceinline__ unsigned long long modes_global_ns() {
 	return t;
 }
 
-template <int MM>
+template <int MM, bool REF>
 __global__ void __launch_bounds__(kModesMinThreads) minimize_modes_kernel(const ModesMinLaunch M) {
 	__shared__ WarpStage stage[kModesMinThreads / 32];
 	ModeStage<MM>* ms = reinterpret_cast<ModeStage<MM>*>(modes_dyn_smem);
@@ -565,7 +832,11 @@ __global__ void __launch_bounds__(kModesMinThreads) minimize_modes_kernel(const 
 				const float t = __shfl_sync(GBA_FULL_MASK, lane == 0 ? rec[k] : 0.f, 0);
 				if (lane == k) dv = t;
 			}
-			v = eval_pose_modes<MM>(L, dv, lane, stage[wib], ms[wib]);
+			if (REF)
+				v = eval_pose_modes_ref<MM>(L, dv, lane, stage[wib], *reinterpret_cast<RefModesExtra*>(&ms[wib]),
+						L.ref_rf + (((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * L.rec.n);
+			else
+				v = eval_pose_modes<MM>(L, dv, lane, stage[wib], ms[wib]);
 			++nev;
 			/* gather the result record on lane 0 */
 			float res[27];
@@ -636,38 +907,66 @@ cudaError_t launch_modes_mm(const ModesLaunch& L, int num_sms, cudaStream_t s) {
 }
 
 template <int MM>
-cudaError_t launch_min_mm(const ModesMinLaunch& M, int blocks, int threads, cudaStream_t s) {
-	const size_t dyn = mode_stage_bytes<MM>(threads);
-	cudaError_t e = allow_smem(minimize_modes_kernel<MM>, dyn);
-	if (e != cudaSuccess) return e;
-	minimize_modes_kernel<MM><<<blocks, threads, dyn, s>>>(M);
-	return cudaGetLastError();
+size_t ref_blocks_mm(const ModesLaunch& L, int num_sms) {
+	const size_t want = (L.n + kModesRefThreads / 32 - 1) / (kModesRefThreads / 32);
+	return std::max<size_t>(1, std::min<size_t>(want,
+			(size_t)num_sms * resident_blocks(modes_ref_kernel<MM>, kModesRefThreads, 0)));
 }
 
 template <int MM>
+cudaError_t launch_ref_mm(const ModesLaunch& L, int num_sms, cudaStream_t s) {
+	modes_ref_kernel<MM><<<(unsigned)ref_blocks_mm<MM>(L, num_sms), kModesRefThreads, 0, s>>>(L);
+	return cudaGetLastError();
+}
+
+template <int MM, bool REF>
+cudaError_t launch_min_mm(const ModesMinLaunch& M, int blocks, int threads, cudaStream_t s) {
+	const size_t dyn = mode_stage_bytes<MM>(threads);
+	cudaError_t e = allow_smem(minimize_modes_kernel<MM, REF>, dyn);
+	if (e != cudaSuccess) return e;
+	minimize_modes_kernel<MM, REF><<<blocks, threads, dyn, s>>>(M);
+	return cudaGetLastError();
+}
+
+template <int MM, bool REF>
 int min_bps_mm(int threads) {
 	const size_t dyn = mode_stage_bytes<MM>(threads);
-	if (allow_smem(minimize_modes_kernel<MM>, dyn) != cudaSuccess) return 1;
+	if (allow_smem(minimize_modes_kernel<MM, REF>, dyn) != cudaSuccess) return 1;
 	int nb = 0;
-	cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, minimize_modes_kernel<MM>, threads, dyn);
+	cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, minimize_modes_kernel<MM, REF>, threads, dyn);
 	return nb > 0 ? nb : 1;
 }
 
 }  // namespace
 
 cudaError_t launch_modes_energy(const ModesLaunch& L, int num_sms, cudaStream_t s) {
+	if (L.ref_order) {
+		if (!L.ref_rf) return cudaErrorInvalidValue;
+		return mode_capacity(L) == 5 ? launch_ref_mm<5>(L, num_sms, s) : launch_ref_mm<GBA_MODES_MAX>(L, num_sms, s);
+	}
 	return mode_capacity(L) == 5 ? launch_modes_mm<5>(L, num_sms, s)
 	                             : launch_modes_mm<GBA_MODES_MAX>(L, num_sms, s);
 }
 
+size_t modes_ref_warps(const ModesLaunch& L, int num_sms) {
+	const size_t blocks = mode_capacity(L) == 5 ? ref_blocks_mm<5>(L, num_sms)
+	                                            : ref_blocks_mm<GBA_MODES_MAX>(L, num_sms);
+	return blocks * (kModesRefThreads / 32);
+}
+
 cudaError_t launch_minimize_modes(const ModesMinLaunch& M, int blocks, int threads, cudaStream_t s) {
-	if (threads != kModesMinThreads) return cudaErrorInvalidValue;
-	return mode_capacity(M.m) == 5 ? launch_min_mm<5>(M, blocks, threads, s)
-	                               : launch_min_mm<GBA_MODES_MAX>(M, blocks, threads, s);
+	if (threads != kModesMinThreads || (M.m.ref_order && !M.m.ref_rf)) return cudaErrorInvalidValue;
+	if (M.m.ref_order)
+		return mode_capacity(M.m) == 5 ? launch_min_mm<5, true>(M, blocks, threads, s)
+		                               : launch_min_mm<GBA_MODES_MAX, true>(M, blocks, threads, s);
+	return mode_capacity(M.m) == 5 ? launch_min_mm<5, false>(M, blocks, threads, s)
+	                               : launch_min_mm<GBA_MODES_MAX, false>(M, blocks, threads, s);
 }
 
 int minimize_modes_blocks_per_sm(int threads, const ModesLaunch& L) {
-	return mode_capacity(L) == 5 ? min_bps_mm<5>(threads) : min_bps_mm<GBA_MODES_MAX>(threads);
+	if (L.ref_order)
+		return mode_capacity(L) == 5 ? min_bps_mm<5, true>(threads) : min_bps_mm<GBA_MODES_MAX, true>(threads);
+	return mode_capacity(L) == 5 ? min_bps_mm<5, false>(threads) : min_bps_mm<GBA_MODES_MAX, false>(threads);
 }
 
 }  // namespace gba

@@ -747,6 +747,7 @@ ModesLaunch Context::modes_launch(gba_id rec, gba_id lig, gba_id grid_rec, gba_i
 	L.par = P->dev;
 	L.par.pair = P->pair_table(GR->dev.nl.dPlateau2);
 	L.trig = trig;
+	L.ref_order = (kernel_opts & GBA_KOPT_REFERENCE_ORDER) ? 1 : 0;
 	L.rec_modes = R->dev.modes;
 	L.rec_ms = 3 * R->dev.n_modes;
 	L.lig_modes = Lg->dev.modes;
@@ -758,6 +759,8 @@ void Context::run_modes(ModesLaunch& L, cudaStream_t s) {
 	StreamScratch scratch(scratch_pool);
 	L.next = (unsigned long long*)scratch.get(2 * sizeof(unsigned long long), s);
 	L.next2 = L.next + 1;
+	if (L.ref_order)
+		L.ref_rf = (float4*)scratch.get(modes_ref_warps(L, num_sms) * std::max<uint32_t>(1, L.rec.n) * sizeof(float4), s);
 	check_cuda(cudaMemsetAsync(L.next, 0, 2 * sizeof(unsigned long long), s), "modes energy: pose counters");
 	check_cuda(launch_modes_energy(L, num_sms, s), "modes energy launch");
 }

@@ -194,11 +194,16 @@ struct ModesLaunch {
 	size_t n;
 	unsigned long long* next; /* pose counters, zero at launch (PoseFeed): receptor pass, */
 	unsigned long long* next2;/* ligand pass; nullptr: fixed stride */
+	int ref_order;            /* GBA_KOPT_REFERENCE_ORDER: the reference CPU path's order */
+	float4* ref_rf;           /* with ref_order: rec.n float4 per launched warp (modes_ref_warps) */
 };
 
 /* the two scoring kernels (receptor pass, then ligand pass), each grid sized
  * to its own occupancy on num_sms SMs */
 cudaError_t launch_modes_energy(const ModesLaunch& L, int num_sms, cudaStream_t s);
+/* warps the reference-order scoring launch uses for L (its scratch: that many
+ * times rec.n float4) */
+size_t modes_ref_warps(const ModesLaunch& L, int num_sms);
 
 struct ModesMinLaunch {
 	ModesLaunch m;                  /* model fields; dofs/out/n unused */

@@ -643,6 +643,10 @@ int gba_minimize_6d_modes(gba_ctx* ctx, gba_id rec, gba_id lig, gba_id grid_rec,
 	const int bps = minimize_modes_blocks_per_sm(threads, M.m);
 	size_t blocks = std::max<size_t>(1, std::min<size_t>((n * 32 + threads - 1) / threads,
 			(size_t)ctx->num_sms * bps));
+	StreamScratch scratch(ctx->scratch_pool);
+	if (M.m.ref_order)   /* the reference order's receptor arrays, one per warp */
+		M.m.ref_rf = (float4*)scratch.get(blocks * (threads / 32) * std::max<uint32_t>(1, M.m.rec.n) *
+				sizeof(float4), s);
 	check_cuda(launch_minimize_modes(M, (int)blocks, threads, s), "modes minimize launch");
 	if (!dev) {
 		copy_out(out_state, M.out_state, n * sizeof(gba_dof6d_modes), s);

@@ -748,6 +748,29 @@ __device__ __forceinline__ float4 ref_channel(const DevIntrpl& g, uint32_t elem,
 			fmul(o.w, g.voxelVol_inv));
 }
 
+/* potForce of one bead at (px, py, pz) staged in slot s (its corner weights
+ * go to the slot): the type channel, plus the charge channel times q when
+ * |q| > 0.001, summed as interpolate does (src/model/interpolation.h:27-53);
+ * zero outside both grids or for mapped type 0. */
+__device__ __forceinline__ float4 ref_grid_term(const DevGrid& G, float px, float py, float pz, uint32_t mapped,
+		float q, int s, WarpStage& W) {
+	BeadGrid bg{0u, 0u};
+	const uint32_t nlk = stage_grid(G, px, py, pz, mapped, q, s, W, bg);
+	float4 pot = make_float4(0.f, 0.f, 0.f, 0.f);
+	if (nlk > 0) {
+		const float* cw = W.cw + kCornerStride * s;
+		const DevIntrpl& g = (bg.t & 0x80000000u) ? G.outer : G.inner;
+		pot = ref_channel(g, bg.t & 0x7fffffffu, cw);
+		if (nlk > 1) {
+			float4 el = ref_channel(g, bg.q & 0x7fffffffu, cw);
+			el.x = fmul(el.x, q); el.y = fmul(el.y, q); el.z = fmul(el.z, q); el.w = fmul(el.w, q);
+			pot.x = fadd(pot.x, el.x); pot.y = fadd(pot.y, el.y); pot.z = fadd(pot.z, el.z);
+			pot.w = fadd(pot.w, el.w);
+		}
+	}
+	return pot;
+}
+
 /* LJPotForce (swi = 1) as the reference computes it: the force factor in
  * double, rounded to float. */
 __device__ __forceinline__ void ref_lj(float dr2, float dr2_inv, float dx, float dy, float dz, const float4 p,
@@ -816,17 +839,11 @@ static_assert(offsetof(WarpStage, cw) % 16 == 0, "RefTerms overlay");
 
 __device__ __forceinline__ RefTerms& ref_terms(WarpStage& W) { return *reinterpret_cast<RefTerms*>(W.cw); }
 
-/* The sub-terms of one pair -- ligand bead staged in slot sl, list entry ent
- * -- into window position b (the loop body of NLPotForce,
- * src/model/neighborlist.h:70-158). */
-__device__ __forceinline__ void ref_pair_terms(const RigidModel& M, WarpStage& W, uint32_t sl, uint32_t ent,
-		int b) {
-	const DevNL& nl = M.grid.nl;
-	const DevParams& P = M.par;
-	const bool typed = nl.typed_list != nullptr;
-	const uint32_t j = typed ? ent & 0xffffffu : ent;
-	const float4 r = __ldg(&M.rec.xyzq[j]);
-	const uint32_t trec = typed ? ent >> 24 : __ldg(&M.rec.tm[j]) & 0xffffu;
+/* The sub-terms of one pair -- ligand bead staged in slot sl, receptor bead
+ * at r (x, y, z, charge) of type trec -- into window position b (the loop
+ * body of NLPotForce, src/model/neighborlist.h:70-158). */
+__device__ __forceinline__ void ref_pair_terms(const DevNL& nl, const DevParams& P, WarpStage& W, uint32_t sl,
+		const float4 r, uint32_t trec, int b) {
 	const float4 bq = W.pq[sl];
 	const uint32_t tlig = __float_as_uint(W.ut[sl].w);
 	float dx = fsub(bq.x, r.x), dy = fsub(bq.y, r.y), dz = fsub(bq.z, r.z);
@@ -929,19 +946,7 @@ __device__ __forceinline__ void eval_round_ref(const RigidModel& M, uint32_t i0,
 		rot_apply(R.m, b.x, b.y, b.z, px, py, pz);
 		px = fadd(px, ttx); py = fadd(py, tty); pz = fadd(pz, ttz);
 		put_bead(W, s, b.x, b.y, b.z, px, py, pz, b.w, type);
-		BeadGrid bg{0u, 0u};
-		const uint32_t nlk = stage_grid(M.grid, px, py, pz, mapped, b.w, s, W, bg);
-		const float* cw = W.cw + kCornerStride * s;
-		if (nlk > 0) {
-			const DevIntrpl& g = (bg.t & 0x80000000u) ? M.grid.outer : M.grid.inner;
-			pot[h] = ref_channel(g, bg.t & 0x7fffffffu, cw);
-			if (nlk > 1) {
-				float4 el = ref_channel(g, bg.q & 0x7fffffffu, cw);
-				el.x = fmul(el.x, b.w); el.y = fmul(el.y, b.w); el.z = fmul(el.z, b.w); el.w = fmul(el.w, b.w);
-				pot[h].x = fadd(pot[h].x, el.x); pot[h].y = fadd(pot[h].y, el.y);
-				pot[h].z = fadd(pot[h].z, el.z); pot[h].w = fadd(pot[h].w, el.w);
-			}
-		}
+		pot[h] = ref_grid_term(M.grid, px, py, pz, mapped, b.w, s, W);
 		if (type != 0) nln[h] = stage_nl(M.grid.nl, px, py, pz, s, W, in_nl[h]);
 	}
 	uint32_t start[2];
@@ -964,7 +969,13 @@ __device__ __forceinline__ void eval_round_ref(const RigidModel& M, uint32_t i0,
 		for (int half = 0; half < 2; ++half) {
 			const uint32_t wb = w + 32 * half;
 			if (wb >= n_pair) break;
-			if (wb + lane < n_pair) ref_pair_terms(M, W, half ? sb : sa, half ? eb : ea, lane);
+			if (wb + lane < n_pair) {
+				const uint32_t ent = half ? eb : ea;
+				const bool typed = M.grid.nl.typed_list != nullptr;
+				const uint32_t j = typed ? ent & 0xffffffu : ent;
+				const uint32_t trec = typed ? ent >> 24 : __ldg(&M.rec.tm[j]) & 0xffffu;
+				ref_pair_terms(M.grid.nl, M.par, W, half ? sb : sa, __ldg(&M.rec.xyzq[j]), trec, lane);
+			}
 			__syncwarp();
 			ref_fold(T, min(n_pair - wb, 32u), half ? sb : sa, lane);
 			__syncwarp();

@@ -13,6 +13,8 @@
 #ifndef GBA_VA13_CUH_
 #define GBA_VA13_CUH_
 
+#include <cmath>
+
 #ifdef __CUDACC__
 #define GBA_HD __host__ __device__ __forceinline__
 #else
@@ -31,9 +33,14 @@
 
 namespace gba {
 
-GBA_HD double va_max(double a, double b) { return a > b ? a : b; }
-GBA_HD double va_min(double a, double b) { return a < b ? a : b; }
-GBA_HD double va_abs(double a) { return a < 0 ? -a : a; }
+/* max, min and abs with the C++ library's semantics (std::max(a, b) =
+ * a < b ? b : a, std::min(a, b) = b < a ? b : a, fabs clears the sign bit),
+ * which decide what a NaN or a signed zero does: a pose whose energy
+ * overflows hands the machine NaN gradients, and every form of the
+ * minimizer must take the same branch on them. */
+GBA_HD double va_max(double a, double b) { return a < b ? b : a; }
+GBA_HD double va_min(double a, double b) { return b < a ? b : a; }
+GBA_HD double va_abs(double a) { return fabs(a); }
 
 /* Products are never contracted with a following add: the host build runs
  * with -ffp-contract=off and the device uses round-to-nearest multiplies, so

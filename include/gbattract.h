@@ -192,12 +192,15 @@ int gba_set_pose_order(gba_ctx* ctx, int enable);
  *                            bit for bit wherever its sin/cos are correctly
  *                            rounded.  Reads the ratio table and the
  *                            native lookups whatever the other options say.
- *                            Slower (a lane walks a bead's list alone);
- *                            applies to gba_energy_6d, the noalloc
- *                            and batch scoring calls, both minimizer forms
- *                            (one warp per pose: no teams), not to
- *                            gba_census_6d or the normal-mode calls.  Off by
- *                            default.
+ *                            Slower; applies to gba_energy_6d, the
+ *                            noalloc and batch scoring calls, both minimizer
+ *                            forms (one warp per pose: no teams), and the
+ *                            normal-mode scoring and minimizers
+ *                            (CPUEnergyService6DModes,
+ *                            src/service/CPUEnergyService6DModes.tpp:121-327;
+ *                            a per-warp receptor array of 16 B per receptor
+ *                            bead in call scratch); not to gba_census_6d.
+ *                            Off by default.
  * The default is the first four.  Changing options drops the cached
  * minimizer graphs. */
 #define GBA_KOPT_RATIO_COMPUTED 1u

@@ -116,7 +116,10 @@ def modes_synth():
     grid_lig = po.build_grid(wl.lig, wl.params, opts)
     out = po.ref_energy_6d_modes(wl.rec, wl.lig, grid_rec, grid_lig, wl.params, wl.dofs,
                                  nworkers=2, item_size=10)
-    pack("modes_synth", wl.rec, wl.lig, wl.params, opts, wl.dofs, out)
+    # the modes path takes sin/cos of the angles and of their negations (invertDOF)
+    ang = np.ascontiguousarray(wl.dofs[:, 3:6])
+    exact = sincos_mask(wl.dofs) & po.libm_sincos_rounds_exactly(-ang)
+    pack("modes_synth", wl.rec, wl.lig, wl.params, opts, wl.dofs, out, dict(sincos_exact=exact))
 
 
 if __name__ == "__main__":

@@ -16,6 +16,9 @@ sin/cos are correctly rounded:
 With the host C library's sin/cos tabulated on the device as well
 (gba_set_host_sincos) the device equals the oracle as the reference runs it
 on this host -- libm sin/cos -- on every pose, minimizations included.
+The normal-mode path (CPUEnergyService6DModes,
+src/service/CPUEnergyService6DModes.tpp:121-327) likewise: the reference's
+modes fixture, a config-2 sample, config-2 minimizations over 16 DOF.
 """
 import ctypes as C
 
@@ -202,3 +205,72 @@ def test_host_sincos_reproduces_the_reference_on_this_host(pkg, oracle, ctx):
             ctx.release(i)
     finally:
         ctx.set_host_sincos(0)
+
+
+def _modes_ids(ctx, pkg, wl, octets=False):
+    rec, lig, par = ctx.upload_protein(wl.rec), ctx.upload_protein(wl.lig), ctx.upload_params(wl.params)
+    gr = ctx.build_grid(rec, par, pkg.GridOptions())
+    gl = ctx.build_grid(lig, par, pkg.GridOptions())
+    for g in (gr, gl):
+        ctx.grid_octets(g, octets)
+    return (rec, lig, gr, gl, par), ctx.download_grid(gr), ctx.download_grid(gl)
+
+
+def test_modes_equals_reference_outputs(golden_cases, oracle, ctx):
+    """The modes fixture (the reference's CPUEnergyService6DModes outputs):
+    bit for bit on every pose whose angles and negated angles the generating
+    host's libm rounded correctly; the correctly-rounded oracle on all."""
+    d = golden_cases["modes_synth"]
+    rec, lig, params, opts = golden_inputs(d)
+    gr, gl = oracle.build_grid(rec, params, opts), oracle.build_grid(lig, params, opts)
+    ids = (ctx.upload_protein(rec), ctx.upload_protein(lig), ctx.upload_grid(gr), ctx.upload_grid(gl),
+           ctx.upload_params(params))
+    got = ctx.energy_6d_modes(*ids, d["dofs"])
+    exact = d["sincos_exact"].astype(bool)
+    with oracle.exact_sincos():
+        ref_x = oracle.energy_6d_modes(rec, lig, gr, gl, params, d["dofs"])
+    assert np.array_equal(got[exact], d["ref_out"][exact])
+    assert np.array_equal(got, ref_x)
+    for i in ids:
+        ctx.release(i)
+
+
+def test_modes_config2_sample_bitwise(pkg, oracle, ctx):
+    """Receptor 1500 / ligand 600 beads with 5 + 5 modes, 256 of config 2's
+    poses, device-built grids with their octet copies."""
+    wl = pkg.synth.make_config(2, n_poses=256)
+    ids, hr, hl = _modes_ids(ctx, pkg, wl, octets=True)
+    got = ctx.energy_6d_modes(*ids, wl.dofs)
+    with oracle.exact_sincos():
+        ref = oracle.energy_6d_modes(wl.rec, wl.lig, hr, hl, wl.params, wl.dofs)
+    assert np.array_equal(got, ref, equal_nan=True)
+    for i in ids:
+        ctx.release(i)
+
+
+def test_modes_minimization_bitwise(pkg, oracle, ctx):
+    """Config 2's modes minimization (16 DOF, maxFunEval 200) on 64 of its
+    poses: device and plain forms equal the correctly-rounded oracle's VA13
+    bit for bit; with the host's sin/cos tabulated, the oracle as the
+    reference runs it."""
+    wl = pkg.synth.make_config(2, n_poses=64)
+    ids, hr, hl = _modes_ids(ctx, pkg, wl)
+    dev = ctx.minimize_6d_modes(*ids, wl.dofs, max_evals=200)
+    plain = ctx.minimize_6d_modes_plain(*ids, wl.dofs, max_evals=200)
+    with oracle.exact_sincos():
+        ref = oracle.minimize_6d_modes(wl.rec, wl.lig, hr, hl, wl.params, wl.dofs, 200)
+    for a, b, c in zip(dev, plain, ref):
+        assert np.array_equal(a, c, equal_nan=True)
+        assert np.array_equal(b, c, equal_nan=True)
+    ctx.set_host_sincos(4096.0)
+    try:
+        dev = ctx.minimize_6d_modes(*ids, wl.dofs, max_evals=200)
+    finally:
+        ctx.set_host_sincos(0)
+    ref = oracle.minimize_6d_modes(wl.rec, wl.lig, hr, hl, wl.params, wl.dofs, 200)
+    for a, c in zip(dev, ref):
+        assert np.array_equal(a, c, equal_nan=True)
+    st = oracle.minimization_stats(dev[1], ref[1])
+    print(f"config 2 minimization sample, reference order + host sin/cos vs the oracle (libm): {st}")
+    for i in ids:
+        ctx.release(i)

@@ -43,6 +43,20 @@ def test_exact_sincos_oracle_bitwise_on_exact_poses(name, golden_cases, oracle):
     assert np.array_equal(got[exact], d["ref_out"][exact])
 
 
+def test_exact_sincos_modes_oracle_bitwise_on_exact_poses(golden_cases, oracle):
+    """The modes path takes sin/cos of each angle and of its negation: where
+    the generating host's libm rounded all of them correctly, the
+    correctly-rounded oracle equals the reference's modes outputs bit for bit."""
+    d = golden_cases["modes_synth"]
+    rec, lig, params, opts = golden_inputs(d)
+    gr, gl = oracle.build_grid(rec, params, opts), oracle.build_grid(lig, params, opts)
+    with oracle.exact_sincos():
+        got = oracle.energy_6d_modes(rec, lig, gr, gl, params, d["dofs"])
+    exact = d["sincos_exact"].astype(bool)
+    assert exact.mean() > 0.85
+    assert np.array_equal(got[exact], d["ref_out"][exact])
+
+
 def test_modes_oracle_matches_reference_fixture(golden_cases, oracle):
     d = golden_cases["modes_synth"]
     rec, lig, params, opts = golden_inputs(d)

@@ -188,13 +188,15 @@ def cpu_rate(pkg, wl, grid_host, seconds: float, nthreads: int):
     return n / dt, n, dt
 
 
-def timed_result_parity(wl, grid_host, got, m: int, nthreads: int):
+def timed_result_parity(wl, grid_host, got, m: int, nthreads: int, ro=None):
     """Parity of the timed workload's own GPU results (the first m poses)
     against the CPU oracle on the same, device-built grid: the scaled error
     bound of the tests, the share of poses within 1e-4 of the bare relative
     error, the errors of the GPU and of the FP32 oracle against the FP64
     oracle; and the same against the oracle with correctly rounded sin/cos
-    (the C library's sinf/cosf misround a few percent of angles by one ulp)."""
+    (the C library's sinf/cosf misround a few percent of angles by one ulp).
+    ro: the same batch scored in the reference's summation order, compared
+    bit for bit with both oracles."""
     from oracle import pyoracle as po
     d = wl.dofs[:m]
     ref, st = po.energy_6d(wl.rec, wl.lig, grid_host, wl.params, d, stats=True, nthreads=nthreads)
@@ -207,6 +209,13 @@ def timed_result_parity(wl, grid_host, got, m: int, nthreads: int):
     out["max_scaled_err_those_poses"] = po.parity_stats(got[:m][exact], ref[exact], st[exact])["max_scaled_err"]
     vs_x = po.parity_stats(got[:m], ref_x, st)
     out["vs_correctly_rounded_sincos_oracle"] = {k: vs_x[k] for k in ("max_scaled_err", "frac_within_1e-4_bare")}
+    if ro is not None:
+        same = np.all(ro[:m] == ref_x, axis=1)
+        out["reference_order"] = {
+            "bitwise_equal_correctly_rounded_sincos_oracle": bool(same.all()),
+            "poses_bitwise_equal_oracle": int(np.all(ro[:m] == ref, axis=1).sum()),
+            "poses_bitwise_equal_oracle_of_those_with_correctly_rounded_libm_sincos":
+                int(np.all(ro[:m][exact] == ref[exact], axis=1).sum())}
     out["bound"] = "per pose |d| / max(|ref|, 0.05 S) <= 1e-4 for E, force and torque, S = sum of |terms|"
     return out
 
@@ -889,6 +898,7 @@ def main():
     # the same batch summed in the reference CPU path's order (outside the
     # timed region; the timed result is kept in `out` for the parity check)
     reference_order = None
+    ro_result = None
     if not args.kopts & KOPT_REFERENCE_ORDER:
         keep = out.clone()
         ctx.set_kernel_options(args.kopts | KOPT_REFERENCE_ORDER)
@@ -898,6 +908,7 @@ def main():
         ctx.set_kernel_options(args.kopts)
         reference_order = {"evals_per_s": n / (ro_ms / 1000.0), "ms_per_step": ro_ms,
                            "time_ratio": ro_ms / (1000.0 * kavg)}
+        ro_result = out.cpu().numpy()
         out.copy_(keep)
 
     cpu = None
@@ -909,7 +920,7 @@ def main():
         rate, ns, dt = cpu_rate(pkg, wl, gh, args.cpu_seconds, nthreads)
         cpu = {"value": rate, "unit": UNIT, "cores": nthreads, "kind": "port",
                "sample": f"first {ns} poses of the workload ({dt:.1f} s on {nthreads} threads)"}
-        parity = timed_result_parity(wl, gh, out.cpu().numpy(), min(ns, 20000), nthreads)
+        parity = timed_result_parity(wl, gh, out.cpu().numpy(), min(ns, 20000), nthreads, ro_result)
 
     l2_peak = measured_l2_peak() if rank == 0 else None
     minim = None

@@ -274,3 +274,12 @@ def test_modes_minimization_bitwise(pkg, oracle, ctx):
     print(f"config 2 minimization sample, reference order + host sin/cos vs the oracle (libm): {st}")
     for i in ids:
         ctx.release(i)
+
+
+def test_host_sincos_arguments(ctx):
+    """Negative, NaN and too-wide ranges are refused; 0 turns the table off."""
+    from gbattract._lib import GbaError
+    for bad in (-1.0, 5000.0, float("nan")):
+        with pytest.raises(GbaError):
+            ctx.set_host_sincos(bad)
+    ctx.set_host_sincos(0)

@@ -151,8 +151,7 @@ struct MinLaunch {
 	unsigned long long budget_ns;   /* per-warp wall-time budget, 0 = none */
 	unsigned long long* t0;         /* earliest warp start (atomicMin), set to ~0 before launch */
 	unsigned long long* done_ns;    /* per pose completion time (globaltimer), may be nullptr */
-	int ref_order;                  /* GBA_KOPT_REFERENCE_ORDER: the reference's summation order
-	                                   (one warp per pose; no team form) */
+	int ref_order;                  /* GBA_KOPT_REFERENCE_ORDER: the reference's summation order */
 };
 
 cudaError_t launch_minimize_rigid(const MinLaunch& L, int blocks, int threads, cudaStream_t s);
@@ -162,7 +161,7 @@ int minimize_blocks_per_sm(int threads, bool ref_order = false);
  * for bit */
 constexpr int kMaxTeam = 7;
 cudaError_t launch_minimize_rigid_team(const MinLaunch& L, int blocks, int team, cudaStream_t s);
-int minimize_team_blocks_per_sm(int team);
+int minimize_team_blocks_per_sm(int team, bool ref_order = false);
 
 /* multi-pair scoring: one launch over the poses of many pairs */
 struct BatchEnergyLaunch {

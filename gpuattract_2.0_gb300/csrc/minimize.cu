@@ -15,9 +15,8 @@
  *
  * Both kernels sum each pose round-wise (rigid_pose.cuh), as the plain
  * per-step form's scoring launches do, so all three give the same bits.
- * With GBA_KOPT_REFERENCE_ORDER the one-warp kernel sums in the reference
- * CPU path's order instead (eval_pose_rigid_ref) and the team kernel is not
- * used.
+ * With GBA_KOPT_REFERENCE_ORDER both sum in the reference CPU path's order
+ * instead (eval_pose_rigid_ref, eval_pose_rigid_team_ref: the same bits).
  *
  * Small jobs (fewer poses than the GPU has warp slots) run the team kernel
  * instead: a team of G warps evaluates one pose, warp t taking the ligand's
@@ -235,7 +234,8 @@ __device__ __forceinline__ void pipe_consume(const MinLaunch& L, PipeSlot& S, un
  * fresh evaluation to its VA13 -- the FP64 minimizer step, about as long as
  * the evaluation on GB300, runs beside it instead of after it.  Each pose
  * still alternates evaluation and VA13 step exactly as in the other forms. */
-__global__ void __launch_bounds__(256, 4) minimize_rigid_team_kernel(const MinLaunch L) {
+template <bool REF>
+__global__ void __launch_bounds__(256, REF ? 2 : 4) minimize_rigid_team_kernel(const MinLaunch L) {
 	const int G = (blockDim.x >> 5) - 1;
 	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 	WarpStage* stage = reinterpret_cast<WarpStage*>(min_stage_smem);
@@ -265,8 +265,12 @@ __global__ void __launch_bounds__(256, 4) minimize_rigid_team_kernel(const MinLa
 			if (S.active && !S.evaluated) {
 				const RigidModel& M = L.models[L.pair_of ? __ldg(&L.pair_of[S.p]) : 0u];
 				float res[7];
-				eval_pose_rigid_team(M, S.cur[0], S.cur[1], S.cur[2], S.cur[3], S.cur[4], S.cur[5], lane,
-						warp - 1, G, stage, slots, res, 1);
+				if (REF)
+					eval_pose_rigid_team_ref(M, S.cur[0], S.cur[1], S.cur[2], S.cur[3], S.cur[4], S.cur[5], lane,
+							warp - 1, G, stage, res, 1);
+				else
+					eval_pose_rigid_team(M, S.cur[0], S.cur[1], S.cur[2], S.cur[3], S.cur[4], S.cur[5], lane,
+							warp - 1, G, stage, slots, res, 1);
 				if (warp == 1) {
 					if (lane < 7) S.res[lane] = res[lane];
 					__syncwarp();
@@ -295,8 +299,11 @@ cudaError_t launch_minimize_rigid(const MinLaunch& L, int blocks, int threads, c
 }
 
 cudaError_t launch_minimize_rigid_team(const MinLaunch& L, int blocks, int team, cudaStream_t s) {
-	if (team < 1 || team > kMaxTeam || L.ref_order) return cudaErrorInvalidValue;
-	minimize_rigid_team_kernel<<<blocks, 32 * (team + 1), team_smem_bytes(team), s>>>(L);
+	if (team < 1 || team > kMaxTeam) return cudaErrorInvalidValue;
+	if (L.ref_order)
+		minimize_rigid_team_kernel<true><<<blocks, 32 * (team + 1), team_smem_bytes(team), s>>>(L);
+	else
+		minimize_rigid_team_kernel<false><<<blocks, 32 * (team + 1), team_smem_bytes(team), s>>>(L);
 	return cudaGetLastError();
 }
 
@@ -312,7 +319,9 @@ static void allow_minimize_smem() {
 			(int)min_stage_bytes(256));
 	cudaFuncSetAttribute(minimize_rigid_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
 			(int)min_stage_bytes(256));
-	cudaFuncSetAttribute(minimize_rigid_team_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+	cudaFuncSetAttribute(minimize_rigid_team_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+			(int)team_smem_bytes(kMaxTeam));
+	cudaFuncSetAttribute(minimize_rigid_team_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
 			(int)team_smem_bytes(kMaxTeam));
 	cudaGetLastError();
 	if (dev >= 0 && dev < 64) done[dev].store(1);
@@ -330,11 +339,15 @@ int minimize_blocks_per_sm(int threads, bool ref_order) {
 	return nb > 0 ? nb : 1;
 }
 
-int minimize_team_blocks_per_sm(int team) {
+int minimize_team_blocks_per_sm(int team, bool ref_order) {
 	allow_minimize_smem();
 	int nb = 0;
-	cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, minimize_rigid_team_kernel, 32 * (team + 1),
-			team_smem_bytes(team));
+	if (ref_order)
+		cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, minimize_rigid_team_kernel<true>, 32 * (team + 1),
+				team_smem_bytes(team));
+	else
+		cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, minimize_rigid_team_kernel<false>, 32 * (team + 1),
+				team_smem_bytes(team));
 	return nb > 0 ? nb : 1;
 }
 

@@ -44,10 +44,14 @@ struct Placement {
 }  // namespace
 
 int Context::minimize_team(const TuneParams& tp, size_t n, uint32_t lig_rounds) const {
-	/* the reference's order sums bead by bead: one warp per pose */
-	if (kernel_opts & GBA_KOPT_REFERENCE_ORDER) return 1;
 	int team = team_override;
 	if (team == 0 && tp.team > 0 && n <= tp.team_poses) team = tp.team;
+	if (team == 0 && (kernel_opts & GBA_KOPT_REFERENCE_ORDER)) {
+		/* the reference order's double-precision steps keep the FP64 pipe
+		 * busy: teams measured no faster (config 0: 59-73 k poses/s for
+		 * teams of 2-4 against 67 k for one warp per pose) */
+		team = 1;
+	}
 	if (team == 0) {
 		/* fewer poses than the one-warp kernel has resident warps: give each
 		 * pose as many warps as fill them, up to its ligand's rounds */
@@ -71,7 +75,8 @@ MinShape min_shape(const Context& ctx, const TuneParams& tp, size_t n, int team)
 	if (team > 1) {
 		/* team evaluation warps plus a control warp; two poses per block */
 		m.threads = 32 * (team + 1);
-		m.blocks = std::min<size_t>((n + 1) / 2, (size_t)ctx.num_sms * minimize_team_blocks_per_sm(team));
+		m.blocks = std::min<size_t>((n + 1) / 2, (size_t)ctx.num_sms *
+				minimize_team_blocks_per_sm(team, (ctx.kernel_opts & GBA_KOPT_REFERENCE_ORDER) != 0));
 	} else {
 		const int bps = std::min(tp.blocks_per_sm,
 				minimize_blocks_per_sm(m.threads, (ctx.kernel_opts & GBA_KOPT_REFERENCE_ORDER) != 0));

@@ -1098,6 +1098,37 @@ __device__ __forceinline__ void eval_pose_rigid_team(const RigidModel& M, float 
 	if (t == 0) finish_pose(W, res);
 }
 
+/* The reference order by a team of G warps (named barrier bar_id): warp t
+ * evaluates rounds t, t + G, ... into its staging area's bead totals
+ * (eval_round_ref); after each group of G rounds warp 0 adds them to the 13
+ * running sums in round and bead order (ref_accumulate over each warp's
+ * staging area) -- the arithmetic of eval_pose_rigid_ref, bit for bit.
+ * Every warp of the team must call it; res is valid in warp 0. */
+__device__ __forceinline__ void eval_pose_rigid_team_ref(const RigidModel& M, float tx, float ty, float tz,
+		float a0, float a1, float a2, int lane, int t, int G, WarpStage* stages, float res[7], int bar_id) {
+	const int nthreads = 32 * G;
+	WarpStage& W = stages[t];
+	if (t == 0) put_pose(W, pose_rotation(a0, a1, a2, lane, M.trig), tx, ty, tz, lane);
+	group_sync(bar_id, nthreads);
+	if (t != 0) {
+		if (lane < 18) W.pose[lane] = stages[0].pose[lane];
+		__syncwarp();
+	}
+	const uint32_t rounds = (M.lig.n + kBeadsPerRound - 1) / kBeadsPerRound;
+	float acc = 0.f;
+	for (uint32_t r0 = 0; r0 < rounds; r0 += G) {
+		const uint32_t r = r0 + t;
+		if (r < rounds) eval_round_ref(M, r * kBeadsPerRound, lane, W);
+		group_sync(bar_id, nthreads);
+		if (t == 0)
+			for (int u = 0; u < G && r0 + u < rounds; ++u)
+				acc = ref_accumulate(stages[u], min((uint32_t)kBeadsPerRound, M.lig.n - (r0 + u) * kBeadsPerRound),
+						lane, acc);
+		group_sync(bar_id, nthreads);
+	}
+	if (t == 0) finish_ref(acc, W, res);
+}
+
 /* Lanes 0..6 store the 7 result floats (one coalesced 28-byte write). */
 __device__ __forceinline__ void store_result7(float* dst, const float res[7], int lane) {
 	float v = 0.f;

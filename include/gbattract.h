@@ -194,7 +194,7 @@ int gba_set_pose_order(gba_ctx* ctx, int enable);
  *                            native lookups whatever the other options say.
  *                            Slower; applies to gba_energy_6d, the
  *                            noalloc and batch scoring calls, both minimizer
- *                            forms (one warp per pose: no teams), and the
+ *                            forms (teams included), and the
  *                            normal-mode scoring and minimizers
  *                            (CPUEnergyService6DModes,
  *                            src/service/CPUEnergyService6DModes.tpp:121-327;

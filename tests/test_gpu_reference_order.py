@@ -283,3 +283,28 @@ def test_host_sincos_arguments(ctx):
         with pytest.raises(GbaError):
             ctx.set_host_sincos(bad)
     ctx.set_host_sincos(0)
+
+
+def test_team_sizes_in_the_reference_order(pkg, oracle, ctx):
+    """Teams of 2..7 warps per pose (each warp a share of the ligand's 64-bead
+    rounds, the bead totals added in round and bead order by the team's
+    first warp) follow the oracle's trajectories bit for bit, as one warp
+    does.  A 260-bead ligand has five rounds: teams of 2, 3 and 4 split
+    unevenly."""
+    wl = pkg.synth.make_pair(0, 500, 260, 300, (38.0, 46.0), seed=4242)
+    rec, lig, par = ctx.upload_protein(wl.rec), ctx.upload_protein(wl.lig), ctx.upload_params(wl.params)
+    gid = ctx.build_grid(rec, par, pkg.GridOptions())
+    ids = (rec, lig, gid, par)
+    grid = ctx.download_grid(gid)
+    with oracle.exact_sincos():
+        ref = oracle.minimize_6d(wl.rec, wl.lig, grid, wl.params, wl.dofs, 40)
+    try:
+        for team in (1, 2, 3, 4, 5, 7, 0):
+            ctx.set_minimize_team(team)
+            got = ctx.minimize_6d(*ids, wl.dofs, max_evals=40)
+            for a, b in zip(got, ref):
+                assert np.array_equal(a, b), f"team {team}"
+    finally:
+        ctx.set_minimize_team(0)
+    for i in (gid, lig, rec, par):
+        ctx.release(i)

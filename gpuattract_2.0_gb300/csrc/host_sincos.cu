@@ -21,6 +21,7 @@
 #include <cmath>
 #include <cstring>
 #include <string>
+#include <system_error>
 #include <thread>
 #include <vector>
 
@@ -75,16 +76,26 @@ extern "C" int gba_set_host_sincos(gba_ctx* ctx, float max_abs) {
 			std::vector<float2> buf(std::min(chunk, n));
 			for (size_t c0 = 0; c0 < n; c0 += chunk) {
 				const size_t m = std::min(chunk, n - c0);
+				const auto fill = [&](unsigned t) {
+					for (size_t k = m * t / nthreads; k < m * (t + 1) / nthreads; ++k) {
+						const size_t e = c0 + k;
+						const uint32_t b = (e >= half ? 0x80000000u : 0u) | (uint32_t)(lo + e % half);
+						const float a = bits_float(b);
+						buf[k] = make_float2(g_sinf(a), g_cosf(a));
+					}
+				};
+				/* slices 1.. on threads (as many as start), slice 0 and any
+				 * slice whose thread could not start on this one */
 				std::vector<std::thread> pool;
-				for (unsigned t = 0; t < nthreads; ++t)
-					pool.emplace_back([&, t] {
-						for (size_t k = m * t / nthreads; k < m * (t + 1) / nthreads; ++k) {
-							const size_t e = c0 + k;
-							const uint32_t b = (e >= half ? 0x80000000u : 0u) | (uint32_t)(lo + e % half);
-							const float a = bits_float(b);
-							buf[k] = make_float2(g_sinf(a), g_cosf(a));
-						}
-					});
+				std::vector<unsigned> here{0u};
+				for (unsigned t = 1; t < nthreads; ++t) {
+					try {
+						pool.emplace_back(fill, t);
+					} catch (const std::system_error&) {
+						here.push_back(t);
+					}
+				}
+				for (unsigned t : here) fill(t);
 				for (auto& th : pool) th.join();
 				check_cuda(cudaMemcpy((float2*)ctx->trig_table.ptr + c0, buf.data(), m * sizeof(float2),
 						cudaMemcpyHostToDevice), "gba_set_host_sincos: upload");

@@ -956,6 +956,10 @@ def main():
                          "peak_source": peak_kind,
                          "bytes_per_launch": bytes_launch, "kernel_ms_avg": 1000.0 * kernel_avg_s,
                          "kernel_launches_timed": kernel_launches,
+                         # the unique DRAM bytes of one launch (ncu) over the same kernel time
+                         "dram": None if traffic is None else {
+                             "achieved": traffic / kernel_avg_s / 1e9, "peak": peak,
+                             "frac": traffic / kernel_avg_s / 1e9 / peak},
                          "l2": None if l2_peak is None else {
                              "achieved": achieved, "peak": l2_peak, "frac": achieved / l2_peak,
                              "peak_source": "measured in this run: graph of 50 copies of a 2 x 48 MB L2-resident "

@@ -44,9 +44,12 @@ __global__ void __launch_bounds__(256, BOUND4 ? 4 : 1) rigid_energy_kernel(const
 }
 
 /* GBA_KOPT_REFERENCE_ORDER: each pose summed in the reference CPU path's
- * order (eval_pose_rigid_ref).  Compiled for two resident 256-thread blocks
- * per SM: a lane holds a channel's eight corners at once. */
-__global__ void __launch_bounds__(256, 2) rigid_energy_ref_kernel(const RigidLaunch L) {
+ * order (eval_pose_rigid_ref).  Compiled for four resident 256-thread blocks
+ * per SM (64 registers): it spills 152 bytes there, but the latency of its
+ * double-precision chains wants the warps -- config 1 measured 15.4 ms per
+ * 100,000 poses at four blocks, 16.7 ms at three (80 registers) and 20.7 ms
+ * at two (108, no spills). */
+__global__ void __launch_bounds__(256, 4) rigid_energy_ref_kernel(const RigidLaunch L) {
 	__shared__ WarpStage stage[8];
 	const int lane = threadIdx.x & 31;
 	PoseFeed feed(L.next);

@@ -804,16 +804,22 @@ __device__ __forceinline__ void ref_coulomb(float dr2_inv, float dx, float dy, f
 		fx = fy = fz = 0.0f;
 		return;
 	}
+	/* (float)(et2 * (double)d) of two floats is the single-precision product
+	 * (the double product is exact); the distance-dependent 2 et2 likewise
+	 * wherever 2 et2 is finite in single precision */
 	if (cdiel) {
-		const double et2 = (double)fmul(qq, __fsqrt_rn(dr2_inv));
-		fx = (float)__dmul_rn(et2, (double)dx);
-		fy = (float)__dmul_rn(et2, (double)dy);
-		fz = (float)__dmul_rn(et2, (double)dz);
+		const float et2 = fmul(qq, __fsqrt_rn(dr2_inv));
+		fx = fmul(et2, dx); fy = fmul(et2, dy); fz = fmul(et2, dz);
 	} else {
-		const double et2 = __dmul_rn(2.0, (double)fmul(qq, dr2_inv));
-		fx = (float)__dmul_rn(et2, (double)dx);
-		fy = (float)__dmul_rn(et2, (double)dy);
-		fz = (float)__dmul_rn(et2, (double)dz);
+		const float et2 = fmul(2.0f, fmul(qq, dr2_inv));
+		if (isfinite(et2)) {
+			fx = fmul(et2, dx); fy = fmul(et2, dy); fz = fmul(et2, dz);
+		} else {
+			const double d2 = __dmul_rn(2.0, (double)fmul(qq, dr2_inv));
+			fx = (float)__dmul_rn(d2, (double)dx);
+			fy = (float)__dmul_rn(d2, (double)dy);
+			fz = (float)__dmul_rn(d2, (double)dz);
+		}
 	}
 }
 

@@ -442,14 +442,23 @@ def bench_modes(ctx, pkg, n_poses: int, steps: int, minimize: bool = True, with_
                        "time_ratio": e0.elapsed_time(e1) / 1000.0 / launch_s}
     del ro_out
     roof = None
+    parity = None
     if with_cpu:
         roof = modes_roofline(ctx, wl, gr, gl, len(wl.dofs), launch_s)
+        # parity of the scored batch's first 512 poses: FP32 oracle and FP64
+        from oracle import pyoracle as po
+        hr, hl = ctx.download_grid(gr), ctx.download_grid(gl)
+        d512 = np.ascontiguousarray(wl.dofs[:512])
+        ref, st = po.energy_6d_modes(wl.rec, wl.lig, hr, hl, wl.params, d512, stats=True)
+        ref64 = po.energy_6d_modes_f64(wl.rec, wl.lig, hr, hl, wl.params, d512)
+        parity = po.modes_parity_stats(out[:512].cpu().numpy(), ref, st, ref64, wl.rec.n_modes,
+                                       wl.lig.n_modes)
     if not minimize:
         for i in (gr, gl, lig, rec, par):
             ctx.release(i)
         return {"workload": f"config 2{' distributions' if small else ''}: receptor {wl.rec.n} / ligand "
                             f"{wl.lig.n} beads, 5+5 modes; {len(wl.dofs)} poses scored", "energy_evals_per_s": evals,
-                "roofline": roof, "reference_order": reference_order}
+                "roofline": roof, "parity": parity, "reference_order": reference_order}
     sub = wl.dofs
     ctx.minimize_6d_modes(*ids, sub[:64], max_evals=10)
     t0 = time.perf_counter()
@@ -470,7 +479,8 @@ def bench_modes(ctx, pkg, n_poses: int, steps: int, minimize: bool = True, with_
     dt_items = time.perf_counter() - t0
     res = {"workload": f"config 2: receptor {wl.rec.n} / ligand {wl.lig.n} beads, 5+5 modes; "
                        f"{len(wl.dofs)} poses scored, {len(sub)} minimized (maxFunEval {steps})",
-           "energy_evals_per_s": evals, "roofline": roof, "minimize_device_poses_per_s": len(sub) / dt_dev,
+           "energy_evals_per_s": evals, "roofline": roof, "parity": parity,
+           "minimize_device_poses_per_s": len(sub) / dt_dev,
            "minimize_plain_poses_per_s": len(sub) / dt_plain, "speedup": dt_plain / dt_dev,
            "subset_5000_device_poses_per_s": len(few) / dt_dev_few,
            "subset_5000_plain_100_pose_items_poses_per_s": len(few) / dt_items,

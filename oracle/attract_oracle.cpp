@@ -14,6 +14,7 @@
 #include <cmath>
 #include <cstring>
 #include <thread>
+#include <type_traits>
 #include <vector>
 
 namespace {
@@ -586,10 +587,17 @@ void deform_transform(const orc_protein* p, const R* amp, const R m[9], const R 
 	}
 }
 
-template <typename R>
+/* Result_6D_Modes with double fields, for the FP64 evaluation */
+struct result6d_modes_f64 {
+	struct { double E, pos[3], ang[3]; } rigid;
+	double modesRec[GBA_MODES_MAX], modesLig[GBA_MODES_MAX];
+};
+
+template <typename R, typename Res = gba_result6d_modes>
 void eval_modes(const Sys<R>& SR, const Sys<R>& SL, const orc_protein* rec, const orc_protein* lig,
-		const orc_params* par, const gba_dof6d_modes& dof, gba_result6d_modes& res, ModesWork<R>& w,
+		const orc_params* par, const gba_dof6d_modes& dof, Res& res, ModesWork<R>& w,
 		orc_pose_stats* stats) {
+	typedef typename std::remove_reference<decltype(res.rigid.E)>::type T;
 	Stats st{stats};
 	if (stats) std::memset(stats, 0, sizeof(*stats));
 	const R pos[3] = {dof.rigid.pos[0], dof.rigid.pos[1], dof.rigid.pos[2]};
@@ -638,13 +646,13 @@ void eval_modes(const Sys<R>& SR, const Sys<R>& SL, const orc_protein* rec, cons
 	reduce_mode_force<R>(nullptr, w.rfx.data(), w.rfy.data(), w.rfz.data(), rec, modesRec);
 	correct_mode_force<R>(rec->mode_force, rec->n_modes, modesRec);
 	std::memset(&res, 0, sizeof(res));
-	for (unsigned m = 0; m < lig->n_modes; ++m) res.modesLig[m] = (float)modesLig[m];
-	for (unsigned m = 0; m < rec->n_modes; ++m) res.modesRec[m] = (float)modesRec[m];
-	res.rigid.E = (float)E;
-	res.rigid.pos[0] = (float)fx; res.rigid.pos[1] = (float)fy; res.rigid.pos[2] = (float)fz;
+	for (unsigned m = 0; m < lig->n_modes; ++m) res.modesLig[m] = (T)modesLig[m];
+	for (unsigned m = 0; m < rec->n_modes; ++m) res.modesRec[m] = (T)modesRec[m];
+	res.rigid.E = (T)E;
+	res.rigid.pos[0] = (T)fx; res.rigid.pos[1] = (T)fy; res.rigid.pos[2] = (T)fz;
 	R a[3];
 	reduce_torque<R>(lig, w.lfx.data(), w.lfy.data(), w.lfz.data(), ang[0], ang[1], ang[2], a, st);
-	res.rigid.ang[0] = (float)a[0]; res.rigid.ang[1] = (float)a[1]; res.rigid.ang[2] = (float)a[2];
+	res.rigid.ang[0] = (T)a[0]; res.rigid.ang[1] = (T)a[1]; res.rigid.ang[2] = (T)a[2];
 }
 
 /* ------------------------------------------------------------------------ */
@@ -1117,6 +1125,30 @@ int orc_energy_6d_modes(const orc_protein* rec, const orc_protein* lig,
 		w.alloc(rec->n, lig->n);
 		for (size_t p = b; p < e; ++p)
 			eval_modes<float>(SR, SL, rec, lig, par, dofs[p], out[p], w, stats ? stats + p : nullptr);
+	});
+	return GBA_OK;
+}
+
+int orc_energy_6d_modes_f64(const orc_protein* rec, const orc_protein* lig,
+		const orc_grid* grid_rec, const orc_grid* grid_lig, const orc_params* par,
+		const gba_dof6d_modes* dofs, size_t n, double* out27, int nthreads) {
+	if (!rec || !lig || !grid_rec || !grid_lig || !par || (n && (!dofs || !out27)))
+		return GBA_ERR_INVALID_ARGUMENT;
+	if (rec->n_modes > GBA_MODES_MAX || lig->n_modes > GBA_MODES_MAX) return GBA_ERR_INVALID_ARGUMENT;
+	Sys<double> SR, SL;
+	SR.init(grid_rec);
+	SL.init(grid_lig);
+	parallel_for(n, nthreads, [&](int, size_t b, size_t e) {
+		ModesWork<double> w;
+		w.alloc(rec->n, lig->n);
+		for (size_t p = b; p < e; ++p) {
+			result6d_modes_f64 r;
+			eval_modes<double>(SR, SL, rec, lig, par, dofs[p], r, w, nullptr);
+			double* o = out27 + 27 * p;
+			o[0] = r.rigid.E;
+			for (int k = 0; k < 3; ++k) { o[1 + k] = r.rigid.pos[k]; o[4 + k] = r.rigid.ang[k]; }
+			for (int m = 0; m < GBA_MODES_MAX; ++m) { o[7 + m] = r.modesRec[m]; o[17 + m] = r.modesLig[m]; }
+		}
 	});
 	return GBA_OK;
 }

@@ -79,6 +79,12 @@ int orc_energy_6d_modes(const orc_protein* rec, const orc_protein* lig,
 		const gba_dof6d_modes* dofs, size_t n, gba_result6d_modes* out,
 		orc_pose_stats* stats, int nthreads);
 
+/* The normal-mode variant in FP64 throughout; out27 holds the
+ * Result_6D_Modes fields as doubles per pose. */
+int orc_energy_6d_modes_f64(const orc_protein* rec, const orc_protein* lig,
+		const orc_grid* grid_rec, const orc_grid* grid_lig, const orc_params* par,
+		const gba_dof6d_modes* dofs, size_t n, double* out27, int nthreads);
+
 /* VA13 (minfor.f + mc11a.f) driving orc_energy_6d for each pose, one pose
  * per thread.  Reports, per pose, the last evaluated state and objective
  * (what RequestHandler::getResultStates/getResultEnGrads return) and the

@@ -78,7 +78,8 @@ def lib():
         if not ORACLE_LIB.exists():
             raise ImportError(f"oracle not built: {ORACLE_LIB} (make -C oracle)")
         _orc = C.CDLL(str(ORACLE_LIB))
-        for f in ("orc_energy_6d", "orc_energy_6d_f64", "orc_energy_6d_modes", "orc_minimize_6d",
+        for f in ("orc_energy_6d", "orc_energy_6d_f64", "orc_energy_6d_modes", "orc_energy_6d_modes_f64",
+                  "orc_minimize_6d",
                   "orc_minimize_6d_modes", "orc_grid_layout", "orc_grid_build", "orc_grid_nl",
                   "orc_grid_voxels", "orc_pairwise_energy_f64"):
             getattr(_orc, f).restype = C.c_int
@@ -199,6 +200,20 @@ def energy_6d_f64(rec, lig, grid, params, dofs, nthreads: int = 0):
     R, L, G, P = protein_c(rec, k), protein_c(lig, k), grid_c(grid, k), params_c(params, k)
     _check(lib().orc_energy_6d_f64(C.byref(R), C.byref(L), C.byref(G), C.byref(P), _p(dofs),
                                    C.c_size_t(n), _p(out), nthreads), "orc_energy_6d_f64")
+    return out
+
+
+def energy_6d_modes_f64(rec, lig, grid_rec, grid_lig, params, dofs, nthreads: int = 0):
+    """The normal-mode evaluation in FP64 throughout: (n, 27) float64."""
+    k = _Keep()
+    dofs = np.ascontiguousarray(dofs, dtype=np.float32)
+    n = dofs.shape[0]
+    out = np.zeros((n, 27), dtype=np.float64)
+    R, L = protein_c(rec, k), protein_c(lig, k)
+    GR, GL, P = grid_c(grid_rec, k), grid_c(grid_lig, k), params_c(params, k)
+    _check(lib().orc_energy_6d_modes_f64(C.byref(R), C.byref(L), C.byref(GR), C.byref(GL),
+                                         C.byref(P), _p(dofs), C.c_size_t(n), _p(out), nthreads),
+           "orc_energy_6d_modes_f64")
     return out
 
 
@@ -408,6 +423,43 @@ def parity_stats(got, ref, st, ref64=None):
         out.update({"fp64_err_median": float(np.median(g64)), "fp64_err_max": float(g64.max()),
                     "oracle_fp32_fp64_err_median": float(np.median(o64)),
                     "oracle_fp32_fp64_err_max": float(o64.max())})
+    return out
+
+
+def mode_gradient_errors(got, ref, Mr: int, Ml: int) -> np.ndarray:
+    """Per pose (finite in ref) and side, |g - r| / max(|r|, 1e-3 max |r|) of
+    the receptor and ligand mode-gradient vectors (Result_6D_Modes columns
+    7.. and 17..)."""
+    errs = []
+    for lo, M in ((7, Mr), (17, Ml)):
+        g = np.asarray(got, np.float64)[:, lo:lo + M]
+        r = np.asarray(ref, np.float64)[:, lo:lo + M]
+        fin = np.all(np.isfinite(r), axis=1) & np.all(np.isfinite(g), axis=1)
+        g, r = g[fin], r[fin]
+        if len(r) == 0:
+            continue
+        nr = np.linalg.norm(r, axis=1)
+        errs.append(np.linalg.norm(g - r, axis=1) / np.maximum(nr, 1e-3 * nr.max() + 1e-30))
+    return np.concatenate(errs) if errs else np.zeros(1)
+
+
+def modes_parity_stats(got, ref, st, ref64, Mr: int, Ml: int) -> dict:
+    """parity_stats of the rigid part of Result_6D_Modes (energy, force,
+    torque) over the poses finite in the FP32 oracle, plus the mode
+    gradients' errors against the FP32 oracle and of both FP32 results
+    against the FP64 one."""
+    got = np.asarray(got)
+    ref = np.asarray(ref)
+    fin = np.isfinite(ref).all(axis=1) & np.isfinite(got).all(axis=1)
+    out = parity_stats(got[fin, :7], ref[fin, :7], st[fin], np.asarray(ref64)[fin, :7])
+    out["poses_finite"] = int(fin.sum())
+    m32 = mode_gradient_errors(got[fin], ref[fin], Mr, Ml)
+    g64 = mode_gradient_errors(got[fin], np.asarray(ref64)[fin], Mr, Ml)
+    o64 = mode_gradient_errors(ref[fin], np.asarray(ref64)[fin], Mr, Ml)
+    out.update({"mode_grad_max_err": float(m32.max()),
+                "mode_grad_fp64_err_median": float(np.median(g64)), "mode_grad_fp64_err_max": float(g64.max()),
+                "oracle_mode_grad_fp64_err_median": float(np.median(o64)),
+                "oracle_mode_grad_fp64_err_max": float(o64.max())})
     return out
 
 

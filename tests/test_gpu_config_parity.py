@@ -86,14 +86,19 @@ def test_config2_sample(pkg, oracle, ctx):
     hr, hl = ctx.download_grid(gr), ctx.download_grid(gl)
     got = ctx.energy_6d_modes(rec, lig, gr, gl, par, wl.dofs)
     ref, st = oracle.energy_6d_modes(wl.rec, wl.lig, hr, hl, wl.params, wl.dofs, stats=True)
+    ref64 = oracle.energy_6d_modes_f64(wl.rec, wl.lig, hr, hl, wl.params, wl.dofs)
     fin = np.isfinite(ref).all(axis=1)
     assert np.array_equal(np.isfinite(got).all(axis=1), fin)
     assert fin.mean() > 0.99
     stats = oracle.parity_stats(got[fin, :7], ref[fin, :7], st[fin])
     me = mode_errors(got, ref, 5, 5)
-    print("config 2 sample:", stats, f"mode gradients max scaled error {me.max():.2e}")
+    full = oracle.modes_parity_stats(got, ref, st, ref64, 5, 5)
+    print("config 2 sample:", stats, f"mode gradients max scaled error {me.max():.2e}; against FP64: {full}")
     assert stats["max_scaled_err"] <= 1e-4
     assert float(me.max()) <= 1e-4
+    # the GPU is as close to the FP64 evaluation as the FP32 oracle is
+    assert full["fp64_err_max"] <= 2 * full["oracle_fp32_fp64_err_max"] + 1e-5
+    assert full["mode_grad_fp64_err_max"] <= 2 * full["oracle_mode_grad_fp64_err_max"] + 1e-5
     for i in (gr, gl, lig, rec, par):
         ctx.release(i)
 

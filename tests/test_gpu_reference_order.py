@@ -308,3 +308,36 @@ def test_team_sizes_in_the_reference_order(pkg, oracle, ctx):
         ctx.set_minimize_team(0)
     for i in (gid, lig, rec, par):
         ctx.release(i)
+
+
+@pytest.mark.parametrize("potshape,dielec", [(0, 0), (0, 1), (1, 1)])
+def test_force_field_branches(pkg, oracle, ctx, potshape, dielec):
+    """The 12-6 shape, both dielectrics and ipon in {-1, 0, 1, 2} (the
+    synthetic tables use 8-6 and ipon 1): the reference order equals the
+    correctly-rounded oracle bit for bit, the default order stays within the
+    parity bound."""
+    from test_gpu_rigid import pose_errors
+    wl = pkg.synth.make_pair(0, 160, 70, 160, (15.0, 24.0), seed=9191)
+    rng = np.random.default_rng(5)
+    T = wl.params.num_types
+    r0 = rng.uniform(3.0, 5.0, (T, T)).astype(np.float32)
+    eps = rng.uniform(0.1, 10.0, (T, T)).astype(np.float32)
+    ipon = rng.choice(np.array([-1, 0, 1, 2], np.int32), size=(T, T))
+    wl.params.table = pkg.model.attract_params(r0, eps, ipon, potshape)
+    wl.params.potshape = potshape
+    wl.params.dielec = dielec
+    grid = oracle.build_grid(wl.rec, wl.params, pkg.GridOptions())
+    ids = _upload(ctx, wl.rec, wl.lig, grid, wl.params)
+    with oracle.exact_sincos():
+        ref_x, st = oracle.energy_6d(wl.rec, wl.lig, grid, wl.params, wl.dofs, stats=True)
+    assert st["n_pairs"].sum() > 1000
+    assert np.array_equal(ctx.energy_6d(*ids, wl.dofs), ref_x)
+    try:
+        ctx.set_kernel_options(KOPT_DEFAULT)
+        got = ctx.energy_6d(*ids, wl.dofs)
+    finally:
+        ctx.set_kernel_options(KOPT_DEFAULT | KOPT_REFERENCE_ORDER)
+    for e in pose_errors(got, ref_x, st):
+        assert float(e.max()) <= 1e-4
+    for i in ids:
+        ctx.release(i)

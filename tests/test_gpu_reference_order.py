@@ -341,3 +341,23 @@ def test_force_field_branches(pkg, oracle, ctx, potshape, dielec):
         assert float(e.max()) <= 1e-4
     for i in ids:
         ctx.release(i)
+
+
+@pytest.mark.parametrize("n_lig", [1, 63, 64, 65, 129])
+def test_round_boundaries_and_edge_poses(pkg, oracle, ctx, n_lig):
+    """Ligands of one, exactly full and partially filled 64-bead rounds, with
+    non-finite and far-away poses mixed in: bit for bit the oracle's, NaN
+    results included."""
+    wl = pkg.synth.make_pair(0, 140, n_lig, 64, (12.0, 22.0), seed=300 + n_lig)
+    dofs = wl.dofs.copy()
+    dofs[5, 0] = np.nan
+    dofs[9, 4] = np.inf
+    dofs[13] = [500.0, 0.0, 0.0, 0.3, 0.2, 0.1]
+    grid = oracle.build_grid(wl.rec, wl.params, pkg.GridOptions())
+    ids = _upload(ctx, wl.rec, wl.lig, grid, wl.params)
+    got = ctx.energy_6d(*ids, dofs)
+    with oracle.exact_sincos():
+        ref = oracle.energy_6d(wl.rec, wl.lig, grid, wl.params, dofs)
+    assert np.array_equal(got, ref, equal_nan=True)
+    for i in ids:
+        ctx.release(i)

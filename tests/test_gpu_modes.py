@@ -73,6 +73,30 @@ def test_modes_fresh_case_vs_oracle(pkg, oracle, ctx, octets):
     assert float(mode_errors(got, ref, 5, 5).max()) <= 1e-4
 
 
+@pytest.mark.parametrize("n_modes", [8, 10])
+def test_more_than_five_modes(pkg, oracle, ctx, n_modes):
+    """Mode counts above five run the kernels compiled for the full capacity
+    of ten (MODES_MAX, src/model/Types_6D_Config.h:11): scoring against the
+    oracle, and the device minimizer equal to the plain per-step form."""
+    wl = pkg.synth.make_pair(2, 120, 60, 64, (16.0, 24.0), n_modes=n_modes, seed=818 + n_modes)
+    opts = pkg.GridOptions()
+    got, gr, gl = run_modes(ctx, oracle, wl.rec, wl.lig, wl.params, opts, wl.dofs, octets=True)
+    ref, st = oracle.energy_6d_modes(wl.rec, wl.lig, gr, gl, wl.params, wl.dofs, stats=True)
+    fin = np.isfinite(ref).all(axis=1)
+    assert fin.mean() > 0.9
+    for e in pose_errors(got[fin, :7], ref[fin, :7], st[fin]):
+        assert float(e.max()) <= 1e-4
+    assert float(mode_errors(got[fin], ref[fin], n_modes, n_modes).max()) <= 1e-4
+    ids = (ctx.upload_protein(wl.rec), ctx.upload_protein(wl.lig), ctx.upload_grid(gr), ctx.upload_grid(gl),
+           ctx.upload_params(wl.params))
+    s1, r1, n1 = ctx.minimize_6d_modes(*ids, wl.dofs[:32], max_evals=40)
+    s2, r2, n2 = ctx.minimize_6d_modes_plain(*ids, wl.dofs[:32], max_evals=40)
+    assert np.array_equal(n1, n2)
+    assert np.array_equal(r1, r2, equal_nan=True) and np.array_equal(s1, s2, equal_nan=True)
+    for i in ids:
+        ctx.release(i)
+
+
 def test_modes_minimizer_device_plain_and_oracle(pkg, oracle, ctx):
     """Device VA13 over 6 + Mr + Ml DOF == the plain per-step form bit for bit;
     against the CPU oracle's VA13 neither side ends lower more often and the

@@ -361,3 +361,19 @@ def test_round_boundaries_and_edge_poses(pkg, oracle, ctx, n_lig):
     assert np.array_equal(got, ref, equal_nan=True)
     for i in ids:
         ctx.release(i)
+
+
+def test_modes_ten_mode_capacity(pkg, oracle, ctx):
+    """Eight modes per protein (the kernels compiled for ten): scoring and a
+    short minimization equal the correctly-rounded oracle bit for bit."""
+    wl = pkg.synth.make_pair(2, 120, 60, 48, (16.0, 24.0), n_modes=8, seed=826)
+    ids, hr, hl = _modes_ids(ctx, pkg, wl)
+    got = ctx.energy_6d_modes(*ids, wl.dofs)
+    with oracle.exact_sincos():
+        ref = oracle.energy_6d_modes(wl.rec, wl.lig, hr, hl, wl.params, wl.dofs)
+        mref = oracle.minimize_6d_modes(wl.rec, wl.lig, hr, hl, wl.params, wl.dofs[:16], 40)
+    assert np.array_equal(got, ref, equal_nan=True)
+    for a, b in zip(ctx.minimize_6d_modes(*ids, wl.dofs[:16], max_evals=40), mref):
+        assert np.array_equal(a, b, equal_nan=True)
+    for i in ids:
+        ctx.release(i)

@@ -202,7 +202,8 @@ int gba_set_pose_order(gba_ctx* ctx, int enable);
  *                            bead in call scratch); not to gba_census_6d.
  *                            Off by default.
  * The default is the first four.  Changing options drops the cached
- * minimizer graphs. */
+ * minimizer graphs; call it while no other call on the context is in
+ * flight. */
 #define GBA_KOPT_RATIO_COMPUTED 1u
 #define GBA_KOPT_COOP_LOOKUP    2u
 #define GBA_KOPT_FOUR_BLOCKS    4u
@@ -225,7 +226,9 @@ int gba_set_kernel_options(gba_ctx* ctx, uint32_t flags);
  * GBA_KOPT_REFERENCE_ORDER the rigid results then equal the reference's on
  * this host bit for bit.  Applies to every rigid and normal-mode call of the
  * context.  max_abs = 0 turns it off and frees the table; max_abs above 4096
- * is rejected.  No reference counterpart. */
+ * is rejected.  Like gba_set_kernel_options, call it while no other call on
+ * the context is in flight (it replaces data those calls read).  No
+ * reference counterpart. */
 int gba_set_host_sincos(gba_ctx* ctx, float max_abs);
 
 /* While enabled, CUDA events are recorded on the launching stream around

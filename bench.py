@@ -314,6 +314,19 @@ def bench_minimization(ctx, pkg, nthreads: int, with_cpu: bool, kopts: int = 15)
                        f"maxFunEval {steps}",
            "batched_device_poses_per_s": n / dt_dev, "batched_device_s": dt_dev,
            "evals_per_pose_mean": float(n_dev.mean())}
+    # roofline of the batched form: the census bytes of an evaluation (taken
+    # at the start poses) times the evaluations made, plus the VA13 state
+    # traffic, over the wall time -- latency-bound by the VA13 steps' FP64
+    # chains, not by memory
+    cen, _ = ctx.census_6d(*ids, wl.dofs)
+    cen = np.asarray(cen.cpu().numpy() if hasattr(cen, "cpu") else cen, np.int64)
+    b_eval = 52 + 128 * (cen[:, 0].mean() + cen[:, 1].mean()) + 8 * cen[:, 2].mean() + 24 * cen[:, 3].mean()
+    state = 8 * (6 + 21 + 6 * 7)
+    achieved = (b_eval + state) * float(n_dev.sum()) / dt_dev / 1e9
+    peak, kind = measured_peaks()
+    out["roofline"] = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                       "peak_source": kind, "bytes_per_eval": b_eval, "state_bytes_per_step": state,
+                       "evals": int(n_dev.sum())}
     for item, key in ((0, "plain_one_launch_per_round"), (100, "plain_100_pose_items")):
         ctx.minimize_6d_plain(*ids, wl.dofs[:64], max_evals=10, item_size=item)
         t0 = time.perf_counter()

@@ -1473,6 +1473,12 @@ extern "C" {
  * records every evaluated point followed by its f: trace[k*(n+1) + ...].
  * Returns the number of evaluations recorded (at most cap). */
 int orc_minfor_trace(int n, const double* x0, int ivmax, double* trace, int cap) {
+	return orc_minfor_trace_nan(n, x0, ivmax, trace, cap, -1);
+}
+
+/* The same with evaluation nan_eval (0-based; -1: none) handing minfor a NaN
+ * gradient component, as an energy that overflowed does. */
+int orc_minfor_trace_nan(int n, const double* x0, int ivmax, double* trace, int cap, int nan_eval) {
 	if (n < 1 || n > 32 || !x0 || !trace) return -1;
 	double x[33];
 	for (int i = 0; i < n; ++i) x[i + 1] = x0[i];
@@ -1486,6 +1492,7 @@ int orc_minfor_trace(int n, const double* x0, int ivmax, double* trace, int cap)
 			g[i] = g[i] - 400.0 * s[i] * a - 2.0 * b;
 			g[i + 1] = g[i + 1] + 200.0 * a;
 		}
+		if (k == nan_eval) g[1] = std::nan("");
 		if (k < cap) {
 			for (int i = 0; i < n; ++i) trace[(size_t)k * (n + 1) + i] = s[i + 1];
 			trace[(size_t)k * (n + 1) + n] = f;

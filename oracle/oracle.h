@@ -156,6 +156,9 @@ int orc_pairwise_energy_f64(const orc_protein* rec, const orc_protein* lig,
 /* minfor on the extended Rosenbrock function; records each evaluated point
  * and f (test of the library's VA13 state machine). */
 int orc_minfor_trace(int n, const double* x0, int ivmax, double* trace, int cap);
+/* The same with evaluation nan_eval (0-based; -1: none) returning a NaN
+ * gradient component. */
+int orc_minfor_trace_nan(int n, const double* x0, int ivmax, double* trace, int cap, int nan_eval);
 
 #ifdef __cplusplus
 }

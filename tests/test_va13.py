@@ -35,3 +35,23 @@ def test_va13_matches_minfor(harness, oracle, n, ivmax, seed):
     # the minimizer makes progress on Rosenbrock
     fa = a[: ka * (n + 1)].reshape(ka, n + 1)[:, n]
     assert fa.min() < fa[0]
+
+
+@pytest.mark.parametrize("nan_eval", [0, 2, 7])
+def test_va13_matches_minfor_on_nan_gradients(harness, oracle, nan_eval):
+    """A NaN gradient component (an energy that overflowed) sends both
+    implementations down the same branches: max, min and abs follow the C++
+    library's semantics in each."""
+    n, ivmax = 6, 60
+    x0 = np.random.default_rng(11).uniform(-1.5, 1.5, n)
+    cap = ivmax + 2
+    a = np.zeros(cap * (n + 1))
+    b = np.zeros(cap * (n + 1))
+    lib = oracle.lib()
+    lib.orc_minfor_trace_nan.restype = C.c_int
+    ka = lib.orc_minfor_trace_nan(n, C.c_void_p(x0.ctypes.data), ivmax, C.c_void_p(a.ctypes.data), cap,
+                                  nan_eval)
+    kb = harness.va13_trace_nan(n, C.c_void_p(x0.ctypes.data), ivmax, C.c_void_p(b.ctypes.data), cap,
+                                nan_eval)
+    assert ka == kb and ka > nan_eval
+    assert np.array_equal(a[: ka * (n + 1)], b[: kb * (n + 1)], equal_nan=True)

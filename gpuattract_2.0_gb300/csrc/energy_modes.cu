@@ -47,16 +47,36 @@ namespace gba {
 
 namespace {
 
+/* Floats of a bead's mode record held in registers (mode_stride(MM)). */
+template <int MM>
+constexpr int kModeWords = (3 * MM + 3) / 4;
+
+/* The bead's M mode vectors from its 16-byte aligned record v (padded to
+ * whole float4s): one 16-byte load per four floats instead of one load per
+ * float -- the records of a warp's beads lie apart, so every load is a
+ * separate L1 wavefront. */
+template <int MM>
+__device__ __forceinline__ void load_modes(const float* __restrict__ v, uint32_t M, float (&w)[4 * kModeWords<MM>]) {
+	const float4* q = reinterpret_cast<const float4*>(v);
+#pragma unroll
+	for (int k = 0; k < kModeWords<MM>; ++k) {
+		const float4 t = 4 * k < 3 * (int)M ? __ldg(q + k) : make_float4(0.f, 0.f, 0.f, 0.f);
+		w[4 * k] = t.x; w[4 * k + 1] = t.y; w[4 * k + 2] = t.z; w[4 * k + 3] = t.w;
+	}
+}
+
 /* x + sum_m a_m v_m, unfused in mode order (rotate_translate_deform). */
 template <int MM>
 __device__ __forceinline__ void deform(const float* __restrict__ v, uint32_t M, const float* amp,
 		float& x, float& y, float& z) {
+	float w[4 * kModeWords<MM>];
+	load_modes<MM>(v, M, w);
 #pragma unroll
 	for (int m = 0; m < MM; ++m)
 		if (m < (int)M) {
-			x = fadd(x, fmul(amp[m], __ldg(v + 3 * m)));
-			y = fadd(y, fmul(amp[m], __ldg(v + 3 * m + 1)));
-			z = fadd(z, fmul(amp[m], __ldg(v + 3 * m + 2)));
+			x = fadd(x, fmul(amp[m], w[3 * m]));
+			y = fadd(y, fmul(amp[m], w[3 * m + 1]));
+			z = fadd(z, fmul(amp[m], w[3 * m + 2]));
 		}
 }
 
@@ -64,11 +84,12 @@ __device__ __forceinline__ void deform(const float* __restrict__ v, uint32_t M, 
 template <int MM>
 __device__ __forceinline__ void project(const float* __restrict__ v, uint32_t M, float fx, float fy,
 		float fz, float sign, float* acc) {
+	float w[4 * kModeWords<MM>];
+	load_modes<MM>(v, M, w);
 #pragma unroll
 	for (int m = 0; m < MM; ++m)
 		if (m < (int)M)
-			acc[m] = ffma(sign, ffma(fz, __ldg(v + 3 * m + 2), ffma(fy, __ldg(v + 3 * m + 1),
-					fmul(fx, __ldg(v + 3 * m)))), acc[m]);
+			acc[m] = ffma(sign, ffma(fz, w[3 * m + 2], ffma(fy, w[3 * m + 1], fmul(fx, w[3 * m]))), acc[m]);
 }
 
 /* Per warp and round: each staged bead's mode vectors, rotated into the frame
@@ -82,10 +103,12 @@ struct ModeStage {
 template <int MM>
 __device__ __forceinline__ void stage_modes(ModeStage<MM>& S, int s, const float* __restrict__ v, uint32_t M,
 		const float m9[9], bool transpose) {
+	float w[4 * kModeWords<MM>];
+	load_modes<MM>(v, M, w);
 #pragma unroll
 	for (int m = 0; m < MM; ++m)
 		if (m < (int)M) {
-			const float vx = __ldg(v + 3 * m), vy = __ldg(v + 3 * m + 1), vz = __ldg(v + 3 * m + 2);
+			const float vx = w[3 * m], vy = w[3 * m + 1], vz = w[3 * m + 2];
 			float a, b, c;
 			if (transpose) rot_apply_t(m9, vx, vy, vz, a, b, c);
 			else rot_apply(m9, vx, vy, vz, a, b, c);

@@ -344,12 +344,14 @@ int gba_upload_protein(gba_ctx* ctx, uint32_t n, const float* xyz, const uint32_
 	item->dev.xyzq = (const float4*)item->xyzq.ptr;
 	item->dev.tm = (const uint32_t*)item->tm.ptr;
 	if (n_modes > 0) {
-		/* reference layout x[i*M+m] | y | z  ->  device [i][m][axis] */
-		std::vector<float> md((size_t)n_modes * 3 * n);
+		/* reference layout x[i*M+m] | y | z  ->  device [i][m][axis], each
+		 * bead's record padded to mode_stride floats */
+		const size_t ms = mode_stride(n_modes);
+		std::vector<float> md(ms * n, 0.0f);
 		for (uint32_t a = 0; a < 3; ++a)
 			for (uint32_t i = 0; i < n; ++i)
 				for (uint32_t m = 0; m < n_modes; ++m)
-					md[((size_t)i * n_modes + m) * 3 + a] = modes[(size_t)a * n * n_modes + (size_t)i * n_modes + m];
+					md[(size_t)i * ms + (size_t)m * 3 + a] = modes[(size_t)a * n * n_modes + (size_t)i * n_modes + m];
 		item->modes.upload(md.data(), md.size() * sizeof(float));
 		item->dev.modes = (const float*)item->modes.ptr;
 		for (uint32_t m = 0; m < n_modes; ++m) item->dev.mode_force[m] = mode_force[m];
@@ -749,9 +751,9 @@ ModesLaunch Context::modes_launch(gba_id rec, gba_id lig, gba_id grid_rec, gba_i
 	L.trig = trig;
 	L.ref_order = (kernel_opts & GBA_KOPT_REFERENCE_ORDER) ? 1 : 0;
 	L.rec_modes = R->dev.modes;
-	L.rec_ms = 3 * R->dev.n_modes;
+	L.rec_ms = mode_stride(R->dev.n_modes);
 	L.lig_modes = Lg->dev.modes;
-	L.lig_ms = 3 * Lg->dev.n_modes;
+	L.lig_ms = mode_stride(Lg->dev.n_modes);
 	return L;
 }
 

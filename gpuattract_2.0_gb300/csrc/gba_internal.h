@@ -28,9 +28,13 @@ struct DevProtein {
 	uint32_t n_modes;
 	const float4* xyzq;       /* n */
 	const uint32_t* tm;       /* n: type | mapped << 16 */
-	const float* modes;       /* n * 3 * n_modes, [i][m][axis] */
+	const float* modes;       /* n * mode_stride(n_modes), [i][m][axis] */
 	float mode_force[GBA_MODES_MAX];
 };
+
+/* Floats per bead of a device mode array: 3 per mode, padded to whole
+ * float4s so that a bead's vectors load as 16-byte words. */
+constexpr uint32_t mode_stride(uint32_t n_modes) { return (3 * n_modes + 3) & ~3u; }
 
 struct DevIntrpl {
 	uint32_t dimN[3];
@@ -185,7 +189,7 @@ struct ModesLaunch {
 	DevParams par;
 	DevTrig trig;
 	const float* rec_modes;   /* [i][m][axis] */
-	uint32_t rec_ms;          /* floats per receptor bead record (3*Mr) */
+	uint32_t rec_ms;          /* floats per receptor bead record (mode_stride(Mr)) */
 	const float* lig_modes;
 	uint32_t lig_ms;
 	const gba_dof6d_modes* dofs;

@@ -65,12 +65,11 @@ __device__ __forceinline__ void load_modes(const float* __restrict__ v, uint32_t
 	}
 }
 
-/* x + sum_m a_m v_m, unfused in mode order (rotate_translate_deform). */
+/* x + sum_m a_m v_m, unfused in mode order (rotate_translate_deform), with
+ * the bead's vectors w already loaded. */
 template <int MM>
-__device__ __forceinline__ void deform(const float* __restrict__ v, uint32_t M, const float* amp,
+__device__ __forceinline__ void deform_w(const float (&w)[4 * kModeWords<MM>], uint32_t M, const float* amp,
 		float& x, float& y, float& z) {
-	float w[4 * kModeWords<MM>];
-	load_modes<MM>(v, M, w);
 #pragma unroll
 	for (int m = 0; m < MM; ++m)
 		if (m < (int)M) {
@@ -78,6 +77,14 @@ __device__ __forceinline__ void deform(const float* __restrict__ v, uint32_t M, 
 			y = fadd(y, fmul(amp[m], w[3 * m + 1]));
 			z = fadd(z, fmul(amp[m], w[3 * m + 2]));
 		}
+}
+
+template <int MM>
+__device__ __forceinline__ void deform(const float* __restrict__ v, uint32_t M, const float* amp,
+		float& x, float& y, float& z) {
+	float w[4 * kModeWords<MM>];
+	load_modes<MM>(v, M, w);
+	deform_w<MM>(w, M, amp, x, y, z);
 }
 
 /* acc[m] += sign * (f . v_m) */
@@ -99,12 +106,11 @@ struct ModeStage {
 	float w[kBeadsPerRound][3][MM];
 };
 
-/* Rotated mode vectors of slot s: w_m = R v_m (transpose = false) or R^T v_m. */
+/* Rotated mode vectors of slot s: w_m = R v_m (transpose = false) or R^T v_m,
+ * from the bead's loaded vectors w. */
 template <int MM>
-__device__ __forceinline__ void stage_modes(ModeStage<MM>& S, int s, const float* __restrict__ v, uint32_t M,
-		const float m9[9], bool transpose) {
-	float w[4 * kModeWords<MM>];
-	load_modes<MM>(v, M, w);
+__device__ __forceinline__ void stage_modes(ModeStage<MM>& S, int s, const float (&w)[4 * kModeWords<MM>],
+		uint32_t M, const float m9[9], bool transpose) {
 #pragma unroll
 	for (int m = 0; m < MM; ++m)
 		if (m < (int)M) {
@@ -215,9 +221,10 @@ __device__ __forceinline__ void modes_rec_pass(const ModesLaunch& L, const Modes
 			if (j < L.rec.n) {
 				const float4 r = __ldg(&L.rec.xyzq[j]);
 				const uint32_t mapped = __ldg(&L.rec.tm[j]) >> 16;
-				const float* vr = L.rec_modes + (size_t)j * L.rec_ms;
+				float vw[4 * kModeWords<MM>];
+				load_modes<MM>(L.rec_modes + (size_t)j * L.rec_ms, Mr, vw);
 				float x = r.x, y = r.y, z = r.z;
-				deform<MM>(vr, Mr, ampR, x, y, z);
+				deform_w<MM>(vw, Mr, ampR, x, y, z);
 				float px, py, pz;
 				rot_apply(Ri, x, y, z, px, py, pz);
 				px = fadd(px, ipx); py = fadd(py, ipy); pz = fadd(pz, ipz);
@@ -227,7 +234,7 @@ __device__ __forceinline__ void modes_rec_pass(const ModesLaunch& L, const Modes
 				 * projection: (R f) . v = f . (R^T v); staged for the
 				 * cooperative lookups only (one lookup per bead or two: the
 				 * per-lane form rotates f instead) */
-				if (nlk[h] && L.grid_lig.coop_lookup) stage_modes<MM>(MS, s, vr, Mr, R.m, true);
+				if (nlk[h] && L.grid_lig.coop_lookup) stage_modes<MM>(MS, s, vw, Mr, R.m, true);
 			}
 		}
 		const uint32_t n_look = queue_lookups(W, nlk, bg, lane);
@@ -283,9 +290,10 @@ __device__ __forceinline__ void modes_lig_pass(const ModesLaunch& L, const Modes
 				const float4 b = __ldg(&L.lig.xyzq[i]);
 				const uint32_t tm = __ldg(&L.lig.tm[i]);
 				const uint32_t type = tm & 0xffffu, mapped = tm >> 16;
-				const float* vl = L.lig_modes + (size_t)i * L.lig_ms;
+				float vw[4 * kModeWords<MM>];
+				load_modes<MM>(L.lig_modes + (size_t)i * L.lig_ms, Ml, vw);
 				float x = b.x, y = b.y, z = b.z;
-				deform<MM>(vl, Ml, ampL, x, y, z);
+				deform_w<MM>(vw, Ml, ampL, x, y, z);
 				float px, py, pz;
 				rot_apply(R.m, x, y, z, px, py, pz);
 				px = fadd(px, tx); py = fadd(py, ty); pz = fadd(pz, tz);
@@ -295,7 +303,7 @@ __device__ __forceinline__ void modes_lig_pass(const ModesLaunch& L, const Modes
 				if (type != 0) nln[h] = stage_nl(L.grid_rec.nl, px, py, pz, s, W, in_nl);
 				/* the global-frame force f is projected in the ligand frame:
 				 * (R^T f) . v = f . (R v) */
-				if (nlk[h] | nln[h]) stage_modes<MM>(MS, s, vl, Ml, R.m, false);
+				if (nlk[h] | nln[h]) stage_modes<MM>(MS, s, vw, Ml, R.m, false);
 			}
 		}
 		const uint32_t n_look = queue_lookups(W, nlk, bg, lane);

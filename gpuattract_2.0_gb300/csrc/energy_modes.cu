@@ -353,8 +353,9 @@ __device__ __forceinline__ void modes_lig_pass(const ModesLaunch& L, const Modes
 				const uint32_t j = __ldg(&L.grid_rec.nl.list[W.lbase[s] + q]);
 				const float4 r = __ldg(&L.rec.xyzq[j]);
 				float rx = r.x, ry = r.y, rz = r.z;
-				const float* vr = L.rec_modes + (size_t)j * L.rec_ms;
-				deform<MM>(vr, Mr, ampR, rx, ry, rz);
+				float vw[4 * kModeWords<MM>];
+				load_modes<MM>(L.rec_modes + (size_t)j * L.rec_ms, Mr, vw);
+				deform_w<MM>(vw, Mr, ampR, rx, ry, rz);
 				const uint32_t trec = __ldg(&L.rec.tm[j]) & 0xffffu;
 				const float4 b = W.pq[s];
 				const float4 u = W.ut[s];
@@ -364,7 +365,10 @@ __device__ __forceinline__ void modes_lig_pass(const ModesLaunch& L, const Modes
 					continue;
 				S.add(e, fx, fy, fz, u.x, u.y, u.z);
 				/* reaction on receptor bead j is -f: its mode gradient gets -(-f . v) */
-				project<MM>(vr, Mr, fx, fy, fz, 1.f, gR);
+#pragma unroll
+				for (int m = 0; m < MM; ++m)
+					if (m < (int)Mr)
+						gR[m] = ffma(1.f, ffma(fz, vw[3 * m + 2], ffma(fy, vw[3 * m + 1], fmul(fx, vw[3 * m]))), gR[m]);
 				project_staged<MM>(MS, s, Ml, fx, fy, fz, -1.f, gL);
 			}
 		}

@@ -53,6 +53,8 @@ struct PairwiseLaunch {
 	double* g_r0;          /* T*T */
 	double* g_eps;         /* T*T */
 	const float4* tab;     /* 3*T*T: per type pair the constants of lj86 (lj_table_kernel) */
+	const float4* rq;      /* rec.n: receptor x, y, z and this call's charge (pack_receptor_kernel) */
+	const uint32_t* tlist; /* the neighbour list with receptor types in bits 24..31, or nullptr */
 	unsigned long long* next;   /* pose counter, zero at launch (PoseFeed) */
 	const uint32_t* order;      /* visiting order (nearest ligands first), or nullptr */
 };
@@ -115,6 +117,17 @@ const uint32_t* near_first_order(const gba_dof6d* dofs, size_t n, StreamScratch&
 	check_cuda(cub::DeviceRadixSort::SortPairs(base + 4 * a, tmp, kb, ib, (int)n, 16, 32, s),
 			"pairwise order: sort");
 	return ib.Current();
+}
+
+/* rq[j] = (x, y, z, q_rec[j]): a neighbour's position and charge in one
+ * 16-byte gather (the receptor records are read in random order, so every
+ * separate load is its own L1 wavefront). */
+__global__ void pack_receptor_kernel(uint32_t n, const float4* __restrict__ xyzq, const float* __restrict__ q,
+		float4* __restrict__ rq) {
+	for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+		const float4 r = xyzq[j];
+		rq[j] = make_float4(r.x, r.y, r.z, q[j]);
+	}
 }
 
 /* LJ energy, radial force factor and d/d(r0, eps) of one 8-6 pair from the
@@ -228,10 +241,11 @@ __global__ void __launch_bounds__(kPairwiseThreads) pairwise_kernel(const Pairwi
 					const uint32_t q = w0 + 32 * h + lane;
 					if (q >= n_pair) continue;
 					const uint32_t s = so[h];
-					const uint32_t j = __ldg(&L.nl.list[W.lbase[s] + q]);
-					const uint32_t tr = __ldg(&L.rec.tm[j]) & 0xffffu;
+					const uint32_t ent = __ldg(&(L.tlist ? L.tlist : L.nl.list)[W.lbase[s] + q]);
+					const uint32_t j = L.tlist ? ent & 0xffffffu : ent;
+					const uint32_t tr = L.tlist ? ent >> 24 : __ldg(&L.rec.tm[j]) & 0xffffu;
 					if (tr == 0) continue;
-					const float4 r = __ldg(&L.rec.xyzq[j]);
+					const float4 r = __ldg(&L.rq[j]);
 					const float4 b = W.pq[s];
 					const float dx = b.x - r.x, dy = b.y - r.y, dz = b.z - r.z;
 					const float r2 = dx * dx + dy * dy + dz * dz;
@@ -243,7 +257,7 @@ __global__ void __launch_bounds__(kPairwiseThreads) pairwise_kernel(const Pairwi
 					float el, fb, dr0, deps;
 					lj86<BACKWARD>(r2, ir2, L.tab + 3 * (size_t)tp, el, fb, dr0, deps);
 					/* Coulomb, no |q q| switch: smooth in the charges */
-					const float qi = b.w, qj = __ldg(&L.q_rec[j]);
+					const float qi = b.w, qj = r.w;
 					float dd, fcf;
 					if (cdiel) {
 						const float ir = sqrtf(ir2);
@@ -353,6 +367,7 @@ extern "C" int gba_pairwise_6d(gba_ctx* ctx, gba_id rec, gba_id lig, gba_id grid
 			L.rec = R->dev;
 			L.lig = Lg->dev;
 			L.nl = G->dev.nl;
+			L.tlist = ctx->typed_list(*G, rec, *R, true);
 		}
 		L.T = pp->num_types;
 		L.r0 = pp->r0;
@@ -387,6 +402,13 @@ extern "C" int gba_pairwise_6d(gba_ctx* ctx, gba_id rec, gba_id lig, gba_id grid
 			check_cuda(cudaGetLastError(), "pairwise: parameter table");
 		}
 		L.tab = tab;
+		float4* rq = (float4*)scratch.get((size_t)std::max<uint32_t>(L.rec.n, 1) * sizeof(float4), s);
+		if (L.rec.n > 0) {
+			pack_receptor_kernel<<<std::min<uint32_t>((L.rec.n + 255) / 256, 1024), 256, 0, s>>>(L.rec.n, L.rec.xyzq,
+					L.q_rec, rq);
+			check_cuda(cudaGetLastError(), "pairwise: receptor records");
+		}
+		L.rq = rq;
 		const int threads = kPairwiseThreads;
 		const size_t smem = backward ? sizeof(double) * (2 * (size_t)L.T * L.T + L.lig.n + L.rec.n) : 0;
 		if (smem + sizeof(PairStage) * (kPairwiseThreads / 32) > 200 * 1024)

@@ -225,8 +225,8 @@ int gba_set_kernel_options(gba_ctx* ctx, uint32_t flags);
  * faithful library returns; at or beyond max_abs the computed ones.  With
  * GBA_KOPT_REFERENCE_ORDER the rigid results then equal the reference's on
  * this host bit for bit.  Applies to every rigid and normal-mode call of the
- * context.  max_abs = 0 turns it off and frees the table; max_abs above 4096
- * is rejected.  Like gba_set_kernel_options, call it while no other call on
+ * context.  max_abs = 0 (or any value up to 2^-12) turns it off and frees
+ * the table; max_abs above 4096, negative or NaN is rejected.  Like gba_set_kernel_options, call it while no other call on
  * the context is in flight (it replaces data those calls read).  No
  * reference counterpart. */
 int gba_set_host_sincos(gba_ctx* ctx, float max_abs);

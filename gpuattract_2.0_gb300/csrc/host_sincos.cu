@@ -88,6 +88,10 @@ extern "C" int gba_set_host_sincos(gba_ctx* ctx, float max_abs) {
 				 * slice whose thread could not start on this one */
 				std::vector<std::thread> pool;
 				std::vector<unsigned> here{0u};
+				/* reserved before the first thread starts: a vector that grew
+				 * (and failed to) under running threads would end the process */
+				pool.reserve(nthreads);
+				here.reserve(nthreads);
 				for (unsigned t = 1; t < nthreads; ++t) {
 					try {
 						pool.emplace_back(fill, t);

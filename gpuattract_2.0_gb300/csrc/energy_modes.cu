@@ -815,6 +815,10 @@ template <int MM, bool REF>
 __global__ void __launch_bounds__(kModesMinThreads) minimize_modes_kernel(const ModesMinLaunch M) {
 	__shared__ WarpStage stage[kModesMinThreads / 32];
 	ModeStage<MM>* ms = reinterpret_cast<ModeStage<MM>*>(modes_dyn_smem);
+	/* per warp, after the mode staging areas: its pose's VA13 state, which
+	 * every lane of the warp steps (the warp form) */
+	static_assert(sizeof(ModeStage<MM>) % 16 == 0, "VA13 states follow the staging areas");
+	VA13<6 + 2 * MM>* vas = reinterpret_cast<VA13<6 + 2 * MM>*>(ms + kModesMinThreads / 32);
 	const int lane = threadIdx.x & 31;
 	const int wib = threadIdx.x >> 5;
 	const ModesLaunch& L = M.m;
@@ -839,7 +843,7 @@ __global__ void __launch_bounds__(kModesMinThreads) minimize_modes_kernel(const 
 			break;
 		}
 		const size_t p = (size_t)slot;
-		VA13<6 + 2 * MM> va;
+		VA13<6 + 2 * MM>& va = vas[wib];
 		/* lane k holds DOF float k (pos, ang, modesRec[10], modesLig[10]) */
 		float dv = lane < 26 ? __ldg(reinterpret_cast<const float*>(M.start + p) + lane) : 0.f;
 		if (lane == 0) {
@@ -873,21 +877,25 @@ __global__ void __launch_bounds__(kModesMinThreads) minimize_modes_kernel(const 
 			else
 				v = eval_pose_modes<MM>(L, dv, lane, stage[wib], ms[wib]);
 			++nev;
-			/* gather the result record on lane 0 */
-			float res[27];
-#pragma unroll
-			for (int k = 0; k < 27; ++k) res[k] = __shfl_sync(GBA_FULL_MASK, v, k);
-			int done = 0;
-			if (lane == 0) {
-				double g[6 + 2 * MM];
-				for (int k = 0; k < 3; ++k) { g[k] = -(double)res[4 + k]; g[3 + k] = -(double)res[1 + k]; }
-				/* mode entries are gradients already (reduceModeForce) */
-				for (uint32_t m = 0; m < Mr; ++m) g[6 + m] = (double)res[7 + m];
-				for (uint32_t m = 0; m < Ml; ++m) g[6 + Mr + m] = (double)res[17 + m];
-				va.provide((double)res[0], g);
-				done = va.done();
+			/* lane j takes gradient element j from the lane holding its entry
+			 * of the result record: -(ang), -(pos), then the mode entries,
+			 * which are gradients already (reduceModeForce) */
+			const int k = lane - 1;
+			int src = 0;
+			bool neg = false;
+			if (lane >= 1 && lane <= jn) {
+				if (k < 3) { src = 4 + k; neg = true; }
+				else if (k < 6) { src = k - 2; neg = true; }
+				else if (k < 6 + (int)Mr) src = 7 + (k - 6);
+				else src = 17 + (k - 6 - (int)Mr);
 			}
-			if (__shfl_sync(GBA_FULL_MASK, done, 0)) break;
+			const float gv = __shfl_sync(GBA_FULL_MASK, v, src);
+			const double gl = neg ? -(double)gv : (double)gv;
+			const float e = __shfl_sync(GBA_FULL_MASK, v, 0);
+			va.provide_w((double)e, [&](int) { return gl; }, VaWarp{lane});
+			/* lane 0's reading for all: no lane may see a state that lane 0,
+			 * gone on to the next pose, has already restarted */
+			if (__shfl_sync(GBA_FULL_MASK, (int)va.done(), 0)) break;
 			if (nev > M.max_evals + 1) {
 				if (lane == 0) atomicExch(M.status, GBA_ERR_DEVICE_CHECK);
 				break;
@@ -954,9 +962,15 @@ cudaError_t launch_ref_mm(const ModesLaunch& L, int num_sms, cudaStream_t s) {
 	return cudaGetLastError();
 }
 
+/* the minimizer's: staging areas and VA13 states, one each per warp */
+template <int MM>
+size_t min_modes_bytes(int threads) {
+	return (size_t)(threads / 32) * (sizeof(ModeStage<MM>) + sizeof(VA13<6 + 2 * MM>));
+}
+
 template <int MM, bool REF>
 cudaError_t launch_min_mm(const ModesMinLaunch& M, int blocks, int threads, cudaStream_t s) {
-	const size_t dyn = mode_stage_bytes<MM>(threads);
+	const size_t dyn = min_modes_bytes<MM>(threads);
 	cudaError_t e = allow_smem(minimize_modes_kernel<MM, REF>, dyn);
 	if (e != cudaSuccess) return e;
 	minimize_modes_kernel<MM, REF><<<blocks, threads, dyn, s>>>(M);
@@ -965,7 +979,7 @@ cudaError_t launch_min_mm(const ModesMinLaunch& M, int blocks, int threads, cuda
 
 template <int MM, bool REF>
 int min_bps_mm(int threads) {
-	const size_t dyn = mode_stage_bytes<MM>(threads);
+	const size_t dyn = min_modes_bytes<MM>(threads);
 	if (allow_smem(minimize_modes_kernel<MM, REF>, dyn) != cudaSuccess) return 1;
 	int nb = 0;
 	cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, minimize_modes_kernel<MM, REF>, threads, dyn);

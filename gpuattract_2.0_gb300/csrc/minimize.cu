@@ -6,8 +6,10 @@
  * request server to the GPU service (src/apps/em/RequestHandler.tpp:102-216,
  * src/apps/em/VA13Solver.cpp:34-75).  Here the whole loop lives on the GPU:
  * a persistent work-queue kernel in which a warp claims poses from an atomic
- * cursor (any pair of a batch), lane 0 runs the VA13 state machine in FP64
- * and the warp evaluates each requested point with the fused rigid energy;
+ * cursor (any pair of a batch), the warp steps the VA13 state machine in
+ * FP64 (its warp form: element-wise work on lanes, independent divisions
+ * together -- va13.cuh) and evaluates each requested point with the fused
+ * rigid energy;
  * the minimizer state never leaves the SM.  A pose ends after the evaluation
  * budget (maxFunEval, src/apps/em/VA13Solver.h:66) or when minfor returns;
  * per pose the last evaluated DOF and Result and the evaluation count are
@@ -24,8 +26,7 @@
  * totals in order (eval_pose_rigid_team) -- the same bits as one warp doing
  * every round -- so a 200-bead ligand (four rounds) evaluates in about the
  * time of one round.  Each block adds a control warp and holds two poses:
- * while the team evaluates one, the control warp's lane 0 runs the other's
- * VA13 step (FP64, as slow as the evaluation on GB300).
+ * while the team evaluates one, the control warp runs the other's VA13 step.
  *
  * Termination is bounded by construction: every path through the machine
  * either requests an evaluation (nfun <= maxFunEval) or finishes; a pose that
@@ -48,6 +49,16 @@ __device__ __forceinline__ unsigned long long global_ns() {
 	unsigned long long t;
 	asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
 	return t;
+}
+
+/* The Result_6D entry behind VA13 gradient element j (1-based, order (ang
+ * xyz, pos xyz): src/apps/em/meta.h:114-121); 0 outside 1..6.  Selects with
+ * constant indices keep res in registers. */
+__device__ __forceinline__ float rigid_grad_entry(const float res[7], int j) {
+	float v = 0.f;
+#pragma unroll
+	for (int k = 1; k <= 6; ++k) v = j == k ? res[k <= 3 ? k + 3 : k - 3] : v;
+	return v;
 }
 
 /* Lane 0 reads the clock and the whole warp takes its decision. */
@@ -118,15 +129,13 @@ __global__ void __launch_bounds__(256, REF ? 2 : 4) minimize_rigid_kernel(const 
 					eval_pose_rigid<false, true>(M, cur[0], cur[1], cur[2], cur[3], cur[4], cur[5], lane,
 							stage[threadIdx.x >> 5], res, nullptr);
 				++nev;
-				int done = 0;
-				if (lane == 0) {
-					/* objective E, gradient -(ang, pos), src/apps/em/meta.h:114-121 */
-					const double g[6] = {-(double)res[4], -(double)res[5], -(double)res[6],
-							-(double)res[1], -(double)res[2], -(double)res[3]};
-					va.provide((double)res[0], g);
-					done = va.done();
-				}
-				if (__shfl_sync(GBA_FULL_MASK, done, 0)) break;
+				/* objective E, gradient -(ang, pos), src/apps/em/meta.h:114-121;
+				 * the whole warp steps the machine, lane j holding element j */
+				const double gl = -(double)rigid_grad_entry(res, lane);
+				va.provide_w((double)res[0], [&](int) { return gl; }, VaWarp{lane});
+				/* lane 0's reading for all: no lane may see a state that lane 0,
+				 * gone on to the next pose, has already restarted */
+				if (__shfl_sync(GBA_FULL_MASK, (int)va.done(), 0)) break;
 				/* VA13 ends within max_evals + 1 evaluations; anything past that is
 				 * a broken machine, reported instead of looping */
 				if (nev > L.max_evals + 1) {
@@ -192,16 +201,17 @@ __device__ __forceinline__ void pipe_claim(const MinLaunch& L, PipeSlot& S, unsi
 	S.active = 1;
 }
 
-/* Thread 0: hands the evaluation of slot S to its VA13; on the pose's end
- * writes its outputs and refills the slot. */
+/* The control warp, every lane: hands the evaluation of slot S to its VA13
+ * (the warp form); then lane 0 alone (t_start is its own) ends the pose --
+ * outputs written, slot refilled -- or readies its next point. */
 __device__ __forceinline__ void pipe_consume(const MinLaunch& L, PipeSlot& S, unsigned long long t_start,
-		unsigned long long budget) {
+		unsigned long long budget, int lane) {
+	/* objective E, gradient -(ang, pos), src/apps/em/meta.h:114-121 */
+	const double gl = -(double)rigid_grad_entry(S.res, lane);
+	S.va.provide_w((double)S.res[0], [&](int) { return gl; }, VaWarp{lane});
+	if (lane != 0) return;
 	S.evaluated = 0;
 	++S.nev;
-	/* objective E, gradient -(ang, pos), src/apps/em/meta.h:114-121 */
-	const double g[6] = {-(double)S.res[4], -(double)S.res[5], -(double)S.res[6],
-			-(double)S.res[1], -(double)S.res[2], -(double)S.res[3]};
-	S.va.provide((double)S.res[0], g);
 	bool stop = S.va.done();
 	/* VA13 ends within max_evals + 1 evaluations; anything past that is a
 	 * broken machine, reported instead of looping */
@@ -228,12 +238,12 @@ __device__ __forceinline__ void pipe_consume(const MinLaunch& L, PipeSlot& S, un
 	pipe_claim(L, S, t_start, budget);
 }
 
-/* The pipelined team kernel: warp 0 is the control warp (its lane 0 runs
- * VA13), warps 1..G evaluate.  A block holds two poses; in half-step h the
- * evaluators score slot h & 1 while the control lane gives slot h & 1 ^ 1's
- * fresh evaluation to its VA13 -- the FP64 minimizer step, about as long as
- * the evaluation on GB300, runs beside it instead of after it.  Each pose
- * still alternates evaluation and VA13 step exactly as in the other forms. */
+/* The pipelined team kernel: warp 0 is the control warp (it steps VA13),
+ * warps 1..G evaluate.  A block holds two poses; in half-step h the
+ * evaluators score slot h & 1 while the control warp gives slot h & 1 ^ 1's
+ * fresh evaluation to its VA13 -- the FP64 minimizer step runs beside the
+ * evaluation instead of after it.  Each pose still alternates evaluation and
+ * VA13 step exactly as in the other forms. */
 template <bool REF>
 __global__ void __launch_bounds__(256, REF ? 2 : 4) minimize_rigid_team_kernel(const MinLaunch L) {
 	const int G = (blockDim.x >> 5) - 1;
@@ -255,11 +265,10 @@ __global__ void __launch_bounds__(256, REF ? 2 : 4) minimize_rigid_team_kernel(c
 		if (!sh.more[h & 1]) break;
 		const int e = h & 1;
 		if (warp == 0) {
-			if (lane == 0) {
-				PipeSlot& S = sh.slot[e ^ 1];
-				if (S.active && S.evaluated) pipe_consume(L, S, t_start, budget);
-				sh.more[(h + 1) & 1] = sh.slot[0].active | sh.slot[1].active;
-			}
+			PipeSlot& S = sh.slot[e ^ 1];
+			/* lane 0's reading for the warp (lane 0 changes the slot inside) */
+			if (__shfl_sync(GBA_FULL_MASK, (int)(S.active && S.evaluated), 0)) pipe_consume(L, S, t_start, budget, lane);
+			if (lane == 0) sh.more[(h + 1) & 1] = sh.slot[0].active | sh.slot[1].active;
 		} else {
 			PipeSlot& S = sh.slot[e];
 			if (S.active && !S.evaluated) {

@@ -166,6 +166,11 @@ int minimize_blocks_per_sm(int threads, bool ref_order = false);
 constexpr int kMaxTeam = 7;
 cudaError_t launch_minimize_rigid_team(const MinLaunch& L, int blocks, int team, cudaStream_t s);
 int minimize_team_blocks_per_sm(int team, bool ref_order = false);
+/* the solo form: a block of `team` warps per pose (no control warp: warp 0
+ * steps VA13 after each evaluation), for jobs whose poses all fit resident;
+ * same results bit for bit */
+cudaError_t launch_minimize_rigid_solo(const MinLaunch& L, int blocks, int team, cudaStream_t s);
+int minimize_solo_blocks_per_sm(int team, bool ref_order = false);
 
 /* multi-pair scoring: one launch over the poses of many pairs */
 struct BatchEnergyLaunch {

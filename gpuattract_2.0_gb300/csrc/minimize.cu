@@ -290,6 +290,47 @@ __global__ void __launch_bounds__(256, REF ? 2 : 4) minimize_rigid_team_kernel(c
 	}
 }
 
+/* The solo team kernel: a block of G warps holds one pose, evaluates it
+ * (eval_pose_rigid_team: the same bits as the other forms) and then steps
+ * its VA13 on warp 0 while the other warps wait.  A pose's step costs one
+ * evaluation plus one VA13 step; in the pipelined kernel above it costs two
+ * evaluations, since the pose waits for the other slot's.  For jobs in
+ * which every pose gets its own resident block. */
+template <bool REF>
+__global__ void __launch_bounds__(256, REF ? 2 : 4) minimize_rigid_solo_kernel(const MinLaunch L) {
+	const int G = blockDim.x >> 5;
+	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+	WarpStage* stage = reinterpret_cast<WarpStage*>(min_stage_smem);
+	float* slots = reinterpret_cast<float*>(stage + G);
+	PipeSlot& S = *reinterpret_cast<PipeSlot*>(slots + 16 * G);
+	unsigned long long t_start = 0;
+	const unsigned long long budget = L.budget_ns ? L.budget_ns : kMinimizeHardCapNs;
+	if (threadIdx.x == 0) {
+		t_start = global_ns();
+		if (L.t0) atomicMin(L.t0, t_start);
+		pipe_claim(L, S, t_start, budget);
+	}
+	for (;;) {
+		__syncthreads();   /* the slot as thread 0 left it */
+		if (!S.active) break;
+		const RigidModel& M = L.models[L.pair_of ? __ldg(&L.pair_of[S.p]) : 0u];
+		float res[7];
+		/* every warp reads the point before the evaluation's first team
+		 * barrier; warp 0 changes the slot only after its last one */
+		if (REF)
+			eval_pose_rigid_team_ref(M, S.cur[0], S.cur[1], S.cur[2], S.cur[3], S.cur[4], S.cur[5], lane, warp, G,
+					stage, res, 1);
+		else
+			eval_pose_rigid_team(M, S.cur[0], S.cur[1], S.cur[2], S.cur[3], S.cur[4], S.cur[5], lane, warp, G,
+					stage, slots, res, 1);
+		if (warp == 0) {
+			if (lane < 7) S.res[lane] = res[lane];
+			__syncwarp();
+			pipe_consume(L, S, t_start, budget, lane);
+		}
+	}
+}
+
 static size_t min_stage_bytes(int threads) {
 	return (size_t)((threads + 31) / 32) * (sizeof(WarpStage) + sizeof(VA13<6>));
 }
@@ -297,6 +338,11 @@ static size_t min_stage_bytes(int threads) {
 /* shared memory of the team kernel with `team` evaluation warps */
 static size_t team_smem_bytes(int team) {
 	return (size_t)team * (sizeof(WarpStage) + sizeof(float) * 16) + sizeof(PipeShared);
+}
+
+/* shared memory of the solo kernel with `team` warps */
+static size_t solo_smem_bytes(int team) {
+	return (size_t)team * (sizeof(WarpStage) + sizeof(float) * 16) + sizeof(PipeSlot);
 }
 
 cudaError_t launch_minimize_rigid(const MinLaunch& L, int blocks, int threads, cudaStream_t s) {
@@ -316,6 +362,15 @@ cudaError_t launch_minimize_rigid_team(const MinLaunch& L, int blocks, int team,
 	return cudaGetLastError();
 }
 
+cudaError_t launch_minimize_rigid_solo(const MinLaunch& L, int blocks, int team, cudaStream_t s) {
+	if (team < 1 || team > kMaxTeam) return cudaErrorInvalidValue;
+	if (L.ref_order)
+		minimize_rigid_solo_kernel<true><<<blocks, 32 * team, solo_smem_bytes(team), s>>>(L);
+	else
+		minimize_rigid_solo_kernel<false><<<blocks, 32 * team, solo_smem_bytes(team), s>>>(L);
+	return cudaGetLastError();
+}
+
 /* Dynamic shared memory above the 48 KB default (eight one-warp staging
  * areas with their VA13 states need ~53 KB): allowed once per device, before
  * any occupancy query or capture. */
@@ -332,6 +387,10 @@ static void allow_minimize_smem() {
 			(int)team_smem_bytes(kMaxTeam));
 	cudaFuncSetAttribute(minimize_rigid_team_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
 			(int)team_smem_bytes(kMaxTeam));
+	cudaFuncSetAttribute(minimize_rigid_solo_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+			(int)solo_smem_bytes(kMaxTeam));
+	cudaFuncSetAttribute(minimize_rigid_solo_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+			(int)solo_smem_bytes(kMaxTeam));
 	cudaGetLastError();
 	if (dev >= 0 && dev < 64) done[dev].store(1);
 }
@@ -357,6 +416,18 @@ int minimize_team_blocks_per_sm(int team, bool ref_order) {
 	else
 		cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, minimize_rigid_team_kernel<false>, 32 * (team + 1),
 				team_smem_bytes(team));
+	return nb > 0 ? nb : 1;
+}
+
+int minimize_solo_blocks_per_sm(int team, bool ref_order) {
+	allow_minimize_smem();
+	int nb = 0;
+	if (ref_order)
+		cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, minimize_rigid_solo_kernel<true>, 32 * team,
+				solo_smem_bytes(team));
+	else
+		cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, minimize_rigid_solo_kernel<false>, 32 * team,
+				solo_smem_bytes(team));
 	return nb > 0 ? nb : 1;
 }
 

@@ -68,15 +68,24 @@ namespace {
 struct MinShape {
 	int team, threads, chunk;
 	size_t blocks;
+	bool solo;        /* team > 1: one pose per block (all resident), else two */
 };
 
 MinShape min_shape(const Context& ctx, const TuneParams& tp, size_t n, int team) {
-	MinShape m{team, tp.threads, 1, 1};
+	MinShape m{team, tp.threads, 1, 1, false};
 	if (team > 1) {
-		/* team evaluation warps plus a control warp; two poses per block */
-		m.threads = 32 * (team + 1);
-		m.blocks = std::min<size_t>((n + 1) / 2, (size_t)ctx.num_sms *
-				minimize_team_blocks_per_sm(team, (ctx.kernel_opts & GBA_KOPT_REFERENCE_ORDER) != 0));
+		const bool ref = (ctx.kernel_opts & GBA_KOPT_REFERENCE_ORDER) != 0;
+		const size_t solo_cap = (size_t)ctx.num_sms * minimize_solo_blocks_per_sm(team, ref);
+		if (n <= solo_cap) {
+			/* every pose its own block of team warps, all resident */
+			m.solo = true;
+			m.threads = 32 * team;
+			m.blocks = std::max<size_t>(1, n);
+		} else {
+			/* team evaluation warps plus a control warp; two poses per block */
+			m.threads = 32 * (team + 1);
+			m.blocks = std::min<size_t>((n + 1) / 2, (size_t)ctx.num_sms * minimize_team_blocks_per_sm(team, ref));
+		}
 	} else {
 		const int bps = std::min(tp.blocks_per_sm,
 				minimize_blocks_per_sm(m.threads, (ctx.kernel_opts & GBA_KOPT_REFERENCE_ORDER) != 0));
@@ -89,8 +98,10 @@ MinShape min_shape(const Context& ctx, const TuneParams& tp, size_t n, int team)
 }
 
 cudaError_t launch_shape(const MinLaunch& L, const MinShape& m, cudaStream_t s) {
-	return m.team > 1 ? launch_minimize_rigid_team(L, (int)m.blocks, m.team, s)
-	                  : launch_minimize_rigid(L, (int)m.blocks, m.threads, s);
+	if (m.team > 1)
+		return m.solo ? launch_minimize_rigid_solo(L, (int)m.blocks, m.team, s)
+		              : launch_minimize_rigid_team(L, (int)m.blocks, m.team, s);
+	return launch_minimize_rigid(L, (int)m.blocks, m.threads, s);
 }
 
 }  // namespace
@@ -125,7 +136,7 @@ void Context::run_minimize(MinLaunch& L, cudaStream_t s, int32_t* status_out, ui
 	key.p0 = L.max_evals;
 	key.p1 = (int)m.blocks;
 	key.p2 = m.threads;
-	key.p3 = m.chunk | m.team << 16;
+	key.p3 = m.chunk | m.team << 16 | (int)m.solo << 24;
 	key.deadline = L.budget_ns;
 	cudaGraphExec_t exec = nullptr;
 	auto it = graphs.find(key);

@@ -411,7 +411,9 @@ typedef struct {
 	int minimize_threads, minimize_chunk;       /* persistent minimizer: block size, poses per grab */
 	float energy_ms, minimize_ms;               /* best sample times (-1 when taken from the cache) */
 	int from_cache;                             /* bit 0: energy, bit 1: minimize read from cache */
-	int minimize_team;                          /* warps per pose (1, or a team of 2..7 plus a control warp) */
+	int minimize_team;                          /* warps per pose: 1, or a team of 2..7 -- a block per pose
+	                                               when all fit resident, else two poses per block with a
+	                                               control warp (team + 1 warps: minimize_threads) */
 } gba_tune_result;
 
 /* Times candidate launch shapes of the scoring kernel (threads per block x

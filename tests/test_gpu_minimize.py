@@ -131,12 +131,22 @@ def test_team_sizes_give_identical_results(pkg, ctx):
     ctx.grid_octets(gid, True)
     ids = (rec, lig, gid, par)
     ref = ctx.minimize_6d_plain(*ids, wl.dofs, max_evals=40)
+    # more poses than blocks of a team per pose can hold resident (team 2:
+    # at most 32 blocks per SM): the two-pose kernel with a control warp
+    rng = np.random.default_rng(4243)
+    big = wl.dofs[rng.integers(0, len(wl.dofs), 5000)].copy()
+    big[:, :3] += rng.normal(0, 1.0, (5000, 3)).astype(np.float32)
+    ref_big = ctx.minimize_6d_plain(*ids, big, max_evals=12)
     try:
         for team in (1, 2, 3, 4, 5, 7, 0):
             ctx.set_minimize_team(team)
             got = ctx.minimize_6d(*ids, wl.dofs, max_evals=40)
             for a, b in zip(got, ref):
                 assert np.array_equal(a, b), f"team {team}"
+        ctx.set_minimize_team(2)
+        s_b, r_b, n_b = ctx.minimize_6d(*ids, big, max_evals=12)
+        assert np.array_equal(n_b, ref_big[2]), "two-pose team kernel"
+        assert np.array_equal(s_b, ref_big[0], equal_nan=True) and np.array_equal(r_b, ref_big[1], equal_nan=True)
     finally:
         ctx.set_minimize_team(0)
     assert np.array_equal(evaluate_roundwise(ctx, ids, ref[0]), ref[1])

@@ -25,8 +25,11 @@
  * 64-bead rounds t, t + G, ... and the team's first warp adding the round
  * totals in order (eval_pose_rigid_team) -- the same bits as one warp doing
  * every round -- so a 200-bead ligand (four rounds) evaluates in about the
- * time of one round.  Each block adds a control warp and holds two poses:
- * while the team evaluates one, the control warp runs the other's VA13 step.
+ * time of one round.  When every pose of the job gets a block of its own
+ * (all resident), warp 0 steps the pose's VA13 after each evaluation (the
+ * solo kernel); otherwise each block adds a control warp and holds two
+ * poses: while the team evaluates one, the control warp runs the other's
+ * VA13 step.
  *
  * Termination is bounded by construction: every path through the machine
  * either requests an evaluation (nfun <= maxFunEval) or finishes; a pose that

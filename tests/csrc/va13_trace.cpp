@@ -6,30 +6,18 @@
 #include <cmath>
 #include <cstddef>
 #include "../../gpuattract_2.0_gb300/csrc/va13.cuh"
+#include "va13_objectives.h"
 
 namespace {
 
-/* kind 0: extended Rosenbrock; 1: coupled double wells; 2: log wells under a
- * sine of the coordinate sum (nonconvex); 3: a gradient that is not the
- * objective's (drives the machine's failure branches) */
+/* kinds 0, 1, 4, 5: va13_objectives.h (the same bits on the device); 2: log
+ * wells under a sine of the coordinate sum (nonconvex); 3: a gradient that
+ * is not the objective's, through sin and cos */
 double objective(int kind, int n, const double* s, double* g) {
+	if (va13_exact_kind(kind)) return va13_exact_objective(kind, n, s, g);
 	double f = 0.0;
 	for (int i = 0; i < n; ++i) g[i] = 0.0;
-	if (kind == 0) {
-		for (int i = 0; i < n - 1; ++i) {
-			const double a = s[i + 1] - s[i] * s[i], b = 1.0 - s[i];
-			f = f + 100.0 * a * a + b * b;
-			g[i] = g[i] - 400.0 * s[i] * a - 2.0 * b;
-			g[i + 1] = g[i + 1] + 200.0 * a;
-		}
-	} else if (kind == 1) {
-		for (int i = 0; i < n; ++i) {
-			const double a = i + 1.0, u = s[i] * s[i] - 1.0, nx = s[(i + 1) % n];
-			f = f + a * u * u + s[i] * nx;
-			g[i] = g[i] + 4.0 * a * s[i] * u + nx;
-			g[(i + 1) % n] = g[(i + 1) % n] + s[i];
-		}
-	} else if (kind == 2) {
+	if (kind == 2) {
 		double sum = 0.0;
 		for (int i = 0; i < n; ++i) sum = sum + s[i];
 		for (int i = 0; i < n; ++i) {
@@ -86,7 +74,7 @@ extern "C" int va13_trace_nan(int n, const double* x0, int ivmax, double* out, i
 /* either form on objective `kind` (warp != 0: provide_w) */
 extern "C" int va13_trace_form(int n, const double* x0, int ivmax, double* out, int cap, int nan_eval, int kind,
 		int warp) {
-	if (n < 1 || n > 31 || kind < 0 || kind > 3) return -1;
+	if (n < 1 || n > 31 || kind < 0 || kind > 5) return -1;
 	return warp ? trace<31, true>(n, x0, ivmax, out, cap, nan_eval, kind)
 	            : trace<31, false>(n, x0, ivmax, out, cap, nan_eval, kind);
 }

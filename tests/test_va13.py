@@ -66,7 +66,7 @@ def _form_trace(harness, n, x0, ivmax, nan_eval, kind, warp):
     return out[: k * (n + 1)].reshape(k, n + 1)
 
 
-@pytest.mark.parametrize("kind", [0, 1, 2, 3])
+@pytest.mark.parametrize("kind", [0, 1, 2, 3, 4, 5])
 @pytest.mark.parametrize("n", [2, 6, 16, 26, 31])
 def test_warp_form_matches_machine(harness, kind, n):
     """The warp form (provide_w, used by the device minimizers: element-wise

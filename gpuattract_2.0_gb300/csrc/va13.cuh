@@ -7,8 +7,10 @@
  * Instead of calling the energy function, the machine stops whenever minfor
  * would call it: `point()` is the DOF vector to evaluate, `provide(f, g)` hands
  * back the objective and gradient and runs to the next evaluation (or to the
- * end).  The same code runs on the host (plain per-step driver) and inside the
- * persistent device kernel.  Arrays are 1-based, mirroring the Fortran.
+ * end).  The host (plain per-step driver) runs `provide`; the device kernels
+ * run `provide_w`, the same arithmetic spread over a warp's lanes (the warp
+ * form, below), which takes the same trajectory bit for bit.  Arrays are
+ * 1-based, mirroring the Fortran.
  */
 #ifndef GBA_VA13_CUH_
 #define GBA_VA13_CUH_
@@ -21,10 +23,11 @@
 #define GBA_HD inline
 #endif
 
-/* Device loops of the machine stay rolled: lane 0 runs it between two
- * evaluations of the whole warp, and unrolled copies of its loops evicted the
- * evaluation's code from the instruction cache (measured: instruction-fetch
- * stalls; the minimizers ran 7-9 % slower unrolled). */
+/* Device loops of the machine stay rolled: it runs between two evaluations
+ * of the whole warp, and unrolled copies of its loops evicted the
+ * evaluation's code from the instruction cache (measured with one lane
+ * stepping it: instruction-fetch stalls; the minimizers ran 7-9 % slower
+ * unrolled). */
 #ifdef __CUDA_ARCH__
 #define GBA_VA_LOOP _Pragma("unroll 1")
 #else

@@ -357,8 +357,10 @@ int gba_minimize_6d_modes_plain(gba_ctx* ctx, gba_id rec, gba_id lig, gba_id gri
  * fewer poses than the one-warp kernel has resident warps give each pose a
  * team of up to 7 warps, never more than its ligand has 64-bead rounds;
  * 1 = one warp per pose; 2..7 = teams of that many warps (capped by the
- * ligand's rounds), each block adding a control warp that runs one pose's
- * VA13 step while the team evaluates the block's other pose.  The result of
+ * ligand's rounds): a block per pose, whose first warp steps the pose's VA13
+ * after each evaluation, when every pose of the job fits resident that way;
+ * otherwise two poses per block and a control warp that runs one pose's
+ * VA13 step while the team evaluates the other.  The result of
  * every pose is the same bit for bit whatever the setting: the minimizers
  * reduce each 64-bead round on its own and add the rounds in order (the
  * plain per-step form's launches do the same; gba_energy_6d reduces once
